@@ -1,0 +1,424 @@
+#!/usr/bin/env python3
+"""Benchmark of the sparse upper-triangular solve on the large irregular single-RHS system.
+
+Workload (one "step" = one complete solve of U x = b to relative residual <= 1e-12):
+  n = 2,000,000 upper-triangular CSR; per row Poisson(8) off-diagonals, each at i + U{1..64}
+  with probability 0.9 else U{i+1..n-1}; values U[-1,1]; diagonal 1 + sum |off|; FP64;
+  b = U x*, x* ~ U[-1,1]; seed 1 (sptrsv_gb300/gen.py).  Seeded synthetic data.
+
+Reported (one JSON line on rank 0):
+  value        solves/s of the chosen form (FP32 bulk solve + FP64 iterative refinement,
+               schedule from the matrix features), inputs resident in HBM, device time of
+               each step with CUDA events on the solver's stream, L2 flushed between steps;
+  e2e          the same through the public C ABI with pinned host b / x (H2D + solve + D2H
+               inside the timed region of every step);
+  plain_fp64_syncfree  the plain FP64 sync-free GPU solve on the same system (the baseline the
+               chosen form is compared with);
+  roofline     the dominant kernel of the chosen form: its algorithmic bytes per launch over
+               its average launch time (CUDA events between kernels, same steps), against the
+               measured HBM copy bandwidth;
+  cpu_baseline the reference's CPU paths (serial backward substitution, OpenMP level-set on
+               all host cores) timed on this host, best of the two.
+--impl reference runs the reference's CPU implementation (oracle/_ref when it was compiled
+from the reference sources on this host, else the oracle's C restatement) as the arm of
+comparison.  Multi-GPU: replicas (one system per rank, no collective); value sums all ranks.
+"""
+import argparse
+import csv
+import io
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "solves/sec & HBM GB/s: chosen vs plain FP64 sync-free, at rel. resid <=1e-12"
+WORKLOAD = ("irregular-2M: n=2,000,000 upper CSR, Poisson(8) off-diagonals/row, 90% at offset U{1..64}, "
+            "10% uniform to the right, FP64, diag=1+sum|off|, b=U x*, seed 1, single RHS")
+RES_TOL = 1e-12
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=2_000_000)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------------------
+class Dist:
+    def __init__(self):
+        self.ws = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.ws > 1:
+            import torch.distributed as dist
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            dist.init_process_group("gloo")
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, v):
+        if not self.pg:
+            return v
+        import torch
+        t = torch.tensor([float(v)], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during a timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.f.flush()
+        self.f.seek(0)
+        rows = [r for r in csv.reader(io.StringIO(self.f.read())) if len(r) >= 9]
+        os.unlink(self.f.name)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].strip() == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profiled_traffic(kernel):
+    """Per-launch DRAM bytes of `kernel` from the committed ncu summary, when one exists."""
+    p = os.path.join(ROOT, "profiles", "roofline_traffic.txt")
+    try:
+        for line in open(p):
+            parts = line.split()
+            if len(parts) >= 2 and parts[0] == kernel:
+                return float(parts[1])
+    except OSError:
+        pass
+    return None
+
+
+def fp64_bytes(n, nnz, rhs=1):
+    """Algorithmic bytes of one FP64 solve: every entry (value + column index) once, the row
+    pointer once, B read and X written once (x gathers assumed cache-resident)."""
+    return 12 * nnz + 4 * (n + 1) + 16 * n * rhs
+
+
+def jacobi_bytes(n, nnz):
+    """Algorithmic bytes of one FP32 Jacobi sweep: off-diagonal values + columns (8 B each),
+    row pointer, FP32 reciprocal diagonal, r, the previous iterate (read once) and the new
+    iterate (written once)."""
+    return 8 * (nnz - n) + 4 * (n + 1) + 4 * n * 4
+
+
+# ---------------------------------------------------------------------------------------
+def cpu_paths(m, b, budget_s=8.0):
+    """Times the reference's CPU paths on this host; returns a dict with the best."""
+    from oracle import oracle
+    R = oracle.ref()
+    kind = "reference" if R is not None else "port"
+    rpu = m.row_ptr.astype(np.uint64)
+    cores = os.cpu_count() or 1
+    x = np.zeros(m.n)
+    res = {}
+
+    def serial():
+        if R is not None:
+            R.ref_base_gauss_upper(m.n, m.val, rpu, m.col, x, b, 1)
+        else:
+            oracle.lib().orc_base_gauss_upper(m.n, m.val, rpu, m.col, x, b, 1)
+
+    def levelset():
+        if R is not None:
+            R.ref_barrier_upper(m.n, x, b, m.val, m.col, rpu, cores, 1)
+        else:
+            oracle.barrier_upper(rpu, m.col, m.val, b, 1, num_threads=cores)
+
+    for name, fn, threads in (("serial base_gauss_upper", serial, 1), ("level-set barrier_upper", levelset, cores)):
+        fn()
+        t0 = time.perf_counter()
+        reps = 0
+        while True:
+            fn()
+            reps += 1
+            el = time.perf_counter() - t0
+            if reps >= 2 and el >= budget_s / 2 or reps >= 50 or el >= budget_s:
+                break
+        res[name] = {"solves_per_s": reps / el, "threads": threads, "reps": reps}
+    best = max(res, key=lambda k: res[k]["solves_per_s"])
+    return {"value": res[best]["solves_per_s"], "unit": "solves/s", "cores": res[best]["threads"], "kind": kind,
+            "sample": f"{best} on the full system, {res[best]['reps']} solves timed on the host "
+                      f"({os.uname().machine}, {cores} cores); other path: "
+                      + "; ".join(f"{k} {v['solves_per_s']:.3g} solves/s ({v['threads']} thr)" for k, v in res.items()
+                                  if k != best),
+            "paths": res, "best": best, "fn": serial if best.startswith("serial") else levelset}
+
+
+def run_reference(args, dist):
+    if dist.rank != 0:
+        return
+    from sptrsv_gb300 import gen
+    from oracle import oracle
+    oracle.build()
+    m, xs, b = gen.irregular_case(args.n)
+    cb = cpu_paths(m, b, budget_s=4.0)
+    fn = cb.pop("fn")
+    for _ in range(args.warmup):
+        fn()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        fn()
+    el = time.perf_counter() - t0
+    v = args.steps / el
+    cb.pop("paths")
+    cb.pop("best")
+    cb["value"] = v
+    line = {"metric": METRIC, "value": v, "unit": "solves/s", "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "n": m.n, "nnz": m.nnz, "rhs": 1},
+            "cpu_baseline": cb,
+            "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------------------
+def run_ours(args, dist):
+    import sptrsv_gb300 as sp
+    from sptrsv_gb300 import gen
+    L = sp._lib.lib()
+    m, xs, b = gen.irregular_case(args.n)
+    s = sp.Solver(dist.local)
+    s.analyse(m.row_ptr, m.col, m.val)
+    info = s.info()
+    n, nnz = m.n, m.nnz
+    h = s.handle
+    nbytes = 8 * n
+    d_b, d_x = __import__("ctypes").c_void_p(), __import__("ctypes").c_void_p()
+    import ctypes
+    assert L.sptrsv_device_alloc(h, nbytes, ctypes.byref(d_b)) == 0
+    assert L.sptrsv_device_alloc(h, nbytes, ctypes.byref(d_x)) == 0
+    L.sptrsv_copy_h2d(h, d_b, b.ctypes.data, nbytes)
+    assert s.sync() == 0
+
+    chosen = sp.make_opts(precision="mixed", schedule="auto")
+    plain = sp.make_opts(schedule="syncfree_warp")
+
+    def dev_solve(o):
+        rc = L.sptrsv_solve(h, ctypes.byref(o), d_b, d_x, 1, sp.COL_MAJOR)
+        if rc:
+            raise sp.SptrsvError(rc, "solve")
+
+    def timed_steps(o, steps, flush=True):
+        ms = []
+        fms = ctypes.c_float()
+        for _ in range(steps):
+            if flush:
+                L.sptrsv_flush_l2(h)
+            L.sptrsv_timer_begin(h)
+            dev_solve(o)
+            L.sptrsv_timer_end(h, ctypes.byref(fms))
+            ms.append(fms.value)
+        rc = s.sync()
+        if rc:
+            raise sp.SptrsvError(rc, "timed solve")
+        return ms
+
+    # correctness of both forms before timing
+    x = np.empty(n)
+    for o in (chosen, plain):
+        dev_solve(o)
+        rc = s.sync()
+        if rc:
+            raise sp.SptrsvError(rc, "check solve")
+    steps_ref, rel_res = s.last_refine()
+    dev_solve(chosen)
+    assert s.sync() == 0
+    steps_ref, rel_res = s.last_refine()
+    L.sptrsv_copy_d2h(h, x.ctypes.data, d_x, nbytes)
+    assert s.sync() == 0
+    err_xstar = float(np.max(np.abs(x - xs)))
+    if not rel_res <= RES_TOL:
+        raise SystemExit(f"chosen form missed the tolerance: {rel_res}")
+
+    # warm-up + timed region (chosen form)
+    timed_steps(chosen, args.warmup)
+    clocks = Clocks(dist.local)
+    dist.barrier()
+    assert s.sync() == 0
+    clocks.start()
+    l0 = s.launches()
+    ms = timed_steps(chosen, args.steps)
+    l1 = s.launches()
+    ck = clocks.stop()
+    dist.barrier()
+    total_s = dist.max(sum(ms) / 1e3)
+    value = dist.ws * args.steps / total_s
+    gpu_launches = l1 - l0
+
+    # plain FP64 sync-free on the same system
+    psteps = max(3, min(args.steps, 5))
+    timed_steps(plain, 1)
+    pms = timed_steps(plain, psteps)
+    plain_sps = psteps / (sum(pms) / 1e3)
+
+    # per-kernel times of the chosen form (CUDA events between kernels, same steps)
+    s.profile(True)
+    timed_steps(chosen, 1)
+    per_kind = {}
+    prof_steps = max(3, min(args.steps, 10))
+    for _ in range(prof_steps):
+        L.sptrsv_flush_l2(h)
+        dev_solve(chosen)
+        for kind, t in s.profile_read():
+            per_kind.setdefault(kind, []).append(t)
+    s.profile(False)
+    kind_names = {1: "fill", 2: "pull_warp", 3: "pull_thread", 4: "push_csc", 5: "levelset", 6: "init",
+                  7: "residual", 8: "check", 9: "jacobi_sweep", 10: "inner_exact", 11: "axpy", 12: "transpose"}
+    shares = {kind_names.get(k, str(k)): {"launches_per_solve": len(v) / prof_steps, "total_ms_per_solve": sum(v) / prof_steps}
+              for k, v in per_kind.items()}
+    dom_kind = max(per_kind, key=lambda k: sum(per_kind[k]))
+    dom_times = [t for t in per_kind[dom_kind] if t > 0]
+    dom_avg_ms = sum(dom_times) / len(dom_times)
+    if dom_kind == 9:
+        dom_bytes, dom_name = jacobi_bytes(n, nnz), "k_jacobi_v"
+    elif dom_kind == 7:
+        dom_bytes, dom_name = fp64_bytes(n, nnz) - 8 * n, "k_residual_v"
+    else:
+        dom_bytes, dom_name = fp64_bytes(n, nnz), kind_names.get(dom_kind, str(dom_kind))
+    peak, peak_src = measured_peak()
+    achieved = dom_bytes / (dom_avg_ms * 1e-3) / 1e9
+    traffic = profiled_traffic(dom_name)
+
+    # e2e through the C ABI with pinned host buffers
+    hb, hx = ctypes.c_void_p(), ctypes.c_void_p()
+    assert L.sptrsv_host_alloc(h, nbytes, ctypes.byref(hb)) == 0
+    assert L.sptrsv_host_alloc(h, nbytes, ctypes.byref(hx)) == 0
+    ctypes.memmove(hb, b.ctypes.data, nbytes)
+    e2e_ms = []
+    fms = ctypes.c_float()
+    for k in range(args.warmup + args.steps):
+        L.sptrsv_flush_l2(h)
+        L.sptrsv_timer_begin(h)
+        rc = L.sptrsv_solve_host(h, ctypes.byref(chosen), hb, hx, 1, sp.COL_MAJOR)
+        L.sptrsv_timer_end(h, ctypes.byref(fms))
+        if rc:
+            raise sp.SptrsvError(rc, "e2e solve")
+        if k >= args.warmup:
+            e2e_ms.append(fms.value)
+    xe = np.ctypeslib.as_array(ctypes.cast(hx, ctypes.POINTER(ctypes.c_double)), shape=(n,)).copy()
+    assert np.max(np.abs(xe - xs)) <= 1e-8
+    e2e_total = dist.max(sum(e2e_ms) / 1e3)
+    e2e_value = dist.ws * args.steps / e2e_total
+
+    cpu = None
+    if dist.rank == 0 and dist.ws >= 1 and not args.no_cpu_baseline:
+        try:
+            cb = cpu_paths(m, b)
+            cb.pop("fn")
+            cb.pop("paths")
+            cb.pop("best")
+            cpu = cb
+        except Exception as e:  # the baseline is reported, never required
+            cpu = {"value": None, "unit": "solves/s", "error": str(e)[:200]}
+
+    L.sptrsv_host_free(h, hb)
+    L.sptrsv_host_free(h, hx)
+    L.sptrsv_device_free(h, d_b)
+    L.sptrsv_device_free(h, d_x)
+
+    if dist.rank != 0:
+        return
+    ms_step = 1e3 * total_s / args.steps
+    fb = fp64_bytes(n, nnz)
+    line = {
+        "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": dist.ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "n": n, "nnz": nnz, "max_level": info["max_level"], "rhs": 1,
+                   "form": "FP32 Jacobi inner sweeps + FP64 residual/update (iterative refinement), CUDA graph",
+                   "l2": "512 MiB L2 flush between timed steps (outside the events); matrix 206 MB > L2",
+                   "parallelism": f"replicas x{dist.ws}"},
+        "hbm_gbs": fb * value / dist.ws / 1e9,
+        "hbm_frac": fb * value / dist.ws / 1e9 / peak,
+        "rel_residual": rel_res, "refine_steps": steps_ref, "max_abs_err_vs_xstar": err_xstar,
+        "plain_fp64_syncfree": {"solves_per_s": plain_sps, "ms_per_solve": 1e3 / plain_sps,
+                                "hbm_gbs": fb * plain_sps / 1e9},
+        "speedup_vs_plain": value / dist.ws / plain_sps,
+        "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes},
+        "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_source": peak_src, "traffic": traffic,
+                     "algorithmic_bytes_per_launch": dom_bytes, "avg_launch_ms": dom_avg_ms},
+        "kernel_shares": shares,
+        "gpu_launches": gpu_launches,
+        "clocks": ck,
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    dist = Dist()
+    try:
+        if args.impl == "reference":
+            run_reference(args, dist)
+        else:
+            run_ours(args, dist)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,159 @@
+/*
+ * sptrsv_gb300.h -- C ABI of the GB300 sparse upper-triangular solver.
+ *
+ * Plain C types only (no CUDA or torch types), so that ctypes, cgo, JNI or any C caller can
+ * bind it.  Two layers:
+ *   1. the reference's own entry points, re-implemented on the GPU with identical C++
+ *      signatures: include/core.h and include/sptrsv_syncfree_opencl.h;
+ *   2. the handle API below, which keeps one matrix and its analysis resident on the
+ *      device, solves many right-hand sides against it, and exposes the schedules.
+ *
+ * Matrix convention (the reference's, core.cpp:18-32): CSR of an upper-triangular U, the
+ * diagonal FIRST in every row, every other column index in (i, n).  Values FP64.
+ * Errors: every function returns an sptrsv_status (0 = success, negative = failure); the
+ * reference-signature functions return the negative status cast to double instead of
+ * their elapsed seconds, and never exit the process.
+ */
+#ifndef SPTRSV_GB300_H
+#define SPTRSV_GB300_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifndef SPTRSV_API
+#define SPTRSV_API __attribute__((visibility("default")))
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  -1 keeps the reference's "not a square matrix" return
+ * (sptrsv_syncfree_opencl.cpp:17-21). */
+enum sptrsv_status {
+    SPTRSV_OK = 0,
+    SPTRSV_ERR_NOT_SQUARE = -1,
+    SPTRSV_ERR_INVALID_ARG = -2,
+    SPTRSV_ERR_CUDA = -3,
+    SPTRSV_ERR_ROW_PTR = -4,        /* row pointer not monotone, or does not start at 0 */
+    SPTRSV_ERR_MISSING_DIAG = -5,   /* a row is empty or its first entry is not the diagonal */
+    SPTRSV_ERR_NOT_UPPER = -6,      /* an off-diagonal entry at or left of the diagonal */
+    SPTRSV_ERR_COL_RANGE = -7,      /* a column index >= n */
+    SPTRSV_ERR_ZERO_PIVOT = -8,     /* a zero or non-finite diagonal */
+    SPTRSV_ERR_TIMEOUT = -9,        /* a device wait ran out of its budget */
+    SPTRSV_ERR_NOT_CONVERGED = -10, /* refinement stopped above its tolerance */
+    SPTRSV_ERR_TOO_LARGE = -11,     /* nnz >= 2^31 or a size above a fixed maximum */
+    SPTRSV_ERR_NO_DEVICE = -12,
+    SPTRSV_ERR_NO_ANALYSIS = -13,   /* solve before analyse */
+    SPTRSV_ERR_SUPERNODES = -14,    /* supernode partition inconsistent with the matrix */
+    SPTRSV_ERR_UNSUPPORTED = -15
+};
+
+/* Solve schedules (kernel families). */
+enum sptrsv_schedule {
+    SPTRSV_SCHED_AUTO = 0,          /* pick from the matrix features */
+    SPTRSV_SCHED_SYNCFREE_WARP = 1, /* CSR pull, warps per row, self-flagging x, bounded spins */
+    SPTRSV_SCHED_SYNCFREE_THREAD = 2, /* CSR pull, one lane per row (kernel_full3.cl family) */
+    SPTRSV_SCHED_SYNCFREE_CSC = 3,  /* CSC push with per-row in-degree counters (kernel_full.cl family) */
+    SPTRSV_SCHED_LEVELSET = 4,      /* persistent kernel, one grid barrier per level */
+    SPTRSV_SCHED_JACOBI = 5,        /* iterative sweeps x <- D^-1 (b - N x); mixed precision only */
+    SPTRSV_SCHED_SUPERNODAL = 6     /* dense supernode blocks on tensor cores */
+};
+
+enum sptrsv_precision {
+    SPTRSV_PREC_FP64 = 0,   /* direct FP64 solve */
+    SPTRSV_PREC_MIXED = 1   /* FP32 inner solves + FP64 residual / update (iterative refinement) */
+};
+
+enum sptrsv_layout {
+    SPTRSV_COL_MAJOR = 0,   /* x[i + r*n]  (core.h solvers, core.cpp:26-28) */
+    SPTRSV_ROW_MAJOR = 1    /* x[i*rhs + r] (sptrsv_syncfree_opencl, kernel_full.cl:163) */
+};
+
+/* Kernel steps reported by sptrsv_profile_read. */
+enum sptrsv_kernel_kind {
+    SPTRSV_K_FILL = 1,         /* x <- pending sentinel */
+    SPTRSV_K_PULL_WARP = 2,    /* sync-free CSR pull, warps per row */
+    SPTRSV_K_PULL_THREAD = 3,  /* sync-free CSR pull, one lane per row */
+    SPTRSV_K_PUSH_CSC = 4,     /* sync-free CSC push */
+    SPTRSV_K_LEVELSET = 5,     /* persistent level-set kernel */
+    SPTRSV_K_INIT = 6,         /* refinement set-up (x = 0, ||b||) */
+    SPTRSV_K_RESIDUAL = 7,     /* r = b - U x in FP64 */
+    SPTRSV_K_CHECK = 8,        /* convergence test */
+    SPTRSV_K_JACOBI = 9,       /* FP32 Jacobi sweep */
+    SPTRSV_K_INNER = 10,       /* exact FP32 inner solve */
+    SPTRSV_K_AXPY = 11,        /* x += d */
+    SPTRSV_K_TRANSPOSE = 12    /* column-major <-> row-major */
+};
+
+typedef struct sptrsv_opts {
+    int schedule;           /* enum sptrsv_schedule */
+    int precision;          /* enum sptrsv_precision */
+    int rows_per_warp;      /* SYNCFREE_WARP: 1, 2, 4, 8 (lanes per row = 32 / rows_per_warp) */
+    int rhs_tile;           /* columns handled per warp pass (0 = min(rhs, 32)) */
+    int inner;              /* MIXED: inner FP32 schedule (enum sptrsv_schedule) */
+    int inner_sweeps;       /* MIXED + JACOBI: sweeps per refinement step */
+    int max_refine;         /* MIXED: maximum refinement steps */
+    double tol;             /* MIXED: target ||b - U x||_2 / ||b||_2 */
+    int64_t spin_budget_ns; /* per-wait limit of every device spin (0 = 2 s) */
+} sptrsv_opts;
+
+typedef struct sptrsv_ctx* sptrsv_handle;
+
+/* Fill *o with the defaults (AUTO schedule, FP64, tol 1e-12, 2 s spin budget). */
+SPTRSV_API void sptrsv_default_opts(sptrsv_opts* o);
+SPTRSV_API const char* sptrsv_status_string(int status);
+/* Status of the last reference-signature call made on this host thread. */
+SPTRSV_API int sptrsv_last_status(void);
+
+SPTRSV_API int sptrsv_create(sptrsv_handle* out, int device);
+SPTRSV_API int sptrsv_destroy(sptrsv_handle h);
+
+/* Upload a host CSR (int64 row pointer) and analyse it: validation, in-degree, levels,
+ * level buckets, FP32 copy and reciprocal diagonal.  Replaces the setup and analyser
+ * stages of sptrsv_syncfree_opencl.cpp:96-267. */
+SPTRSV_API int sptrsv_analyse_host(sptrsv_handle h, int n, int64_t nnz, const int64_t* row_ptr, const int* col,
+                        const double* val);
+/* Same on caller-owned device arrays (int32 row pointer); the handle keeps the pointers. */
+SPTRSV_API int sptrsv_analyse_device(sptrsv_handle h, int n, int nnz, const int* d_row_ptr, const int* d_col,
+                          const double* d_val);
+
+/* Analysis results copied to host memory. */
+SPTRSV_API int sptrsv_info(sptrsv_handle h, int* n, int* nnz, int* max_level);
+SPTRSV_API int sptrsv_get_levels(sptrsv_handle h, uint64_t* levels);       /* core.cpp:244-270 values */
+SPTRSV_API int sptrsv_get_in_degree(sptrsv_handle h, int* in_degree);      /* kernel_full.cl:40-52 values */
+SPTRSV_API int sptrsv_get_level_buckets(sptrsv_handle h, int* level_ptr, int* level_rows); /* core.cpp:282-288 */
+SPTRSV_API int sptrsv_get_level_tasks(sptrsv_handle h, int num_threads, int* tasks);      /* core.cpp:289-332 */
+
+/* Solve U X = B with device-resident B and X (rhs columns, layout enum sptrsv_layout),
+ * enqueued on the handle's stream.  Returns after the enqueue; the device status is read by
+ * sptrsv_sync. */
+SPTRSV_API int sptrsv_solve(sptrsv_handle h, const sptrsv_opts* o, const double* d_b, double* d_x, int rhs, int layout);
+/* Same with host B and X: H2D, solve, D2H on the handle's stream, then synchronise. */
+SPTRSV_API int sptrsv_solve_host(sptrsv_handle h, const sptrsv_opts* o, const double* b, double* x, int rhs, int layout);
+/* Wait for the handle's stream; returns the first device error of the enqueued work. */
+SPTRSV_API int sptrsv_sync(sptrsv_handle h);
+/* Refinement steps and final relative residual of the last MIXED solve (after sync). */
+SPTRSV_API int sptrsv_last_refine(sptrsv_handle h, int* steps, double* rel_residual);
+
+/* Device and pinned-host memory, copies and timing on the handle's stream. */
+SPTRSV_API int sptrsv_device_alloc(sptrsv_handle h, size_t bytes, void** ptr);
+SPTRSV_API int sptrsv_device_free(sptrsv_handle h, void* ptr);
+SPTRSV_API int sptrsv_host_alloc(sptrsv_handle h, size_t bytes, void** ptr); /* pinned */
+SPTRSV_API int sptrsv_host_free(sptrsv_handle h, void* ptr);
+SPTRSV_API int sptrsv_copy_h2d(sptrsv_handle h, void* dst, const void* src, size_t bytes);
+SPTRSV_API int sptrsv_copy_d2h(sptrsv_handle h, void* dst, const void* src, size_t bytes);
+SPTRSV_API int sptrsv_timer_begin(sptrsv_handle h);
+SPTRSV_API int sptrsv_timer_end(sptrsv_handle h, float* ms);     /* synchronises */
+SPTRSV_API int sptrsv_flush_l2(sptrsv_handle h);                 /* writes 512 MiB of scratch */
+SPTRSV_API int64_t sptrsv_kernel_launches(sptrsv_handle h);      /* kernels this handle has launched */
+SPTRSV_API int sptrsv_device_sm_count(sptrsv_handle h);
+/* Record a CUDA event after every kernel step of later solves (also inside their graphs). */
+SPTRSV_API int sptrsv_profile_enable(sptrsv_handle h, int enable);
+/* After a profiled solve: per-step kinds (enum sptrsv_kernel_kind) and device times in ms, in
+ * launch order; returns the number of steps written (at most cap).  Synchronises. */
+SPTRSV_API int sptrsv_profile_read(sptrsv_handle h, int* kinds, float* ms, int cap);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

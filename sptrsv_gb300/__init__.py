@@ -1,0 +1,246 @@
+"""sptrsv_gb300 -- GPU sparse upper-triangular solver for the GB300 (sm_103a).
+
+Python front end of libsptrsv_gb300.so.  Two layers, both straight onto the C ABI:
+
+* the reference's interface (xnd-r/SPTRSV include/core.h:10-19 and
+  include/sptrsv_syncfree_opencl.h:11-37): the same function names, argument order and
+  meaning, on numpy arrays, returning elapsed seconds (negative status on failure);
+* ``Solver``: a handle that keeps one matrix and its analysis on the device and solves many
+  right-hand sides, with every schedule (sync-free warp / thread / CSC push, level-set,
+  FP32 + FP64 refinement) selectable.
+
+All numerical work happens in the CUDA kernels; nothing here computes a solution.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import Opts
+
+SCHED = {"auto": 0, "syncfree_warp": 1, "syncfree_thread": 2, "syncfree_csc": 3, "levelset": 4, "jacobi": 5,
+         "supernodal": 6}
+PREC = {"fp64": 0, "mixed": 1}
+COL_MAJOR, ROW_MAJOR = 0, 1
+
+
+class SptrsvError(RuntimeError):
+    def __init__(self, status, what=""):
+        self.status = status
+        msg = _lib.lib().sptrsv_status_string(status).decode()
+        super().__init__(f"{what}: status {status} ({msg})" if what else f"status {status} ({msg})")
+
+
+def _check(rc, what=""):
+    if rc != 0:
+        raise SptrsvError(rc, what)
+
+
+def status_string(s):
+    return _lib.lib().sptrsv_status_string(int(s)).decode()
+
+
+def last_status():
+    return _lib.lib().sptrsv_last_status()
+
+
+def make_opts(schedule="auto", precision="fp64", rows_per_warp=None, rhs_tile=None, inner="auto", inner_sweeps=None,
+              max_refine=None, tol=None, spin_budget_ns=None):
+    """struct sptrsv_opts from sptrsv_default_opts, with the given fields replaced."""
+    o = Opts()
+    _lib.lib().sptrsv_default_opts(ctypes.byref(o))
+    o.schedule = SCHED[schedule] if isinstance(schedule, str) else int(schedule)
+    o.precision = PREC[precision] if isinstance(precision, str) else int(precision)
+    o.inner = SCHED[inner] if isinstance(inner, str) else int(inner)
+    for name, v in (("rows_per_warp", rows_per_warp), ("rhs_tile", rhs_tile), ("inner_sweeps", inner_sweeps),
+                    ("max_refine", max_refine), ("tol", tol), ("spin_budget_ns", spin_budget_ns)):
+        if v is not None:
+            setattr(o, name, v)
+    return o
+
+
+def _c(a, dt):
+    return np.ascontiguousarray(a, dtype=dt)
+
+
+# --------------------------------------------------------------------------------------
+# The reference interface (core.h / sptrsv_syncfree_opencl.h).  Arrays are numpy; outputs
+# are written into the caller's arrays, as in the reference.
+
+def base_gauss_upper(n, val, row_index, col, x, b, rhs):
+    """core.h:10 -- x = U^{-1} b; CSR (uint64 row_index, diagonal first), X/B column-major."""
+    return _lib.dropin("base_gauss_upper")(n, val, row_index, col, x, b, rhs)
+
+
+def base_gauss_upper_new(n, val, row_index, col, x, b, rhs):
+    """core.h:11."""
+    return _lib.dropin("base_gauss_upper_new")(n, val, row_index, col, x, b, rhs)
+
+
+def supernodal_upper(sn, supernodes, x, val, row, col_index, n, rhs):
+    """core.h:12 -- in place: x holds b on entry.  `row` = CSR columns, `col_index` = uint64 row pointer."""
+    return _lib.dropin("supernodal_upper")(sn, supernodes, x, val, row, col_index, n, rhs)
+
+
+def supernodal_upper_new(sn, supernodes, x, val, row, col_index, n, rhs):
+    """core.h:13."""
+    return _lib.dropin("supernodal_upper_new")(sn, supernodes, x, val, row, col_index, n, rhs)
+
+
+def supernodal_blas_upper(n, nz, sn, supernodes, x, val, col_index, row, rhs):
+    """core.h:14 -- padded format: val_pad, uint64 padded columns, int padded row pointer."""
+    return _lib.dropin("supernodal_blas_upper")(n, nz, sn, supernodes, x, val, col_index, row, rhs)
+
+
+def supernodal_blas_upper_new(n, nz, sn, supernodes, x, val, col_index, row, rhs):
+    """core.h:15."""
+    return _lib.dropin("supernodal_blas_upper_new")(n, nz, sn, supernodes, x, val, col_index, row, rhs)
+
+
+def ccs2ccs_pad(val, row, col_index, val_pad, col_index_pad, row_pad, nodes, sn, nnz):
+    """core.h:16 -- `sn` and `nnz` are ctypes.c_int (passed by reference, as int& there)."""
+    return _lib.dropin("ccs2ccs_pad")(val, row, col_index, val_pad, col_index_pad, row_pad, nodes,
+                                      ctypes.byref(sn), ctypes.byref(nnz))
+
+
+def setLevelUpAndGetMaxLevel(n, col, row_index, levelsUp):  # noqa: N802 (reference name)
+    """core.h:17 -- fills uint64 levelsUp, returns the largest level."""
+    return _lib.dropin("setLevelUpAndGetMaxLevel")(n, col, row_index, levelsUp)
+
+
+def barrier_upper(n, x, b, val, col, row, num_of_threads, rhs):
+    """core.h:18 -- level-set solve (the GPU ignores num_of_threads)."""
+    return _lib.dropin("barrier_upper")(n, x, b, val, col, row, num_of_threads, rhs)
+
+
+def barrier_upper_new(n, x, b, val, col, row, num_of_threads, rhs):
+    """core.h:19."""
+    return _lib.dropin("barrier_upper_new")(n, x, b, val, col, row, num_of_threads, rhs)
+
+
+def sptrsv_syncfree_opencl(cscColPtr, cscRowIdx, cscVal, m, n, nnz, x, b, rhs):  # noqa: N803
+    """sptrsv_syncfree_opencl.h:11-19 -- CSC (diagonal last), X/B row-major."""
+    return _lib.dropin("sptrsv_syncfree_opencl")(cscColPtr, cscRowIdx, cscVal, m, n, nnz, x, b, rhs)
+
+
+def sptrsv_syncfree2_opencl(cscColPtr, cscRowIdx, cscVal, m, n, nnz, x, b):  # noqa: N803
+    """sptrsv_syncfree_opencl.h:21-28."""
+    return _lib.dropin("sptrsv_syncfree2_opencl")(cscColPtr, cscRowIdx, cscVal, m, n, nnz, x, b)
+
+
+def sptrsv_syncfree3_opencl(csrColIdx, csrRowPtr, csrVal, m, n, nnz, x, b):  # noqa: N803
+    """sptrsv_syncfree_opencl.h:30-37 -- CSR (diagonal first), one lane per row."""
+    return _lib.dropin("sptrsv_syncfree3_opencl")(csrColIdx, csrRowPtr, csrVal, m, n, nnz, x, b)
+
+
+# --------------------------------------------------------------------------------------
+class Solver:
+    """One device-resident matrix U (CSR, diagonal first) and its analysis."""
+
+    def __init__(self, device=0):
+        self._h = ctypes.c_void_p()
+        _check(_lib.lib().sptrsv_create(ctypes.byref(self._h), device), "sptrsv_create")
+        self.n = 0
+        self.nnz = 0
+
+    def close(self):
+        if self._h:
+            _lib.lib().sptrsv_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    def analyse(self, row_ptr, col, val):
+        rp = _c(row_ptr, np.int64)
+        n = len(rp) - 1
+        _check(_lib.lib().sptrsv_analyse_host(self._h, n, int(rp[-1]), rp, _c(col, np.int32), _c(val, np.float64)),
+               "analyse")
+        self.n, self.nnz = n, int(rp[-1])
+        return self
+
+    def analyse_device(self, n, nnz, d_row_ptr, d_col, d_val):
+        _check(_lib.lib().sptrsv_analyse_device(self._h, n, nnz, d_row_ptr, d_col, d_val), "analyse_device")
+        self.n, self.nnz = n, nnz
+        return self
+
+    def info(self):
+        n, nnz, ml = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        _check(_lib.lib().sptrsv_info(self._h, ctypes.byref(n), ctypes.byref(nnz), ctypes.byref(ml)), "info")
+        return {"n": n.value, "nnz": nnz.value, "max_level": ml.value}
+
+    def levels(self):
+        out = np.zeros(self.n, dtype=np.uint64)
+        _check(_lib.lib().sptrsv_get_levels(self._h, out), "levels")
+        return out
+
+    def in_degree(self):
+        out = np.zeros(self.n, dtype=np.int32)
+        _check(_lib.lib().sptrsv_get_in_degree(self._h, out), "in_degree")
+        return out
+
+    def level_buckets(self):
+        ml = self.info()["max_level"]
+        ptr = np.zeros(ml + 2, dtype=np.int32)
+        rows = np.zeros(self.n, dtype=np.int32)
+        _check(_lib.lib().sptrsv_get_level_buckets(self._h, ptr, rows), "level_buckets")
+        return ptr, rows
+
+    def level_tasks(self, num_threads):
+        ml = self.info()["max_level"]
+        out = np.zeros((ml + 1) * (num_threads + 1), dtype=np.int32)
+        _check(_lib.lib().sptrsv_get_level_tasks(self._h, num_threads, out), "level_tasks")
+        return out.reshape(ml + 1, num_threads + 1)
+
+    def solve(self, b, rhs=1, layout=COL_MAJOR, **opts):
+        """Host B (n*rhs float64) -> host X; raises SptrsvError on any failure."""
+        o = make_opts(**opts)
+        bb = _c(b, np.float64).reshape(-1)
+        x = np.empty(self.n * rhs, dtype=np.float64)
+        _check(_lib.lib().sptrsv_solve_host(self._h, ctypes.byref(o), bb.ctypes.data, x.ctypes.data, rhs, layout),
+               "solve")
+        return x
+
+    def solve_device(self, d_b, d_x, rhs=1, layout=COL_MAJOR, opts=None):
+        o = opts if opts is not None else make_opts()
+        _check(_lib.lib().sptrsv_solve(self._h, ctypes.byref(o), d_b, d_x, rhs, layout), "solve_device")
+
+    def sync(self):
+        return _lib.lib().sptrsv_sync(self._h)
+
+    def last_refine(self):
+        s, r = ctypes.c_int(), ctypes.c_double()
+        _lib.lib().sptrsv_last_refine(self._h, ctypes.byref(s), ctypes.byref(r))
+        return s.value, r.value
+
+    def launches(self):
+        return _lib.lib().sptrsv_kernel_launches(self._h)
+
+    def sm_count(self):
+        return _lib.lib().sptrsv_device_sm_count(self._h)
+
+    def profile(self, enable=True):
+        _check(_lib.lib().sptrsv_profile_enable(self._h, 1 if enable else 0), "profile_enable")
+
+    def profile_read(self, cap=4096):
+        """[(kind, ms)] of the last profiled solve, in launch order."""
+        kinds = np.zeros(cap, dtype=np.int32)
+        ms = np.zeros(cap, dtype=np.float32)
+        k = _lib.lib().sptrsv_profile_read(self._h, kinds, ms, cap)
+        if k < 0:
+            raise SptrsvError(k, "profile_read")
+        return list(zip(kinds[:k].tolist(), ms[:k].tolist()))
+

@@ -1,0 +1,102 @@
+// handle.cuh -- the state behind an sptrsv_handle: one device, one stream, one resident
+// matrix with its analysis, grow-only work buffers and a small cache of solve graphs.
+#pragma once
+#include <cstdint>
+#include <vector>
+#include <cuda_runtime.h>
+#include "common.cuh"
+
+namespace sptrsv {
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t cap = 0;
+    int ensure(size_t bytes);
+    void release();
+    template <typename T> T* as() const { return reinterpret_cast<T*>(p); }
+};
+
+struct GraphKey {
+    sptrsv_opts o;
+    const double* b;
+    double* x;
+    int rhs;
+    int layout;
+    int warps;
+    bool prof;
+    bool same(const GraphKey& k) const {
+        return o.schedule == k.o.schedule && o.precision == k.o.precision && o.rows_per_warp == k.o.rows_per_warp &&
+               o.rhs_tile == k.o.rhs_tile && o.inner == k.o.inner && o.inner_sweeps == k.o.inner_sweeps &&
+               o.max_refine == k.o.max_refine && o.tol == k.o.tol && o.spin_budget_ns == k.o.spin_budget_ns &&
+               b == k.b && x == k.x && rhs == k.rhs && layout == k.layout && warps == k.warps && prof == k.prof;
+    }
+};
+
+struct GraphEntry {
+    GraphKey key;
+    cudaGraphExec_t exec = nullptr;
+    int64_t kernels = 0;
+};
+
+struct Handle {
+    int device = 0;
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    int sm_count = 0;
+    int64_t launches = 0;
+    Ctl* ctl = nullptr;
+    bool use_graphs = true;
+    int warps_override = 0;
+
+    // matrix (device; either owned copies or caller-owned pointers)
+    int n = 0, nnz = 0;
+    bool analysed = false;
+    bool levels_ready = false;
+    const int* rp = nullptr;
+    const int* col = nullptr;
+    const double* val = nullptr;
+    DevBuf own_rp, own_col, own_val;
+
+    // analysis
+    DevBuf val32, invd, invd32, in_degree, levels, level_ptr, level_rows, stats;
+    int max_level = 0;
+    double max_ratio = 0.0, mean_len = 0.0, std_len = 0.0;
+    DevBuf csc_ptr, csc_row, csc_val;
+    bool have_csc = false;
+
+    // work
+    DevBuf scratch, xw, bw, r32, d32a, d32b, norms, indeg_work, left, db, dx, flush;
+    unsigned flush_byte = 1;
+    bool last_mixed = false;
+    int last_steps = 0;
+    double last_res = 0.0;
+    std::vector<GraphEntry> graphs;
+
+    // per-launch profiling: an event after every kernel step of a solve (captured into the
+    // graph as event-record nodes); durations are read after the solve completes
+    bool profiling = false;
+    cudaEvent_t prof0 = nullptr;
+    std::vector<cudaEvent_t> prof_ev;
+    std::vector<int> prof_kind;
+    int prof_n = 0;
+    int mark(int kind);
+
+    ~Handle();
+    int read_ctl(Ctl* out);
+    int reset_ctl();
+    void drop_graphs();
+    void drop_matrix();
+    int set_matrix_host(int n, int64_t nnz, const int64_t* rp, const int* col, const double* val);
+    int analyse();
+    int ensure_levels();
+    int build_csc();
+    sptrsv_opts resolve(const sptrsv_opts* o, int rhs) const;
+    int prepare(const sptrsv_opts& o, int rhs, int layout);
+    int enqueue(const sptrsv_opts& o, const double* b, double* x, int rhs, int layout);
+    int solve(const sptrsv_opts* o, const double* b, double* x, int rhs, int layout);
+    int sync();
+};
+
+void set_last_status(int s);
+
+}  // namespace sptrsv

@@ -1,0 +1,104 @@
+// kernels.cuh -- internal declarations shared by the .cu translation units.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+#include "common.cuh"
+
+namespace sptrsv {
+
+// Bump allocator over one device buffer; take() returns nullptr when the buffer is full.
+struct Scratch {
+    char* base = nullptr;
+    size_t cap = 0;
+    size_t used = 0;
+    template <typename T>
+    T* take(size_t count) {
+        size_t off = (used + 255) & ~(size_t)255;
+        size_t bytes = count * sizeof(T);
+        if (off + bytes > cap) return nullptr;
+        used = off + bytes;
+        return reinterpret_cast<T*>(base + off);
+    }
+};
+
+// api.cu
+__global__ void k_narrow_rp(int count, const int64_t* in, int* out, Ctl* ctl);
+
+// analysis.cu
+__global__ void k_validate(int n, int nnz, const int* rp, const int* col, const double* val, int* in_degree,
+                           double* invd, float* invd32, Ctl* ctl);
+__global__ void k_to_f32(size_t count, const double* a, float* b);
+__global__ void k_row_stats(int n, const int* rp, const double* val, unsigned long long* max_ratio_bits,
+                            unsigned long long* sum_len2);
+__global__ void k_levels(int n, const int* rp, const int* col, int* level, Ctl* ctl, int64_t budget);
+__global__ void k_level_hist(int n, const int* level, int* cnt);
+__global__ void k_level_tasks(int max_level, const int* lptr, const int* lrows, const int* rp, int T, int* tasks);
+__global__ void k_entry_rows(int n, const int* rp, int* erow);
+__global__ void k_gather_csc(int nnz, const int* perm, const int* erow, const double* val, int* crow, double* cval);
+__global__ void k_col_hist(int nnz, const int* col, int* cnt);
+__global__ void k_in_degree_csc(int nnz, const int* crow, int* indeg);
+__global__ void k_validate_csc(int n, int nnz, const int* cp, const int* crow, const double* cval, double* invd,
+                               Ctl* ctl);
+int scan_exclusive(const int* in, int* out, int count, int* part_scratch, cudaStream_t st, int64_t* launches);
+int scan_partials_needed(int count);
+int stable_sort_perm(const unsigned* keys_in, int count, int key_bits, int* perm, Scratch& scr, cudaStream_t st,
+                     int64_t* launches);
+
+// solve.cu -- launchers (return sptrsv_status; add their launches to *launches)
+struct SolveArgs {
+    int n;
+    const int* rp;
+    const int* col;
+    const void* val;     // double* or float*
+    const void* invd;    // double* or float*
+    const void* b;       // row-major n x rhs
+    void* x;             // row-major n x rhs
+    int rhs;
+    Ctl* ctl;
+    int64_t budget;
+    int sm_count;
+    int warps;           // resident warps to launch (0 = full occupancy)
+    cudaStream_t st;
+    int64_t* launches;
+};
+int launch_fill_pending(bool f32, void* x, size_t count, cudaStream_t st, int64_t* launches);
+int launch_pull_warp(bool f32, const SolveArgs& a, int rows_per_warp, int rhs_tile);
+int launch_pull_thread(bool f32, const SolveArgs& a);
+int launch_push_csc(const SolveArgs& a, const int* cp, const int* crow, const double* cval, int* indeg_work,
+                    double* left_sum);
+int launch_levelset(bool f32, const SolveArgs& a, int max_level, const int* lptr, const int* lrows);
+int launch_transpose(bool to_row_major, const double* src, double* dst, int n, int rhs, cudaStream_t st,
+                     int64_t* launches);
+
+// refine.cu
+struct RefineArgs {
+    int n, nnz, rhs;
+    const int* rp;
+    const int* col;
+    const double* val;
+    const float* val32;
+    const double* invd;
+    const float* invd32;
+    const double* b;   // row-major n x rhs
+    double* x;         // row-major n x rhs
+    float* r32;        // n x rhs
+    float* d32[2];     // n x rhs ping-pong
+    double* rn2;       // rhs  (||r_c||^2)
+    double* bn2;       // rhs  (||b_c||^2)
+    Ctl* ctl;
+    double tol;
+    int64_t budget;
+    int sm_count;
+    cudaStream_t st;
+    int64_t* launches;
+};
+int launch_refine_init(const RefineArgs& a);
+int launch_residual(const RefineArgs& a, bool jacobi_seed, int final_check);
+int launch_check(const RefineArgs& a, int step, bool reset_ticket);
+int launch_jacobi_sweep(const RefineArgs& a, int src, bool last);
+int launch_axpy_pending(const RefineArgs& a, int src);
+int launch_exact_inner(const RefineArgs& a, int schedule, int rows_per_warp, int dst, int max_level,
+                       const int* lptr, const int* lrows);
+
+}  // namespace sptrsv

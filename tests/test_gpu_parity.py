@@ -1,0 +1,299 @@
+"""GPU parity: every schedule and every reference-signature entry point, through the C ABI,
+against the reference's own outputs (golden.npz) and the CPU oracle.
+
+Tolerances (FP64 paths): elementwise relative error <= 1e-10 against the reference's serial
+solve, relative residual ||b - U x||_2 / ||b||_2 <= 1e-12.  Integer outputs (levels,
+in-degree, level buckets and tasks, padded index arrays) are compared bit for bit.
+"""
+import ctypes
+import hashlib
+
+import numpy as np
+import pytest
+
+import sptrsv_gb300 as sp
+from sptrsv_gb300 import gen
+
+pytestmark = pytest.mark.gpu
+
+ELEM_TOL = 1e-10
+RES_TOL = 1e-12
+GOLDEN_CASES = ["csr_5_upper", "csr_6_upper", "rand3000", "lap12", "chain500", "snr800"]
+FP64_SCHEDULES = [("syncfree_warp", 1), ("syncfree_warp", 2), ("syncfree_warp", 4), ("syncfree_warp", 8),
+                  ("syncfree_thread", 0), ("syncfree_csc", 0), ("levelset", 0)]
+
+
+def _case(g, tag):
+    rp, col, val = g[tag + "/row_ptr"].astype(np.int64), g[tag + "/col"], g[tag + "/val"]
+    rhs = int(g[tag + "/rhs"][0]) if tag + "/rhs" in g else 2
+    b = g[tag + "/b"] if tag + "/b" in g else np.ones((len(rp) - 1) * rhs)
+    return rp, col, val, b, rhs
+
+
+def elem_err(x, ref):
+    x = np.asarray(x).reshape(-1)
+    ref = np.asarray(ref).reshape(-1)
+    scale = max(np.max(np.abs(ref)), 1e-300)
+    return float(np.max(np.abs(x - ref) / np.maximum(np.abs(ref), 1e-12 * scale)))
+
+
+@pytest.fixture(scope="module")
+def solver():
+    s = sp.Solver(0)
+    yield s
+    s.close()
+
+
+@pytest.mark.parametrize("tag", GOLDEN_CASES)
+def test_analysis_bit_exact(golden, orc, solver, tag):
+    rp, col, val, _, _ = _case(golden, tag)
+    solver.analyse(rp, col, val)
+    assert np.array_equal(solver.levels(), golden[tag + "/levels"])
+    assert solver.info()["max_level"] == int(golden[tag + "/max_level"][0])
+    assert np.array_equal(solver.in_degree(), np.diff(rp).astype(np.int32))
+    lv, ml = orc.levels(rp.astype(np.uint64), col)
+    ptr_o, rows_o = orc.level_buckets(lv, ml)
+    ptr, rows = solver.level_buckets()
+    assert np.array_equal(ptr, ptr_o) and np.array_equal(rows, rows_o)
+    for T in (1, 3, 16):
+        assert np.array_equal(solver.level_tasks(T), orc.level_tasks(ml, ptr_o, rows_o, rp.astype(np.uint64), T))
+
+
+def test_levels_200k_digest(golden, solver):
+    m = gen.random_upper(200_000, 8.0, 0.9, 64, 1)
+    solver.analyse(m.row_ptr, m.col, m.val)
+    lv = solver.levels()
+    assert solver.info()["max_level"] == int(golden["rand200k/max_level"][0])
+    assert hashlib.sha256(lv.tobytes()).digest() == golden["rand200k/levels_sha256"].tobytes()
+
+
+@pytest.mark.parametrize("tag", GOLDEN_CASES)
+@pytest.mark.parametrize("sched,rpw", FP64_SCHEDULES)
+def test_fp64_schedules_match_reference(golden, orc, solver, tag, sched, rpw):
+    rp, col, val, b, rhs = _case(golden, tag)
+    solver.analyse(rp, col, val)
+    ref = golden[tag + "/base"]
+    if sched == "syncfree_thread":
+        rhs_run, bb, ref = 1, b[: len(rp) - 1], ref[: len(rp) - 1]
+    else:
+        rhs_run, bb = rhs, b
+    x = solver.solve(bb, rhs=rhs_run, schedule=sched, rows_per_warp=rpw or None)
+    assert elem_err(x, ref) <= ELEM_TOL
+    assert orc.rel_residual(rp.astype(np.uint64), col, val, x, bb, rhs_run) <= RES_TOL
+
+
+@pytest.mark.parametrize("rhs", [2, 5, 8, 33])
+@pytest.mark.parametrize("layout", [sp.COL_MAJOR, sp.ROW_MAJOR])
+@pytest.mark.parametrize("sched", ["syncfree_warp", "syncfree_csc", "levelset"])
+def test_multi_rhs(orc, solver, rhs, layout, sched):
+    m = gen.random_upper(5000, 6.0, 0.9, 64, 31)
+    solver.analyse(m.row_ptr, m.col, m.val)
+    b_cm = gen.uniform(32 + rhs, m.n * rhs)
+    ref = orc.base_gauss_upper(m.row_ptr.astype(np.uint64), m.col, m.val, b_cm, rhs)
+    if layout == sp.ROW_MAJOR:
+        b = b_cm.reshape(rhs, m.n).T.copy().reshape(-1)
+        x = solver.solve(b, rhs=rhs, layout=layout, schedule=sched).reshape(m.n, rhs).T.reshape(-1)
+    else:
+        x = solver.solve(b_cm, rhs=rhs, layout=layout, schedule=sched)
+    assert elem_err(x, ref) <= ELEM_TOL
+
+
+@pytest.mark.parametrize("inner", ["jacobi", "syncfree_warp", "syncfree_thread", "levelset"])
+@pytest.mark.parametrize("tag", ["rand3000", "lap12", "snr800"])
+def test_mixed_refinement_reaches_1e12(golden, orc, solver, inner, tag):
+    rp, col, val, b, rhs = _case(golden, tag)
+    rhs_run = 1 if inner == "syncfree_thread" else rhs
+    bb = b[: (len(rp) - 1) * rhs_run]
+    solver.analyse(rp, col, val)
+    x = solver.solve(bb, rhs=rhs_run, precision="mixed", schedule=inner, max_refine=20)
+    steps, res = solver.last_refine()
+    assert res <= RES_TOL and steps >= 1
+    assert orc.rel_residual(rp.astype(np.uint64), col, val, x, bb, rhs_run) <= 2 * RES_TOL
+    assert elem_err(x, golden[tag + "/base"][: len(x)]) <= ELEM_TOL
+
+
+def test_device_pointer_api(orc, solver):
+    torch = pytest.importorskip("torch")
+    m = gen.random_upper(20_000, 8.0, 0.9, 64, 41)
+    rhs = 4
+    dev = torch.device("cuda:0")
+    rp = torch.tensor(m.row_ptr.astype(np.int32), device=dev)
+    col = torch.tensor(m.col, device=dev)
+    val = torch.tensor(m.val, device=dev)
+    b_cm = gen.uniform(42, m.n * rhs)
+    b_rm = torch.tensor(b_cm.reshape(rhs, m.n).T.copy(), device=dev)
+    x = torch.empty_like(b_rm)
+    solver.analyse_device(m.n, m.nnz, rp.data_ptr(), col.data_ptr(), val.data_ptr())
+    torch.cuda.synchronize()
+    solver.solve_device(b_rm.data_ptr(), x.data_ptr(), rhs=rhs, layout=sp.ROW_MAJOR)
+    assert solver.sync() == 0
+    ref = orc.base_gauss_upper(m.row_ptr.astype(np.uint64), m.col, m.val, b_cm, rhs)
+    assert elem_err(x.cpu().numpy().T.reshape(-1), ref) <= ELEM_TOL
+
+
+# ---------------------------------------------------------------------------------------
+# The reference-signature entry points
+
+@pytest.mark.parametrize("tag", GOLDEN_CASES)
+def test_dropin_base_and_barrier(golden, tag):
+    rp, col, val, b, rhs = _case(golden, tag)
+    n = len(rp) - 1
+    rpu = rp.astype(np.uint64)
+    for name, key in (("base_gauss_upper", "base"), ("base_gauss_upper_new", "base_new")):
+        x = np.zeros(n * rhs)
+        t = getattr(sp, name)(n, val, rpu, col, x, b.copy(), rhs)
+        assert t >= 0, sp.status_string(int(t))
+        assert elem_err(x, golden[f"{tag}/{key}"]) <= ELEM_TOL
+    for name in ("barrier_upper", "barrier_upper_new"):
+        x = np.zeros(n * rhs)
+        t = getattr(sp, name)(n, x, b.copy(), val, col, rpu, 4, rhs)
+        assert t >= 0
+        assert elem_err(x, golden[f"{tag}/barrier_t3"]) <= ELEM_TOL
+    lv = np.zeros(n, dtype=np.uint64)
+    ml = sp.setLevelUpAndGetMaxLevel(n, col, rpu, lv)
+    assert ml == int(golden[tag + "/max_level"][0]) and np.array_equal(lv, golden[tag + "/levels"])
+
+
+@pytest.mark.parametrize("tag", ["csr_6_upper", "snr800"])
+def test_dropin_supernodal(golden, tag):
+    rp, col, val, b, rhs = _case(golden, tag)
+    n = len(rp) - 1
+    rpu = rp.astype(np.uint64)
+    snodes = golden[tag + "/snodes"].astype(np.int32)
+    sn = len(snodes) - 1
+    for name, key in (("supernodal_upper", "super"), ("supernodal_upper_new", "super_new")):
+        x = b.copy()
+        t = getattr(sp, name)(sn, snodes, x, val, col, rpu, n, rhs)
+        assert t >= 0
+        assert elem_err(x, golden[f"{tag}/{key}"]) <= ELEM_TOL
+    w = np.diff(snodes).astype(np.int64)
+    total = int(rp[-1]) + int(np.sum(w * (w - 1) // 2))
+    vp = np.zeros(total)
+    cp = np.zeros(total, dtype=np.uint64)
+    rpp = np.zeros(n + 1, dtype=np.int32)
+    sn_c, nz_c = ctypes.c_int(sn), ctypes.c_int(0)
+    t = sp.ccs2ccs_pad(val, col, rpu, vp, cp, rpp, snodes, sn_c, nz_c)
+    assert t >= 0 and nz_c.value == len(golden[tag + "/pad_val"])
+    assert np.array_equal(vp, golden[tag + "/pad_val"])
+    assert np.array_equal(cp, golden[tag + "/pad_col"])
+    assert np.array_equal(rpp, golden[tag + "/pad_rowptr"])
+    for name in ("supernodal_blas_upper", "supernodal_blas_upper_new"):
+        x = b.copy()
+        t = getattr(sp, name)(n, nz_c.value, sn, snodes, x, vp, cp, rpp, rhs)
+        assert t >= 0
+        assert elem_err(x, golden[tag + "/blas"]) <= ELEM_TOL
+
+
+@pytest.mark.parametrize("tag", GOLDEN_CASES)
+def test_dropin_syncfree_opencl(golden, orc, tag):
+    rp, col, val, b, rhs = _case(golden, tag)
+    n = len(rp) - 1
+    cp, rt, vt = orc.transpose(rp.astype(np.uint64), col, val)
+    rt32 = rt.astype(np.int32)
+    ref_cm = golden[tag + "/base"]
+    b_rm = b.reshape(rhs, n).T.copy().reshape(-1)
+    x = np.zeros(n * rhs)
+    t = sp.sptrsv_syncfree_opencl(cp, rt32, vt, n, n, len(vt), x, b_rm, rhs)
+    assert t >= 0
+    assert elem_err(x.reshape(n, rhs).T.reshape(-1), ref_cm) <= ELEM_TOL
+    x1 = np.zeros(n)
+    assert sp.sptrsv_syncfree2_opencl(cp, rt32, vt, n, n, len(vt), x1, b[:n].copy()) >= 0
+    assert elem_err(x1, ref_cm[:n]) <= ELEM_TOL
+    x3 = np.zeros(n)
+    assert sp.sptrsv_syncfree3_opencl(col, rp.astype(np.int32), val, n, n, len(val), x3, b[:n].copy()) >= 0
+    assert elem_err(x3, ref_cm[:n]) <= ELEM_TOL
+    assert sp.sptrsv_syncfree_opencl(cp, rt32, vt, n, n + 1, len(vt), x, b_rm, rhs) == -1.0
+
+
+# ---------------------------------------------------------------------------------------
+# Invalid inputs are reported, never hang or fault
+
+def _bad(kind):
+    m = gen.random_upper(3000, 5.0, 0.9, 32, 51)
+    rp, col, val = m.row_ptr.copy(), m.col.copy(), m.val.copy()
+    i = 1234
+    s = rp[i]
+    if kind == "missing_diag":
+        col[s] = col[s + 1] if rp[i + 1] - s > 1 else i + 1
+        want = -5
+    elif kind == "lower":
+        col[s + 1] = i - 3
+        want = -6
+    elif kind == "col_range":
+        col[s + 1] = m.n + 7
+        want = -7
+    elif kind == "row_ptr":
+        rp[i] = rp[i + 1] + 2
+        want = -4
+    elif kind == "zero_pivot":
+        val[s] = 0.0
+        want = -8
+    elif kind == "nan_pivot":
+        val[s] = np.nan
+        want = -8
+    return m.n, rp, col, val, want
+
+
+@pytest.mark.parametrize("kind", ["missing_diag", "lower", "col_range", "row_ptr", "zero_pivot", "nan_pivot"])
+def test_invalid_matrix_statuses(solver, kind):
+    n, rp, col, val, want = _bad(kind)
+    if kind == "lower" and rp[1235] - rp[1234] < 2:
+        pytest.skip("row too short for this injection")
+    with pytest.raises(sp.SptrsvError) as e:
+        solver.analyse(rp, col, val)
+    assert e.value.status == want
+    x = np.zeros(n)
+    t = sp.base_gauss_upper(n, val, rp.astype(np.uint64), col, x, np.ones(n), 1)
+    assert t == float(want) and sp.last_status() == want
+
+
+def test_spin_budget_timeout_then_recovery(orc, solver):
+    # a pure chain: row i depends on row i+1; a 1 ns wait budget must run out
+    n = 200_000
+    rp = np.arange(0, 2 * n, 2, dtype=np.int64)
+    rp = np.append(rp, 2 * n - 1)
+    col = np.empty(2 * n - 1, dtype=np.int32)
+    col[0::2] = np.arange(n)
+    col[1::2] = np.arange(1, n)
+    val = np.empty(2 * n - 1)
+    val[0::2] = 2.0
+    val[1::2] = -1.0
+    solver.analyse(rp, col, val)
+    b = np.ones(n)
+    with pytest.raises(sp.SptrsvError) as e:
+        solver.solve(b, schedule="syncfree_warp", spin_budget_ns=1)
+    assert e.value.status == -9
+    x = solver.solve(b, schedule="syncfree_warp")
+    ref = orc.base_gauss_upper(rp.astype(np.uint64), col, val, b, 1)
+    assert elem_err(x, ref) <= ELEM_TOL
+
+
+# ---------------------------------------------------------------------------------------
+# Full-size workloads
+
+def test_band_laplace_full(orc, solver):
+    m, xs, b = gen.band_laplace_case()
+    solver.analyse(m.row_ptr, m.col, m.val)
+    assert solver.info()["max_level"] == 4096
+    ref = orc.base_gauss_upper(m.row_ptr.astype(np.uint64), m.col, m.val, b, 1)
+    for sched in ("syncfree_warp", "syncfree_thread", "syncfree_csc", "levelset"):
+        x = solver.solve(b, schedule=sched)
+        assert elem_err(x, ref) <= ELEM_TOL, sched
+        assert orc.rel_residual(m.row_ptr.astype(np.uint64), m.col, m.val, x, b, 1) <= RES_TOL
+    x = solver.solve(b, precision="mixed")
+    assert solver.last_refine()[1] <= RES_TOL
+    assert elem_err(x, ref) <= ELEM_TOL
+
+
+def test_irregular_2m_full(orc, solver):
+    m, xs, b = gen.irregular_case()
+    solver.analyse(m.row_ptr, m.col, m.val)
+    ref = orc.base_gauss_upper(m.row_ptr.astype(np.uint64), m.col, m.val, b, 1)
+    x = solver.solve(b, schedule="syncfree_warp")
+    assert elem_err(x, ref) <= ELEM_TOL
+    x = solver.solve(b, precision="mixed", schedule="jacobi")
+    steps, res = solver.last_refine()
+    assert res <= RES_TOL
+    assert elem_err(x, ref) <= ELEM_TOL
+    # property at full size: the solution of U x = U x* is x*
+    assert np.max(np.abs(x - xs)) <= 1e-9
