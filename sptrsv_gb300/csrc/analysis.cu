@@ -150,7 +150,7 @@ __device__ __forceinline__ int block_exclusive_scan(int v, int* total) {
     return res;
 }
 
-__global__ void k_scan_partials(const int* __restrict__ in, int count, int* __restrict__ part) {
+__global__ void k_scan_partials(const int* in, int count, int* part) {
     const int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
     int s = 0;
 #pragma unroll
@@ -176,7 +176,7 @@ __global__ void k_scan_single(int* part, int count) {
     }
 }
 
-__global__ void k_scan_final(const int* __restrict__ in, int count, const int* __restrict__ part, int* __restrict__ out) {
+__global__ void k_scan_final(const int* in, int count, const int* part, int* out) {
     const int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
     int v[kScanItems];
     int s = 0;

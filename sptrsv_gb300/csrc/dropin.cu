@@ -75,11 +75,12 @@ __global__ void k_pad_fill(int n, const int* __restrict__ rp, const int* __restr
     }
 }
 // Inverse: drop the `i - start` leading padding entries of every padded row.
-__global__ void k_unpad_lengths(int n, const int* __restrict__ prp, const int* __restrict__ start, int* __restrict__ len,
-                                Ctl* ctl) {
+__global__ void k_unpad_lengths(int n, int nz, const int* __restrict__ prp, const int* __restrict__ start,
+                                int* __restrict__ len, Ctl* ctl) {
+    if (blockIdx.x == 0 && threadIdx.x == 0 && (prp[0] != 0 || prp[n] > nz)) record_error(ctl, SPTRSV_ERR_ROW_PTR);
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const int l = prp[i + 1] - prp[i] - (i - start[i]);
-        if (l < 1) { record_error(ctl, SPTRSV_ERR_SUPERNODES); len[i] = 0; }
+        if (l < 1 || prp[i + 1] < prp[i]) { record_error(ctl, SPTRSV_ERR_SUPERNODES); len[i] = 0; }
         else len[i] = l;
     }
 }
@@ -219,7 +220,7 @@ static double blas_padded(int n, int nz, size_t sn, int* supernodes, double* x, 
         return fail(SPTRSV_ERR_CUDA);
     if ((rc = h->reset_ctl())) return fail(rc);
     k_snode_start<<<h->sm_count, 256, 0, h->st>>>((int)sn, d_sn, n, start, h->ctl);
-    k_unpad_lengths<<<h->sm_count * 4, 256, 0, h->st>>>(n, prp, start, len, h->ctl);
+    k_unpad_lengths<<<h->sm_count * 4, 256, 0, h->st>>>(n, nz, prp, start, len, h->ctl);
     h->launches += 2;
     if ((rc = scan_exclusive(len, len, n, part, h->st, &h->launches))) return fail(rc);
     Ctl c{};
@@ -379,6 +380,7 @@ double ccs2ccs_pad(double* val, int* row, uint64_t* col_index, double* val_pad, 
     const int n = nodes[sn];
     if (n <= 0) return fail(SPTRSV_ERR_SUPERNODES);
     if ((rc = h->set_matrix_host(n, (int64_t)col_index[n], (const int64_t*)col_index, row, val))) return fail(rc);
+    if ((rc = h->analyse())) return fail(rc);  // the pad kernels index through the checked CSR
     const int nz0 = h->nnz;
     h->drop_graphs();
     if (cudaEventRecord(h->ev0, h->st) != cudaSuccess) return fail(SPTRSV_ERR_CUDA);
