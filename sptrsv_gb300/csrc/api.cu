@@ -391,7 +391,8 @@ int Handle::solve(const sptrsv_opts* o_in, const double* b, double* x, int rhs, 
     int rc;
     if ((rc = prepare(o, rhs, layout))) return rc;
     last_mixed = o.precision == SPTRSV_PREC_MIXED;
-    if (!use_graphs) return enqueue(o, b, x, rhs, layout);
+    // profiled solves launch directly: their per-step events are timed from the host stream
+    if (!use_graphs || profiling) return enqueue(o, b, x, rhs, layout);
     GraphKey key;
     key.o = o;
     key.b = b;

@@ -18,6 +18,9 @@ pytestmark = pytest.mark.gpu
 
 ELEM_TOL = 1e-10
 RES_TOL = 1e-12
+# The refined mixed path is specified by its residual (<= 1e-12); its elementwise error
+# against the FP64 solve is then bounded by the conditioning, checked here at 1e-8.
+MIXED_ELEM_TOL = 1e-8
 GOLDEN_CASES = ["csr_5_upper", "csr_6_upper", "rand3000", "lap12", "chain500", "snr800"]
 FP64_SCHEDULES = [("syncfree_warp", 1), ("syncfree_warp", 2), ("syncfree_warp", 4), ("syncfree_warp", 8),
                   ("syncfree_thread", 0), ("syncfree_csc", 0), ("levelset", 0)]
@@ -109,7 +112,7 @@ def test_mixed_refinement_reaches_1e12(golden, orc, solver, inner, tag):
     steps, res = solver.last_refine()
     assert res <= RES_TOL and steps >= 1
     assert orc.rel_residual(rp.astype(np.uint64), col, val, x, bb, rhs_run) <= 2 * RES_TOL
-    assert elem_err(x, golden[tag + "/base"][: len(x)]) <= ELEM_TOL
+    assert elem_err(x, golden[tag + "/base"][: len(x)]) <= MIXED_ELEM_TOL
 
 
 def test_device_pointer_api(orc, solver):
@@ -282,7 +285,7 @@ def test_band_laplace_full(orc, solver):
         assert orc.rel_residual(m.row_ptr.astype(np.uint64), m.col, m.val, x, b, 1) <= RES_TOL
     x = solver.solve(b, precision="mixed")
     assert solver.last_refine()[1] <= RES_TOL
-    assert elem_err(x, ref) <= ELEM_TOL
+    assert elem_err(x, ref) <= MIXED_ELEM_TOL
 
 
 def test_irregular_2m_full(orc, solver):
@@ -294,6 +297,6 @@ def test_irregular_2m_full(orc, solver):
     x = solver.solve(b, precision="mixed", schedule="jacobi")
     steps, res = solver.last_refine()
     assert res <= RES_TOL
-    assert elem_err(x, ref) <= ELEM_TOL
+    assert elem_err(x, ref) <= MIXED_ELEM_TOL
     # property at full size: the solution of U x = U x* is x*
     assert np.max(np.abs(x - xs)) <= 1e-9
