@@ -147,6 +147,26 @@ SPTRSV_API int sptrsv_timer_end(sptrsv_handle h, float* ms);     /* synchronises
 SPTRSV_API int sptrsv_flush_l2(sptrsv_handle h);                 /* writes 512 MiB of scratch */
 SPTRSV_API int64_t sptrsv_kernel_launches(sptrsv_handle h);      /* kernels this handle has launched */
 SPTRSV_API int sptrsv_device_sm_count(sptrsv_handle h);
+/* Largest n accepted by sptrsv_solve_noalloc (its reciprocal diagonal lives in a fixed array). */
+#define SPTRSV_NOALLOC_MAX_ROWS (1 << 20)
+
+/* No counterpart in the reference.  The FP64 sync-free warp solve of U x = b (one RHS) for
+ * callers that cannot allocate device memory: programs that give the whole GPU to their own
+ * memory pool and forbid any other allocation, and latency-critical loops that cannot pay for
+ * cudaMalloc / cudaFree (which synchronise the device and may fail at run time).  The caller
+ * passes device arrays only -- CSR of U with an int32 row pointer and the diagonal first in
+ * every row, b and x -- and an optional stream (NULL = the legacy default stream).  No memory
+ * is allocated: the spin control block and the reciprocal diagonal live in one fixed device
+ * array of SPTRSV_NOALLOC_MAX_ROWS * 8 + 256 bytes that every GPU loading this library holds
+ * until the process exits.  n above SPTRSV_NOALLOC_MAX_ROWS returns SPTRSV_ERR_TOO_LARGE.
+ * The first call on a device looks up that device's array address (cudaGetSymbolAddress), so
+ * make the first call before any stream capture starts.  The matrix is checked first (same
+ * statuses as sptrsv_analyse_*).  The call is synchronous: it returns the solve's status after
+ * the stream has drained.  All calls share the array and each rewrites it, so calls that
+ * overlap on the GPU race: order them on one stream or one host thread. */
+SPTRSV_API int sptrsv_solve_noalloc(int n, int nnz, const int* d_row_ptr, const int* d_col, const double* d_val,
+                                    const double* d_b, double* d_x, void* stream);
+
 /* Record a CUDA event after every kernel step of later solves (also inside their graphs). */
 SPTRSV_API int sptrsv_profile_enable(sptrsv_handle h, int enable);
 /* After a profiled solve: per-step kinds (enum sptrsv_kernel_kind) and device times in ms, in

@@ -93,6 +93,7 @@ C_API = {
     "sptrsv_flush_l2": ([c_vp], c_int),
     "sptrsv_kernel_launches": ([c_vp], c_i64),
     "sptrsv_device_sm_count": ([c_vp], c_int),
+    "sptrsv_solve_noalloc": ([c_int, c_int, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp], c_int),
     "sptrsv_profile_enable": ([c_vp, c_int], c_int),
     "sptrsv_profile_read": ([c_vp, i32, _P(dtype=np.float32, flags="C_CONTIGUOUS"), c_int], c_int),
 }
