@@ -91,10 +91,13 @@ typedef struct sptrsv_opts {
     int rows_per_warp;      /* SYNCFREE_WARP: 1, 2, 4, 8 (lanes per row = 32 / rows_per_warp) */
     int rhs_tile;           /* columns handled per warp pass (0 = min(rhs, 32)) */
     int inner;              /* MIXED: inner FP32 schedule (enum sptrsv_schedule) */
-    int inner_sweeps;       /* MIXED + JACOBI: sweeps per refinement step */
+    int inner_sweeps;       /* MIXED + JACOBI: sweeps per step in unlooped (profiled / graph-less)
+                               solves; device-looped solves stop on the change test (cap 200) */
     int max_refine;         /* MIXED: maximum refinement steps */
     double tol;             /* MIXED: target ||b - U x||_2 / ||b||_2 */
     int64_t spin_budget_ns; /* per-wait limit of every device spin (0 = 2 s) */
+    int resident_warps;     /* sync-free kernels: warps launched (0 = chosen from the level width) */
+    int inner_tol_exp;      /* MIXED + JACOBI: inner sweeps stop when max|change| <= 10^-e max|d| (0 = 6) */
 } sptrsv_opts;
 
 typedef struct sptrsv_ctx* sptrsv_handle;
@@ -132,8 +135,9 @@ SPTRSV_API int sptrsv_solve(sptrsv_handle h, const sptrsv_opts* o, const double*
 SPTRSV_API int sptrsv_solve_host(sptrsv_handle h, const sptrsv_opts* o, const double* b, double* x, int rhs, int layout);
 /* Wait for the handle's stream; returns the first device error of the enqueued work. */
 SPTRSV_API int sptrsv_sync(sptrsv_handle h);
-/* Refinement steps and final relative residual of the last MIXED solve (after sync). */
-SPTRSV_API int sptrsv_last_refine(sptrsv_handle h, int* steps, double* rel_residual);
+/* Refinement steps, total inner Jacobi sweeps and final relative residual of the last MIXED
+ * solve (valid after sptrsv_sync or a host-buffer solve). */
+SPTRSV_API int sptrsv_last_refine(sptrsv_handle h, int* steps, int* inner_sweeps, double* rel_residual);
 
 /* Device and pinned-host memory, copies and timing on the handle's stream. */
 SPTRSV_API int sptrsv_device_alloc(sptrsv_handle h, size_t bytes, void** ptr);

@@ -45,7 +45,7 @@ def last_status():
 
 
 def make_opts(schedule="auto", precision="fp64", rows_per_warp=None, rhs_tile=None, inner="auto", inner_sweeps=None,
-              max_refine=None, tol=None, spin_budget_ns=None):
+              max_refine=None, tol=None, spin_budget_ns=None, resident_warps=None, inner_tol_exp=None):
     """struct sptrsv_opts from sptrsv_default_opts, with the given fields replaced."""
     o = Opts()
     _lib.lib().sptrsv_default_opts(ctypes.byref(o))
@@ -53,7 +53,8 @@ def make_opts(schedule="auto", precision="fp64", rows_per_warp=None, rhs_tile=No
     o.precision = PREC[precision] if isinstance(precision, str) else int(precision)
     o.inner = SCHED[inner] if isinstance(inner, str) else int(inner)
     for name, v in (("rows_per_warp", rows_per_warp), ("rhs_tile", rhs_tile), ("inner_sweeps", inner_sweeps),
-                    ("max_refine", max_refine), ("tol", tol), ("spin_budget_ns", spin_budget_ns)):
+                    ("max_refine", max_refine), ("tol", tol), ("spin_budget_ns", spin_budget_ns),
+                    ("resident_warps", resident_warps), ("inner_tol_exp", inner_tol_exp)):
         if v is not None:
             setattr(o, name, v)
     return o
@@ -222,9 +223,16 @@ class Solver:
         return _lib.lib().sptrsv_sync(self._h)
 
     def last_refine(self):
-        s, r = ctypes.c_int(), ctypes.c_double()
-        _lib.lib().sptrsv_last_refine(self._h, ctypes.byref(s), ctypes.byref(r))
+        """(refinement steps, relative residual) of the last mixed solve."""
+        s, w, r = ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
+        _lib.lib().sptrsv_last_refine(self._h, ctypes.byref(s), ctypes.byref(w), ctypes.byref(r))
         return s.value, r.value
+
+    def last_sweeps(self):
+        """Total inner Jacobi sweeps of the last mixed solve (device-looped graphs)."""
+        s, w, r = ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
+        _lib.lib().sptrsv_last_refine(self._h, ctypes.byref(s), ctypes.byref(w), ctypes.byref(r))
+        return w.value
 
     def launches(self):
         return _lib.lib().sptrsv_kernel_launches(self._h)

@@ -24,7 +24,7 @@ class Opts(ctypes.Structure):
     """struct sptrsv_opts (include/sptrsv_gb300.h)."""
     _fields_ = [("schedule", c_int), ("precision", c_int), ("rows_per_warp", c_int), ("rhs_tile", c_int),
                 ("inner", c_int), ("inner_sweeps", c_int), ("max_refine", c_int), ("tol", c_dbl),
-                ("spin_budget_ns", c_i64)]
+                ("spin_budget_ns", c_i64), ("resident_warps", c_int), ("inner_tol_exp", c_int)]
 
 
 # C++ entry points with the reference's signatures (include/core.h, include/sptrsv_syncfree_opencl.h);
@@ -81,7 +81,7 @@ C_API = {
     "sptrsv_solve": ([c_vp, ctypes.POINTER(Opts), c_vp, c_vp, c_int, c_int], c_int),
     "sptrsv_solve_host": ([c_vp, ctypes.POINTER(Opts), c_vp, c_vp, c_int, c_int], c_int),
     "sptrsv_sync": ([c_vp], c_int),
-    "sptrsv_last_refine": ([c_vp, _c_int_p, ctypes.POINTER(c_dbl)], c_int),
+    "sptrsv_last_refine": ([c_vp, _c_int_p, _c_int_p, ctypes.POINTER(c_dbl)], c_int),
     "sptrsv_device_alloc": ([c_vp, c_sz, ctypes.POINTER(c_vp)], c_int),
     "sptrsv_device_free": ([c_vp, c_vp], c_int),
     "sptrsv_host_alloc": ([c_vp, c_sz, ctypes.POINTER(c_vp)], c_int),

@@ -82,6 +82,7 @@ void Handle::drop_matrix() {
     analysed = false;
     levels_ready = false;
     have_csc = false;
+    have_offdiag = false;
     n = nnz = max_level = 0;
     rp = col = nullptr;
     val = nullptr;
@@ -207,19 +208,13 @@ sptrsv_opts Handle::resolve(const sptrsv_opts* o, int rhs) const {
         }
     }
     if (r.precision == SPTRSV_PREC_MIXED) {
-        if (r.schedule == SPTRSV_SCHED_JACOBI) {
-            r.inner = SPTRSV_SCHED_JACOBI;
-        } else {
-            r.inner = r.schedule;
-        }
-        if (r.inner == SPTRSV_SCHED_JACOBI && max_ratio >= 1.0) r.inner = SPTRSV_SCHED_SYNCFREE_WARP;
+        r.inner = (r.schedule == SPTRSV_SCHED_JACOBI) ? SPTRSV_SCHED_JACOBI : r.schedule;
         if (r.inner == SPTRSV_SCHED_SYNCFREE_CSC) r.inner = SPTRSV_SCHED_SYNCFREE_WARP;
-        if (r.inner_sweeps <= 0) {
-            // sweeps so that max_ratio^s <= 1e-6 (FP32 correction accuracy), clamped
-            int s = 12;
-            if (max_ratio > 0 && max_ratio < 1.0) s = (int)std::ceil(std::log(1e-6) / std::log(max_ratio));
-            r.inner_sweeps = std::max(2, std::min(s, 64));
-        }
+        // Jacobi sweeps contract only for strictly diagonally dominant U
+        if (r.inner == SPTRSV_SCHED_JACOBI && !(max_ratio < 1.0)) r.inner = SPTRSV_SCHED_SYNCFREE_WARP;
+        // flat (unlooped) graphs run a fixed number of sweeps per correction
+        if (r.inner_sweeps <= 0) r.inner_sweeps = 16;
+        if (r.inner_tol_exp <= 0) r.inner_tol_exp = 6;
     }
     if (r.rows_per_warp <= 0) {
         const double m = mean_len;
@@ -239,6 +234,8 @@ int Handle::prepare(const sptrsv_opts& o, int rhs, int layout) {
         if ((rc = xw.ensure(sizeof(double) * nr))) return rc;
     }
     if (o.precision == SPTRSV_PREC_MIXED) {
+        if (o.inner == SPTRSV_SCHED_JACOBI && rhs == 1)
+            if ((rc = ensure_offdiag())) return rc;
         if ((rc = r32.ensure(sizeof(float) * nr))) return rc;
         if ((rc = d32a.ensure(sizeof(float) * nr))) return rc;
         if ((rc = d32b.ensure(sizeof(float) * nr))) return rc;
@@ -282,7 +279,7 @@ int Handle::enqueue(const sptrsv_opts& o, const double* b, double* x, int rhs, i
     a.ctl = ctl;
     a.budget = o.spin_budget_ns;
     a.sm_count = sm_count;
-    a.warps = warps_override;
+    a.warps = resident_warps(o);
     a.st = st;
     a.launches = &launches;
     if (o.precision == SPTRSV_PREC_FP64) {
@@ -319,28 +316,7 @@ int Handle::enqueue(const sptrsv_opts& o, const double* b, double* x, int rhs, i
         }
     } else {
         RefineArgs ra{};
-        ra.n = n;
-        ra.nnz = nnz;
-        ra.rhs = rhs;
-        ra.rp = rp;
-        ra.col = col;
-        ra.val = val;
-        ra.val32 = val32.as<float>();
-        ra.invd = invd.as<double>();
-        ra.invd32 = invd32.as<float>();
-        ra.b = brm;
-        ra.x = xrm;
-        ra.r32 = r32.as<float>();
-        ra.d32[0] = d32a.as<float>();
-        ra.d32[1] = d32b.as<float>();
-        ra.rn2 = norms.as<double>();
-        ra.bn2 = norms.as<double>() + rhs;
-        ra.ctl = ctl;
-        ra.tol = o.tol;
-        ra.budget = o.spin_budget_ns;
-        ra.sm_count = sm_count;
-        ra.st = st;
-        ra.launches = &launches;
+        if ((rc = refine_args(o, brm, xrm, rhs, &ra))) return rc;
         const bool jac = o.inner == SPTRSV_SCHED_JACOBI;
         if ((rc = launch_refine_init(ra))) return rc;
         if ((rc = mark(SPTRSV_K_INIT))) return rc;
@@ -356,14 +332,14 @@ int Handle::enqueue(const sptrsv_opts& o, const double* b, double* x, int rhs, i
                     if ((rc = mark(SPTRSV_K_AXPY))) return rc;
                 } else {
                     for (int q = 1; q < o.inner_sweeps; ++q) {
-                        if ((rc = launch_jacobi_sweep(ra, src, q == o.inner_sweeps - 1))) return rc;
+                        if ((rc = launch_jacobi_sweep(ra, src, q == o.inner_sweeps - 1, false))) return rc;
                         if ((rc = mark(SPTRSV_K_JACOBI))) return rc;
                         src ^= 1;
                     }
                 }
             } else {
                 if ((rc = launch_exact_inner(ra, o.inner, o.rows_per_warp, 0, max_level, level_ptr.as<int>(),
-                                             level_rows.as<int>())))
+                                             level_rows.as<int>(), resident_warps(o))))
                     return rc;
                 if ((rc = mark(SPTRSV_K_INNER))) return rc;
                 if ((rc = launch_axpy_pending(ra, 0))) return rc;
@@ -382,6 +358,157 @@ int Handle::enqueue(const sptrsv_opts& o, const double* b, double* x, int rhs, i
     return 0;
 }
 
+int Handle::resident_warps(const sptrsv_opts& o) const {
+    if (o.resident_warps > 0) return o.resident_warps;
+    if (warps_override > 0) return warps_override;
+    // enough rows in flight to cover ~32 levels of the DAG; more warps only add spin traffic
+    const double width = levels_ready && max_level > 0 ? (double)n / max_level : 64.0;
+    const int rows = (int)std::min(1.0e9, std::max(256.0, width * 32.0));
+    const int rpw = o.rows_per_warp > 0 ? o.rows_per_warp : 1;
+    return std::max(64, rows / rpw);
+}
+
+int Handle::ensure_offdiag() {
+    if (have_offdiag) return 0;
+    int rc;
+    if ((rc = offdiag.ensure(sizeof(int2) * ((size_t)(nnz - n) + 4)))) return rc;
+    CUDA_TRY(cudaMemsetAsync(offdiag.p, 0, sizeof(int2) * ((size_t)(nnz - n) + 4), st));
+    if ((rc = launch_build_offdiag(n, rp, col, val, offdiag.as<int2>(), sm_count, st, &launches))) return rc;
+    CUDA_TRY(cudaStreamSynchronize(st));
+    have_offdiag = true;
+    return 0;
+}
+
+int Handle::refine_args(const sptrsv_opts& o, const double* b, double* x, int rhs, RefineArgs* ra) {
+    RefineArgs& r = *ra;
+    r = RefineArgs{};
+    r.n = n;
+    r.nnz = nnz;
+    r.rhs = rhs;
+    r.rp = rp;
+    r.col = col;
+    r.val = val;
+    r.val32 = val32.as<float>();
+    r.invd = invd.as<double>();
+    r.invd32 = invd32.as<float>();
+    r.off = (have_offdiag && rhs == 1) ? offdiag.as<int2>() : nullptr;
+    r.b = b;
+    r.x = x;
+    r.r32 = r32.as<float>();
+    r.d32[0] = d32a.as<float>();
+    r.d32[1] = d32b.as<float>();
+    r.rn2 = norms.as<double>();
+    r.bn2 = norms.as<double>() + rhs;
+    r.ctl = ctl;
+    r.tol = o.tol;
+    r.budget = o.spin_budget_ns;
+    r.sm_count = sm_count;
+    r.st = st;
+    r.launches = &launches;
+    return 0;
+}
+
+// Device-looped mixed solves: Jacobi inner sweeps run in conditional WHILE nodes, so the whole
+// solve is one graph launch with no launches after convergence.
+bool Handle::cond_eligible(const sptrsv_opts& o, int rhs) const {
+    (void)rhs;
+    return use_graphs && !profiling && o.precision == SPTRSV_PREC_MIXED && o.inner == SPTRSV_SCHED_JACOBI;
+}
+
+int Handle::build_cond_graph(const sptrsv_opts& o, const double* b, double* x, int rhs, int layout,
+                             cudaGraphExec_t* out, int64_t* fixed_kernels) {
+    *out = nullptr;
+    const bool conv = rhs > 1 && layout == SPTRSV_COL_MAJOR;
+    const double* brm = conv ? bw.as<double>() : b;
+    double* xrm = conv ? xw.as<double>() : x;
+    RefineArgs ra{};
+    int rc = refine_args(o, brm, xrm, rhs, &ra);
+    if (rc) return rc;
+    int64_t scratch_launches = 0;
+    ra.launches = &scratch_launches;
+    cudaGraph_t g = nullptr;
+    CUDA_TRY(cudaGraphCreate(&g, 0));
+    cudaGraphConditionalHandle ho = 0, hi = 0;
+    cudaError_t e = cudaGraphConditionalHandleCreate(&ho, g, 1, cudaGraphCondAssignDefault);
+    if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&hi, g, 0, cudaGraphCondAssignDefault);
+    if (e != cudaSuccess) { cudaGraphDestroy(g); return set_cuda_error(e, "conditional handle"); }
+    cudaGraph_t obody = nullptr, ibody = nullptr;
+    const float eps = powf(10.f, -(float)o.inner_tol_exp);
+    const int max_sweeps = 200;  // per correction; the change test normally stops far earlier
+    auto add_while = [&](cudaGraph_t parent, cudaGraphConditionalHandle h, cudaGraph_t* body) -> cudaError_t {
+        cudaStreamCaptureStatus cs;
+        const cudaGraphNode_t* deps = nullptr;
+        size_t nd = 0;
+        cudaError_t er = cudaStreamGetCaptureInfo(st, &cs, nullptr, nullptr, &deps, nullptr, &nd);
+        if (er != cudaSuccess) return er;
+        // cudaGraphNodeParams has no usable default constructor: build it in zeroed storage
+        alignas(cudaGraphNodeParams) unsigned char raw[sizeof(cudaGraphNodeParams)];
+        memset(raw, 0, sizeof(raw));
+        cudaGraphNodeParams* p = reinterpret_cast<cudaGraphNodeParams*>(raw);
+        p->type = cudaGraphNodeTypeConditional;
+        p->conditional.handle = h;
+        p->conditional.type = cudaGraphCondTypeWhile;
+        p->conditional.size = 1;
+        cudaGraphNode_t node;
+        er = cudaGraphAddNode(&node, parent, deps, nullptr, nd, p);
+        if (er != cudaSuccess) return er;
+        *body = p->conditional.phGraph_out[0];
+        return cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+    };
+    // top level: [transpose b] memset ctl, init, WHILE(outer), [transpose x]
+    e = cudaStreamBeginCaptureToGraph(st, g, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
+    if (e == cudaSuccess) {
+        if (!rc && conv) rc = launch_transpose(true, b, bw.as<double>(), n, rhs, st, &scratch_launches);
+        if (!rc && cudaMemsetAsync(ctl, 0, sizeof(Ctl), st) != cudaSuccess) rc = SPTRSV_ERR_CUDA;
+        if (!rc) rc = launch_refine_init(ra);
+        if (!rc && add_while(g, ho, &obody) != cudaSuccess) rc = SPTRSV_ERR_CUDA;
+        if (!rc && conv) rc = launch_transpose(false, xrm, x, n, rhs, st, &scratch_launches);
+        cudaGraph_t g2 = nullptr;
+        cudaError_t e2 = cudaStreamEndCapture(st, &g2);
+        if (!rc && e2 != cudaSuccess) rc = set_cuda_error(e2, "capture top");
+    } else {
+        rc = set_cuda_error(e, "begin capture top");
+    }
+    const int64_t fixed = scratch_launches;
+    // outer body: residual (seeds d0), test, WHILE(inner), x += d
+    if (!rc) {
+        e = cudaStreamBeginCaptureToGraph(st, obody, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
+        if (e == cudaSuccess) {
+            rc = launch_residual(ra, true, 0);
+            if (!rc) rc = launch_check_outer(ra, o.max_refine, ho, hi);
+            if (!rc && add_while(obody, hi, &ibody) != cudaSuccess) rc = SPTRSV_ERR_CUDA;
+            if (!rc) rc = launch_axpy_pending(ra, 0);
+            cudaGraph_t g2 = nullptr;
+            cudaError_t e2 = cudaStreamEndCapture(st, &g2);
+            if (!rc && e2 != cudaSuccess) rc = set_cuda_error(e2, "capture outer");
+        } else {
+            rc = set_cuda_error(e, "begin capture outer");
+        }
+    }
+    // inner body: two sweeps (d0 -> d1 -> d0), the second measuring its change, then the test
+    if (!rc) {
+        e = cudaStreamBeginCaptureToGraph(st, ibody, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
+        if (e == cudaSuccess) {
+            rc = launch_jacobi_sweep(ra, 0, false, false);
+            if (!rc) rc = launch_jacobi_sweep(ra, 1, false, true);
+            if (!rc) rc = launch_check_inner(ra, eps, max_sweeps, hi);
+            cudaGraph_t g2 = nullptr;
+            cudaError_t e2 = cudaStreamEndCapture(st, &g2);
+            if (!rc && e2 != cudaSuccess) rc = set_cuda_error(e2, "capture inner");
+        } else {
+            rc = set_cuda_error(e, "begin capture inner");
+        }
+    }
+    if (!rc) {
+        e = cudaGraphInstantiate(out, g, 0);
+        if (e != cudaSuccess) rc = set_cuda_error(e, "instantiate conditional");
+    }
+    cudaGraphDestroy(g);
+    (void)cudaGetLastError();
+    *fixed_kernels = fixed;
+    return rc;
+}
+
 int Handle::solve(const sptrsv_opts* o_in, const double* b, double* x, int rhs, int layout) {
     if (!analysed) return SPTRSV_ERR_NO_ANALYSIS;
     if (rhs < 1 || !b || !x || (layout != SPTRSV_COL_MAJOR && layout != SPTRSV_ROW_MAJOR)) return SPTRSV_ERR_INVALID_ARG;
@@ -391,8 +518,10 @@ int Handle::solve(const sptrsv_opts* o_in, const double* b, double* x, int rhs, 
     int rc;
     if ((rc = prepare(o, rhs, layout))) return rc;
     last_mixed = o.precision == SPTRSV_PREC_MIXED;
+    last_cond = false;
     // profiled solves launch directly: their per-step events are timed from the host stream
     if (!use_graphs || profiling) return enqueue(o, b, x, rhs, layout);
+    const bool cond = cond_eligible(o, rhs);
     GraphKey key;
     key.o = o;
     key.b = b;
@@ -405,8 +534,33 @@ int Handle::solve(const sptrsv_opts* o_in, const double* b, double* x, int rhs, 
         if (g.key.same(key)) {
             CUDA_TRY(cudaGraphLaunch(g.exec, st));
             launches += g.kernels;
+            last_cond = cond;
+            cond_fixed_kernels = g.kernels;
             return 0;
         }
+    }
+    if (cond) {
+        cudaGraphExec_t exec = nullptr;
+        int64_t fixed = 0;
+        rc = build_cond_graph(o, b, x, rhs, layout, &exec, &fixed);
+        if (!rc && exec) {
+            GraphEntry ge;
+            ge.key = key;
+            ge.exec = exec;
+            ge.kernels = fixed;
+            if (graphs.size() >= 16) {
+                cudaGraphExecDestroy(graphs.front().exec);
+                graphs.erase(graphs.begin());
+            }
+            graphs.push_back(ge);
+            CUDA_TRY(cudaGraphLaunch(exec, st));
+            launches += fixed;
+            last_cond = true;
+            cond_fixed_kernels = fixed;
+            return 0;
+        }
+        // conditional nodes unavailable: fall through to the flat graph
+        (void)cudaGetLastError();
     }
     const int64_t before = launches;
     CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
@@ -445,7 +599,13 @@ int Handle::sync() {
     if (c.status) return c.status;
     if (last_mixed) {
         last_steps = c.steps;
+        last_sweeps = c.inner_total;
         last_res = c.rel_res;
+        if (last_cond) {
+            // per outer iteration: residual, test, axpy; per inner pair: two sweeps + test
+            launches += 3ll * (c.steps + 1) + c.inner_total + c.inner_total / 2;
+            last_cond = false;
+        }
         if (!c.done) return SPTRSV_ERR_NOT_CONVERGED;
     }
     return 0;
@@ -484,7 +644,7 @@ Handle::~Handle() {
     if (prof0) cudaEventDestroy(prof0);
     DevBuf* bufs[] = {&own_rp, &own_col, &own_val, &val32, &invd, &invd32, &in_degree, &levels, &level_ptr,
                       &level_rows, &stats, &csc_ptr, &csc_row, &csc_val, &scratch, &xw, &bw, &r32, &d32a, &d32b,
-                      &norms, &indeg_work, &left, &db, &dx, &flush};
+                      &norms, &indeg_work, &left, &db, &dx, &flush, &offdiag};
     for (DevBuf* b : bufs) b->release();
     if (ctl) cudaFree(ctl);
     if (ev0) cudaEventDestroy(ev0);
@@ -510,6 +670,8 @@ void sptrsv_default_opts(sptrsv_opts* o) {
     o->max_refine = 8;
     o->tol = 1e-12;
     o->spin_budget_ns = sptrsv::kDefaultBudgetNs;
+    o->resident_warps = 0;
+    o->inner_tol_exp = 6;
 }
 
 const char* sptrsv_status_string(int s) {
@@ -692,9 +854,10 @@ int sptrsv_sync(sptrsv_handle hh) {
     return h->sync();
 }
 
-int sptrsv_last_refine(sptrsv_handle hh, int* steps, double* rel_residual) {
+int sptrsv_last_refine(sptrsv_handle hh, int* steps, int* inner_sweeps, double* rel_residual) {
     H();
     if (steps) *steps = h->last_steps;
+    if (inner_sweeps) *inner_sweeps = h->last_sweeps;
     if (rel_residual) *rel_residual = h->last_res;
     return 0;
 }

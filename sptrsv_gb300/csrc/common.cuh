@@ -37,7 +37,10 @@ struct Ctl {
     double bnorm2;         // MIXED: ||b||^2
     double rel_res;        // MIXED: last relative residual
     unsigned int ticket2;  // second ticket (analysis kernels)
-    int pad[3];
+    unsigned int dmax_bits;  // MIXED + JACOBI: max |d| of the last checked sweep (float bits)
+    unsigned int dchg_bits;  // MIXED + JACOBI: max |d_new - d_old| of the last checked sweep
+    int inner_count;       // MIXED + JACOBI: sweeps of the current inner solve
+    int inner_total;       // MIXED + JACOBI: sweeps over the whole solve
 };
 
 template <typename T> struct Pend;

@@ -5,6 +5,7 @@
 #include <vector>
 #include <cuda_runtime.h>
 #include "common.cuh"
+#include "kernels.cuh"
 
 namespace sptrsv {
 
@@ -28,6 +29,7 @@ struct GraphKey {
         return o.schedule == k.o.schedule && o.precision == k.o.precision && o.rows_per_warp == k.o.rows_per_warp &&
                o.rhs_tile == k.o.rhs_tile && o.inner == k.o.inner && o.inner_sweeps == k.o.inner_sweeps &&
                o.max_refine == k.o.max_refine && o.tol == k.o.tol && o.spin_budget_ns == k.o.spin_budget_ns &&
+               o.resident_warps == k.o.resident_warps && o.inner_tol_exp == k.o.inner_tol_exp &&
                b == k.b && x == k.x && rhs == k.rhs && layout == k.layout && warps == k.warps && prof == k.prof;
     }
 };
@@ -63,12 +65,17 @@ struct Handle {
     double max_ratio = 0.0, mean_len = 0.0, std_len = 0.0;
     DevBuf csc_ptr, csc_row, csc_val;
     bool have_csc = false;
+    DevBuf offdiag;        // interleaved FP32 off-diagonals for the Jacobi sweeps
+    bool have_offdiag = false;
 
     // work
     DevBuf scratch, xw, bw, r32, d32a, d32b, norms, indeg_work, left, db, dx, flush;
     unsigned flush_byte = 1;
     bool last_mixed = false;
+    bool last_cond = false;       // the last solve ran the conditional (device-looped) graph
+    int64_t cond_fixed_kernels = 0;
     int last_steps = 0;
+    int last_sweeps = 0;
     double last_res = 0.0;
     std::vector<GraphEntry> graphs;
 
@@ -93,6 +100,12 @@ struct Handle {
     sptrsv_opts resolve(const sptrsv_opts* o, int rhs) const;
     int prepare(const sptrsv_opts& o, int rhs, int layout);
     int enqueue(const sptrsv_opts& o, const double* b, double* x, int rhs, int layout);
+    int ensure_offdiag();
+    bool cond_eligible(const sptrsv_opts& o, int rhs) const;
+    int refine_args(const sptrsv_opts& o, const double* b, double* x, int rhs, RefineArgs* ra);
+    int build_cond_graph(const sptrsv_opts& o, const double* b, double* x, int rhs, int layout,
+                         cudaGraphExec_t* out, int64_t* fixed_kernels);
+    int resident_warps(const sptrsv_opts& o) const;
     int solve(const sptrsv_opts* o, const double* b, double* x, int rhs, int layout);
     int sync();
 };

@@ -80,6 +80,7 @@ struct RefineArgs {
     const float* val32;
     const double* invd;
     const float* invd32;
+    const int2* off;   // interleaved (column, FP32 value) off-diagonals, or nullptr
     const double* b;   // row-major n x rhs
     double* x;         // row-major n x rhs
     float* r32;        // n x rhs
@@ -93,12 +94,17 @@ struct RefineArgs {
     cudaStream_t st;
     int64_t* launches;
 };
+int launch_build_offdiag(int n, const int* rp, const int* col, const double* val, int2* off, int sm_count,
+                         cudaStream_t st, int64_t* launches);
 int launch_refine_init(const RefineArgs& a);
 int launch_residual(const RefineArgs& a, bool jacobi_seed, int final_check);
 int launch_check(const RefineArgs& a, int step, bool reset_ticket);
-int launch_jacobi_sweep(const RefineArgs& a, int src, bool last);
+int launch_check_outer(const RefineArgs& a, int max_refine, cudaGraphConditionalHandle ho,
+                       cudaGraphConditionalHandle hi);
+int launch_check_inner(const RefineArgs& a, float eps, int max_sweeps, cudaGraphConditionalHandle hi);
+int launch_jacobi_sweep(const RefineArgs& a, int src, bool last, bool stats);
 int launch_axpy_pending(const RefineArgs& a, int src);
 int launch_exact_inner(const RefineArgs& a, int schedule, int rows_per_warp, int dst, int max_level,
-                       const int* lptr, const int* lrows);
+                       const int* lptr, const int* lrows, int warps);
 
 }  // namespace sptrsv

@@ -1,24 +1,37 @@
 // refine.cu -- FP32 bulk solves with FP64 iterative refinement.
 //
-// One refinement step, all on the device (no host round trip, so the whole sequence can be
-// captured in a CUDA graph):
-//   r   = b - U x               FP64 SpMV over the FP64 values (k_residual); ||r_c||^2 per
-//                               column is accumulated for the convergence test; r is also
-//                               stored in FP32 as the inner right-hand side;
-//   test                        k_check: rel = max_c ||r_c|| / ||b_c||; once rel <= tol the
-//                               `done` flag is raised and every later kernel returns at once;
+// One refinement step, all on the device (no host round trip, so the whole solve is one
+// CUDA graph launch):
+//   r   = b - U x               FP64 SpMV over the FP64 values (k_residual_*); ||r_c||^2 per
+//                               column for the convergence test; r is also stored in FP32 as
+//                               the inner right-hand side, and d0 = D^-1 r seeds the sweeps;
+//   test                        rel = max_c ||r_c|| / ||b_c||; once rel <= tol the `done` flag
+//                               is raised (flat graphs: every later kernel returns at once;
+//                               conditional graphs: the outer WHILE node stops);
 //   d  ~= U^{-1} r              FP32 inner solve, either
-//                                 JACOBI: d <- D^{-1} (r - N d), `inner_sweeps` sweeps over
-//                                 the FP32 values (fully parallel; converges for any
-//                                 triangular U because N is nilpotent, fast when U is
-//                                 diagonally dominant), or
+//                                 JACOBI: d <- D^-1 (r - N d) sweeps over an interleaved
+//                                 (column, FP32 value) copy of the off-diagonals, until the
+//                                 largest change is below 10^-e of the largest |d| (the inner
+//                                 WHILE node) -- fully parallel; it converges for any
+//                                 triangular U because N is nilpotent, and fast when U is
+//                                 diagonally dominant -- or
 //                                 an exact FP32 sync-free / level-set solve (solve.cu);
-//   x  += d                     FP64 update (fused into the last Jacobi sweep).
+//   x  += d                     FP64 update.
 // x starts at 0, so the first residual is b itself.
+//
+// Row-streaming kernels for short rows use warp tiles of 32 consecutive rows: the warp copies
+// the tile's entries into shared memory with independent coalesced loads (16-byte vectors for
+// the interleaved FP32 copy), then each lane sums its own row sequentially (deterministic).
+// Tiles with more than kTileMax entries read straight from global memory; long-row matrices
+// use the warp-per-row kernels (LPR lanes per row).
 #include "common.cuh"
 #include "kernels.cuh"
 
 namespace sptrsv {
+
+constexpr int kTileMax = 512;   // staged entries per warp
+constexpr int kJacWarps = 8;    // warps per block, Jacobi tile kernel (4 KiB stage per warp)
+constexpr int kResWarps = 4;    // warps per block, residual tile kernel (6 KiB stage per warp)
 
 __device__ __forceinline__ bool is_done(const Ctl* ctl) { return *(volatile const int*)&ctl->done != 0; }
 
@@ -47,8 +60,75 @@ __global__ void k_colnorm2(int n, int rhs, const double* __restrict__ b, double*
     for (int c = threadIdx.x; c < rhs; c += blockDim.x) atomicAdd(out + c, acc[c]);
 }
 
-// r = b - U x; r32 = (float)r; seed: d0 = D^{-1} r (Jacobi) or d0 = pending (exact inner).
-// rhs == 1: LPR lanes per row.
+// Interleaved FP32 off-diagonals: entry k of row i (k > rp[i]) goes to slot k - i - 1, so the
+// off-diagonals of row i occupy [rp[i] - i, rp[i+1] - i - 1).
+__global__ void k_build_offdiag(int n, const int* __restrict__ rp, const int* __restrict__ col,
+                                const double* __restrict__ val, int2* __restrict__ off) {
+    const int lane = threadIdx.x & 31;
+    for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += (gridDim.x * blockDim.x) >> 5)
+        for (int k = rp[i] + 1 + lane; k < rp[i + 1]; k += 32)
+            off[k - i - 1] = make_int2(col[k], __float_as_int((float)val[k]));
+}
+
+__device__ __forceinline__ void seed_out(int seed, float* d0, size_t p, double r, double invd) {
+    if (seed == 1) d0[p] = (float)(r * invd);
+    else if (seed == 2) d0[p] = __uint_as_float(kPend32);
+}
+
+// r = b - U x (rhs == 1), warp tiles of 32 rows staged in shared memory.
+__global__ void __launch_bounds__(kResWarps * 32) k_residual_tile(int n, const int* __restrict__ rp,
+                                                                  const int* __restrict__ col,
+                                                                  const double* __restrict__ val,
+                                                                  const double* __restrict__ invd,
+                                                                  const double* __restrict__ b,
+                                                                  const double* __restrict__ x, float* __restrict__ r32,
+                                                                  float* __restrict__ d0, int seed,
+                                                                  double* __restrict__ rn2, const Ctl* ctl) {
+    __shared__ int s_col[kResWarps][kTileMax];
+    __shared__ double s_val[kResWarps][kTileMax];
+    __shared__ double s_acc;
+    if (is_done(ctl)) return;
+    if (threadIdx.x == 0) s_acc = 0.0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int* sc = s_col[w];
+    double* sv = s_val[w];
+    double acc = 0.0;
+    for (int t = blockIdx.x * kResWarps + w; t * 32 < n; t += gridDim.x * kResWarps) {
+        const int r0 = t * 32, i = r0 + lane;
+        const int s = rp[min(i, n)];
+        int e = __shfl_down_sync(0xffffffffu, s, 1);
+        if (lane == 31) e = rp[min(r0 + 32, n)];
+        const int E0 = __shfl_sync(0xffffffffu, s, 0), E1 = __shfl_sync(0xffffffffu, e, 31);
+        double sum = 0.0;
+        if (E1 - E0 <= kTileMax) {
+            for (int q = lane; q < E1 - E0; q += 32) {
+                sc[q] = __ldg(col + E0 + q);
+                sv[q] = __ldg(val + E0 + q);
+            }
+            __syncwarp();
+            if (i < n) {
+#pragma unroll 4
+                for (int k = s - E0; k < e - E0; ++k) sum = fma(sv[k], __ldg(x + sc[k]), sum);
+            }
+            __syncwarp();
+        } else if (i < n) {
+            for (int k = s; k < e; ++k) sum = fma(__ldg(val + k), __ldg(x + __ldg(col + k)), sum);
+        }
+        if (i < n) {
+            const double r = b[i] - sum;
+            r32[i] = (float)r;
+            seed_out(seed, d0, i, r, invd[i]);
+            acc += r * r;
+        }
+    }
+    acc = warp_sum(acc);
+    if (lane == 0) atomicAdd(&s_acc, acc);
+    __syncthreads();
+    if (threadIdx.x == 0) atomicAdd(rn2, s_acc);
+}
+
+// r = b - U x (rhs == 1), LPR lanes per row (long rows).
 template <int LPR>
 __global__ void __launch_bounds__(256) k_residual_v(int n, const int* __restrict__ rp, const int* __restrict__ col,
                                                     const double* __restrict__ val, const double* __restrict__ invd,
@@ -74,12 +154,11 @@ __global__ void __launch_bounds__(256) k_residual_v(int n, const int* __restrict
         if (gl == 0) {
             const double r = b[i] - sum;
             r32[i] = (float)r;
-            if (seed == 1) d0[i] = (float)(r * invd[i]);
-            else if (seed == 2) d0[i] = __uint_as_float(kPend32);
+            seed_out(seed, d0, i, r, invd[i]);
             acc += r * r;
         }
     }
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    acc = warp_sum(acc);
     if (lane == 0) atomicAdd(&s_acc, acc);
     __syncthreads();
     if (threadIdx.x == 0) atomicAdd(rn2, s_acc);
@@ -93,8 +172,8 @@ __global__ void __launch_bounds__(256) k_residual_m(int n, int rhs, const int* _
                                                     float* __restrict__ d0, int seed, double* __restrict__ rn2,
                                                     const Ctl* ctl) {
     if (is_done(ctl)) return;
-    extern __shared__ double s_acc[];
-    for (int c = threadIdx.x; c < rhs; c += blockDim.x) s_acc[c] = 0.0;
+    extern __shared__ double s_accm[];
+    for (int c = threadIdx.x; c < rhs; c += blockDim.x) s_accm[c] = 0.0;
     __syncthreads();
     const int lane = threadIdx.x & 31;
     const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -108,18 +187,15 @@ __global__ void __launch_bounds__(256) k_residual_m(int n, int rhs, const int* _
             const size_t p = (size_t)i * rhs + c;
             const double r = b[p] - sum;
             r32[p] = (float)r;
-            if (seed == 1) d0[p] = (float)(r * di);
-            else if (seed == 2) d0[p] = __uint_as_float(kPend32);
-            atomicAdd(&s_acc[c], r * r);
+            seed_out(seed, d0, p, r, di);
+            atomicAdd(&s_accm[c], r * r);
         }
     }
     __syncthreads();
-    for (int c = threadIdx.x; c < rhs; c += blockDim.x) atomicAdd(rn2 + c, s_acc[c]);
+    for (int c = threadIdx.x; c < rhs; c += blockDim.x) atomicAdd(rn2 + c, s_accm[c]);
 }
 
-__global__ void k_check(int rhs, double* rn2, const double* bn2, Ctl* ctl, double tol, int step, int reset_ticket) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    if (ctl->done) return;
+__device__ __forceinline__ double rel_of(int rhs, double* rn2, const double* bn2) {
     double rel = 0.0;
     for (int c = 0; c < rhs; ++c) {
         const double r = rn2[c], bb = bn2[c];
@@ -127,25 +203,149 @@ __global__ void k_check(int rhs, double* rn2, const double* bn2, Ctl* ctl, doubl
         rel = fmax(rel, q);
         rn2[c] = 0.0;
     }
+    return rel;
+}
+
+// Flat graphs: the convergence test of step `step`.
+__global__ void k_check(int rhs, double* rn2, const double* bn2, Ctl* ctl, double tol, int step, int reset_ticket) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    if (ctl->done) return;
+    const double rel = rel_of(rhs, rn2, bn2);
     ctl->rel_res = rel;
     ctl->steps = step;
     if (rel <= tol) ctl->done = 1;
     if (reset_ticket) ctl->ticket = 0u;
 }
 
-// One Jacobi sweep: dst = D^{-1} (r - N src); last: x += D^{-1} (r - N src) instead.
+// Conditional graphs: the test at the top of every outer iteration.  Continues (and arms the
+// inner loop) while rel > tol and fewer than max_refine corrections were applied.
+__global__ void k_check_outer(int rhs, double* rn2, const double* bn2, Ctl* ctl, double tol, int max_refine,
+                              cudaGraphConditionalHandle h_outer, cudaGraphConditionalHandle h_inner) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const double rel = rel_of(rhs, rn2, bn2);
+    ctl->rel_res = rel;
+    const int step = ctl->steps;
+    const bool stop = rel <= tol || step >= max_refine;
+    if (rel <= tol) ctl->done = 1;
+    ctl->inner_count = 0;
+    ctl->dmax_bits = 0u;
+    ctl->dchg_bits = 0u;
+    if (stop) {
+        cudaGraphSetConditional(h_outer, 0);
+        cudaGraphSetConditional(h_inner, 0);
+    } else {
+        ctl->steps = step + 1;
+        cudaGraphSetConditional(h_inner, 1);
+    }
+}
+
+// Conditional graphs: after each pair of sweeps.  Stops the inner loop once the largest
+// change is at most eps times the largest |d|, or after max_sweeps sweeps.
+__global__ void k_check_inner(Ctl* ctl, float eps, int max_sweeps, cudaGraphConditionalHandle h_inner) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const float dmax = __uint_as_float(ctl->dmax_bits), dchg = __uint_as_float(ctl->dchg_bits);
+    const int cnt = ctl->inner_count + 2;
+    ctl->inner_count = cnt;
+    ctl->inner_total += 2;
+    ctl->dmax_bits = 0u;
+    ctl->dchg_bits = 0u;
+    if (!(dchg > eps * dmax) || cnt >= max_sweeps) cudaGraphSetConditional(h_inner, 0);
+}
+
+__device__ __forceinline__ void reduce_stats(float dmax, float dchg, Ctl* ctl, unsigned* s_max) {
+    for (int o = 16; o > 0; o >>= 1) {
+        dmax = fmaxf(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
+        dchg = fmaxf(dchg, __shfl_xor_sync(0xffffffffu, dchg, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMax(&s_max[0], __float_as_uint(dmax));
+        atomicMax(&s_max[1], __float_as_uint(dchg));
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        atomicMax(&ctl->dmax_bits, s_max[0]);
+        atomicMax(&ctl->dchg_bits, s_max[1]);
+    }
+}
+
+// One FP32 Jacobi sweep over warp tiles: dst = D^-1 (r - N src), or x += that when `last`.
+// stats: accumulate max|d| and max|d - src| (non-negative floats order like their bits).
+__global__ void __launch_bounds__(kJacWarps * 32) k_jacobi_tile(int n, const int* __restrict__ rp,
+                                                                const int2* __restrict__ off,
+                                                                const float* __restrict__ invd,
+                                                                const float* __restrict__ r,
+                                                                const float* __restrict__ src, float* __restrict__ dst,
+                                                                double* __restrict__ x, int last, int stats, Ctl* ctl) {
+    __shared__ __align__(16) int2 stage[kJacWarps][kTileMax];
+    __shared__ unsigned s_max[2];
+    if (is_done(ctl)) return;
+    if (threadIdx.x < 2) s_max[threadIdx.x] = 0u;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int2* sb = stage[w];
+    float dmax = 0.f, dchg = 0.f;
+    for (int t = blockIdx.x * kJacWarps + w; t * 32 < n; t += gridDim.x * kJacWarps) {
+        const int r0 = t * 32, i = r0 + lane;
+        const int ii = min(i, n);
+        const int s = rp[ii] - ii;  // first off-diagonal slot of row i
+        int e = __shfl_down_sync(0xffffffffu, s, 1);
+        if (lane == 31) {
+            const int j = min(r0 + 32, n);
+            e = rp[j] - j;
+        }
+        const int E0 = __shfl_sync(0xffffffffu, s, 0), E1 = __shfl_sync(0xffffffffu, e, 31);
+        float sum = 0.f;
+        const int a0 = E0 & ~1;  // 16-byte aligned start (pairs of int2)
+        if (E1 - a0 <= kTileMax) {
+            const int npair = (E1 - a0 + 1) >> 1;
+            const int4* v4 = reinterpret_cast<const int4*>(off + a0);
+            int4* s4 = reinterpret_cast<int4*>(sb);
+            for (int q = lane; q < npair; q += 32) s4[q] = __ldg(v4 + q);
+            __syncwarp();
+            if (i < n) {
+#pragma unroll 4
+                for (int k = s - a0; k < e - a0; ++k) {
+                    const int2 p = sb[k];
+                    sum = fmaf(__int_as_float(p.y), __ldg(src + p.x), sum);
+                }
+            }
+            __syncwarp();
+        } else if (i < n) {
+            for (int k = s; k < e; ++k) {
+                const int2 p = __ldg(off + k);
+                sum = fmaf(__int_as_float(p.y), __ldg(src + p.x), sum);
+            }
+        }
+        if (i < n) {
+            const float d = (r[i] - sum) * invd[i];
+            if (stats) {
+                dmax = fmaxf(dmax, fabsf(d));
+                dchg = fmaxf(dchg, fabsf(d - src[i]));
+            }
+            if (last) x[i] += (double)d;
+            else dst[i] = d;
+        }
+    }
+    if (stats) reduce_stats(dmax, dchg, ctl, s_max);
+}
+
+// Same sweep, LPR lanes per row over the CSR FP32 values (long rows).
 template <int LPR>
 __global__ void __launch_bounds__(256) k_jacobi_v(int n, const int* __restrict__ rp, const int* __restrict__ col,
                                                   const float* __restrict__ val, const float* __restrict__ invd,
                                                   const float* __restrict__ r, const float* __restrict__ src,
                                                   float* __restrict__ dst, double* __restrict__ x, int last,
-                                                  const Ctl* ctl) {
+                                                  int stats, Ctl* ctl) {
+    __shared__ unsigned s_max[2];
     if (is_done(ctl)) return;
+    if (threadIdx.x < 2) s_max[threadIdx.x] = 0u;
+    __syncthreads();
     const int lane = threadIdx.x & 31;
     const int gl = lane % LPR;
     const unsigned gmask = (LPR == 32) ? 0xffffffffu : (((1u << LPR) - 1u) << ((lane / LPR) * LPR));
     const long long gid = ((long long)blockIdx.x * blockDim.x + threadIdx.x) / LPR;
     const long long gstride = ((long long)gridDim.x * blockDim.x) / LPR;
+    float dmax = 0.f, dchg = 0.f;
     for (long long i = gid; i < n; i += gstride) {
         const int s = rp[i], e = rp[i + 1];
         float sum = 0.f;
@@ -154,21 +354,30 @@ __global__ void __launch_bounds__(256) k_jacobi_v(int n, const int* __restrict__
         for (int o = LPR / 2; o > 0; o >>= 1) sum += __shfl_xor_sync(gmask, sum, o);
         if (gl == 0) {
             const float d = (r[i] - sum) * invd[i];
+            if (stats) {
+                dmax = fmaxf(dmax, fabsf(d));
+                dchg = fmaxf(dchg, fabsf(d - src[i]));
+            }
             if (last) x[i] += (double)d;
             else dst[i] = d;
         }
     }
+    if (stats) reduce_stats(dmax, dchg, ctl, s_max);
 }
 
 __global__ void __launch_bounds__(256) k_jacobi_m(int n, int rhs, const int* __restrict__ rp,
                                                   const int* __restrict__ col, const float* __restrict__ val,
                                                   const float* __restrict__ invd, const float* __restrict__ r,
                                                   const float* __restrict__ src, float* __restrict__ dst,
-                                                  double* __restrict__ x, int last, const Ctl* ctl) {
+                                                  double* __restrict__ x, int last, int stats, Ctl* ctl) {
+    __shared__ unsigned s_max[2];
     if (is_done(ctl)) return;
+    if (threadIdx.x < 2) s_max[threadIdx.x] = 0u;
+    __syncthreads();
     const int lane = threadIdx.x & 31;
     const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const long long ws = ((long long)gridDim.x * blockDim.x) >> 5;
+    float dmax = 0.f, dchg = 0.f;
     for (long long i = w; i < n; i += ws) {
         const int s = rp[i], e = rp[i + 1];
         const float di = invd[i];
@@ -177,10 +386,15 @@ __global__ void __launch_bounds__(256) k_jacobi_m(int n, int rhs, const int* __r
             for (int k = s + 1; k < e; ++k) sum = fmaf(val[k], src[(size_t)col[k] * rhs + c], sum);
             const size_t p = (size_t)i * rhs + c;
             const float d = (r[p] - sum) * di;
+            if (stats) {
+                dmax = fmaxf(dmax, fabsf(d));
+                dchg = fmaxf(dchg, fabsf(d - src[p]));
+            }
             if (last) x[p] += (double)d;
             else dst[p] = d;
         }
     }
+    if (stats) reduce_stats(dmax, dchg, ctl, s_max);
 }
 
 __global__ void k_axpy_f32(size_t count, const float* __restrict__ d, double* __restrict__ x, const Ctl* ctl) {
@@ -202,8 +416,19 @@ static int lpr_for(int n, int nnz) {
     if (mean <= 24.0) return 16;
     return 32;
 }
+// warp tiles pay off while a 32-row tile usually fits the stage
+static bool short_rows(const RefineArgs& a) { return a.rhs == 1 && (double)a.nnz / a.n <= 14.0; }
+static bool use_tiles(const RefineArgs& a) { return short_rows(a) && a.off; }
 
 static int stream_grid(int sm_count) { return sm_count * 8; }
+
+int launch_build_offdiag(int n, const int* rp, const int* col, const double* val, int2* off, int sm_count,
+                         cudaStream_t st, int64_t* launches) {
+    k_build_offdiag<<<sm_count * 8, 256, 0, st>>>(n, rp, col, val, off);
+    ++*launches;
+    CUDA_TRY(cudaGetLastError());
+    return 0;
+}
 
 int launch_refine_init(const RefineArgs& a) {
     CUDA_TRY(cudaMemsetAsync(a.x, 0, sizeof(double) * (size_t)a.n * a.rhs, a.st));
@@ -219,7 +444,10 @@ int launch_refine_init(const RefineArgs& a) {
 int launch_residual(const RefineArgs& a, bool jacobi_seed, int final_check) {
     const int seed = final_check ? 0 : (jacobi_seed ? 1 : 2);
     const int grid = stream_grid(a.sm_count);
-    if (a.rhs == 1) {
+    if (short_rows(a)) {
+        k_residual_tile<<<a.sm_count * 16, kResWarps * 32, 0, a.st>>>(a.n, a.rp, a.col, a.val, a.invd, a.b, a.x,
+                                                                      a.r32, a.d32[0], seed, a.rn2, a.ctl);
+    } else if (a.rhs == 1) {
         switch (lpr_for(a.n, a.nnz)) {
             case 4: k_residual_v<4><<<grid, 256, 0, a.st>>>(a.n, a.rp, a.col, a.val, a.invd, a.b, a.x, a.r32, a.d32[0], seed, a.rn2, a.ctl); break;
             case 8: k_residual_v<8><<<grid, 256, 0, a.st>>>(a.n, a.rp, a.col, a.val, a.invd, a.b, a.x, a.r32, a.d32[0], seed, a.rn2, a.ctl); break;
@@ -242,19 +470,39 @@ int launch_check(const RefineArgs& a, int step, bool reset_ticket) {
     return 0;
 }
 
-int launch_jacobi_sweep(const RefineArgs& a, int src, bool last) {
+int launch_check_outer(const RefineArgs& a, int max_refine, cudaGraphConditionalHandle ho,
+                       cudaGraphConditionalHandle hi) {
+    k_check_outer<<<1, 32, 0, a.st>>>(a.rhs, a.rn2, a.bn2, a.ctl, a.tol, max_refine, ho, hi);
+    ++*a.launches;
+    CUDA_TRY(cudaGetLastError());
+    return 0;
+}
+
+int launch_check_inner(const RefineArgs& a, float eps, int max_sweeps, cudaGraphConditionalHandle hi) {
+    k_check_inner<<<1, 32, 0, a.st>>>(a.ctl, eps, max_sweeps, hi);
+    ++*a.launches;
+    CUDA_TRY(cudaGetLastError());
+    return 0;
+}
+
+int launch_jacobi_sweep(const RefineArgs& a, int src, bool last, bool stats) {
     const int grid = stream_grid(a.sm_count);
     const float* s = a.d32[src];
     float* d = a.d32[src ^ 1];
-    if (a.rhs == 1) {
+    const int st_flag = stats ? 1 : 0;
+    if (use_tiles(a)) {
+        k_jacobi_tile<<<a.sm_count * 8, kJacWarps * 32, 0, a.st>>>(a.n, a.rp, a.off, a.invd32, a.r32, s, d, a.x, last,
+                                                                  st_flag, a.ctl);
+    } else if (a.rhs == 1) {
         switch (lpr_for(a.n, a.nnz)) {
-            case 4: k_jacobi_v<4><<<grid, 256, 0, a.st>>>(a.n, a.rp, a.col, a.val32, a.invd32, a.r32, s, d, a.x, last, a.ctl); break;
-            case 8: k_jacobi_v<8><<<grid, 256, 0, a.st>>>(a.n, a.rp, a.col, a.val32, a.invd32, a.r32, s, d, a.x, last, a.ctl); break;
-            case 16: k_jacobi_v<16><<<grid, 256, 0, a.st>>>(a.n, a.rp, a.col, a.val32, a.invd32, a.r32, s, d, a.x, last, a.ctl); break;
-            default: k_jacobi_v<32><<<grid, 256, 0, a.st>>>(a.n, a.rp, a.col, a.val32, a.invd32, a.r32, s, d, a.x, last, a.ctl); break;
+            case 4: k_jacobi_v<4><<<grid, 256, 0, a.st>>>(a.n, a.rp, a.col, a.val32, a.invd32, a.r32, s, d, a.x, last, st_flag, a.ctl); break;
+            case 8: k_jacobi_v<8><<<grid, 256, 0, a.st>>>(a.n, a.rp, a.col, a.val32, a.invd32, a.r32, s, d, a.x, last, st_flag, a.ctl); break;
+            case 16: k_jacobi_v<16><<<grid, 256, 0, a.st>>>(a.n, a.rp, a.col, a.val32, a.invd32, a.r32, s, d, a.x, last, st_flag, a.ctl); break;
+            default: k_jacobi_v<32><<<grid, 256, 0, a.st>>>(a.n, a.rp, a.col, a.val32, a.invd32, a.r32, s, d, a.x, last, st_flag, a.ctl); break;
         }
     } else {
-        k_jacobi_m<<<grid, 256, 0, a.st>>>(a.n, a.rhs, a.rp, a.col, a.val32, a.invd32, a.r32, s, d, a.x, last, a.ctl);
+        k_jacobi_m<<<grid, 256, 0, a.st>>>(a.n, a.rhs, a.rp, a.col, a.val32, a.invd32, a.r32, s, d, a.x, last,
+                                           st_flag, a.ctl);
     }
     ++*a.launches;
     CUDA_TRY(cudaGetLastError());
@@ -271,7 +519,7 @@ int launch_axpy_pending(const RefineArgs& a, int src) {
 }
 
 int launch_exact_inner(const RefineArgs& a, int schedule, int rows_per_warp, int dst, int max_level,
-                       const int* lptr, const int* lrows) {
+                       const int* lptr, const int* lrows, int warps) {
     SolveArgs s{};
     s.n = a.n;
     s.rp = a.rp;
@@ -284,7 +532,7 @@ int launch_exact_inner(const RefineArgs& a, int schedule, int rows_per_warp, int
     s.ctl = a.ctl;
     s.budget = a.budget;
     s.sm_count = a.sm_count;
-    s.warps = 0;
+    s.warps = warps;
     s.st = a.st;
     s.launches = a.launches;
     if (schedule == SPTRSV_SCHED_LEVELSET) return launch_levelset(true, s, max_level, lptr, lrows);
