@@ -41,7 +41,15 @@ __global__ void k_colnorm2(int n, int rhs, const double* __restrict__ b, double*
     for (int c = threadIdx.x; c < rhs; c += blockDim.x) acc[c] = 0.0;
     __syncthreads();
     const int per_pass = (blockDim.x / rhs) > 0 ? (blockDim.x / rhs) : 0;
-    if (per_pass > 0 && (int)threadIdx.x < per_pass * rhs) {
+    if (rhs == 1) {
+        double s = 0.0;
+        for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+            const double v = b[i];
+            s += v * v;
+        }
+        s = warp_sum(s);
+        if ((threadIdx.x & 31) == 0) atomicAdd(&acc[0], s);
+    } else if (per_pass > 0 && (int)threadIdx.x < per_pass * rhs) {
         const int c = threadIdx.x % rhs, r0 = threadIdx.x / rhs;
         double s = 0.0;
         for (long long i = (long long)blockIdx.x * per_pass + r0; i < n; i += (long long)gridDim.x * per_pass) {
@@ -422,6 +430,14 @@ static bool use_tiles(const RefineArgs& a) { return short_rows(a) && a.off; }
 
 static int stream_grid(int sm_count) { return sm_count * 8; }
 
+// One resident wave: blocks per SM from the occupancy calculator, times the SM count, so that a
+// grid-stride kernel never leaves a partial second wave.
+static int resident_grid(const void* fn, int block, int sm_count) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, block, 0) != cudaSuccess || per_sm < 1) per_sm = 1;
+    return per_sm * sm_count;
+}
+
 int launch_build_offdiag(int n, const int* rp, const int* col, const double* val, int2* off, int sm_count,
                          cudaStream_t st, int64_t* launches) {
     k_build_offdiag<<<sm_count * 8, 256, 0, st>>>(n, rp, col, val, off);
@@ -445,7 +461,9 @@ int launch_residual(const RefineArgs& a, bool jacobi_seed, int final_check) {
     const int seed = final_check ? 0 : (jacobi_seed ? 1 : 2);
     const int grid = stream_grid(a.sm_count);
     if (short_rows(a)) {
-        k_residual_tile<<<a.sm_count * 16, kResWarps * 32, 0, a.st>>>(a.n, a.rp, a.col, a.val, a.invd, a.b, a.x,
+        static int grid_rt = 0;
+        if (!grid_rt) grid_rt = resident_grid((const void*)k_residual_tile, kResWarps * 32, a.sm_count);
+        k_residual_tile<<<grid_rt, kResWarps * 32, 0, a.st>>>(a.n, a.rp, a.col, a.val, a.invd, a.b, a.x,
                                                                       a.r32, a.d32[0], seed, a.rn2, a.ctl);
     } else if (a.rhs == 1) {
         switch (lpr_for(a.n, a.nnz)) {
@@ -491,7 +509,9 @@ int launch_jacobi_sweep(const RefineArgs& a, int src, bool last, bool stats) {
     float* d = a.d32[src ^ 1];
     const int st_flag = stats ? 1 : 0;
     if (use_tiles(a)) {
-        k_jacobi_tile<<<a.sm_count * 8, kJacWarps * 32, 0, a.st>>>(a.n, a.rp, a.off, a.invd32, a.r32, s, d, a.x, last,
+        static int grid_jt = 0;
+        if (!grid_jt) grid_jt = resident_grid((const void*)k_jacobi_tile, kJacWarps * 32, a.sm_count);
+        k_jacobi_tile<<<grid_jt, kJacWarps * 32, 0, a.st>>>(a.n, a.rp, a.off, a.invd32, a.r32, s, d, a.x, last,
                                                                   st_flag, a.ctl);
     } else if (a.rhs == 1) {
         switch (lpr_for(a.n, a.nnz)) {
