@@ -371,9 +371,13 @@ int Handle::resident_warps(const sptrsv_opts& o) const {
 int Handle::ensure_offdiag() {
     if (have_offdiag) return 0;
     int rc;
+    const int kRoffPad = 64;
     if ((rc = offdiag.ensure(sizeof(int2) * ((size_t)(nnz - n) + 4)))) return rc;
+    if ((rc = roff.ensure(sizeof(int) * ((size_t)n + 1 + kRoffPad)))) return rc;
     CUDA_TRY(cudaMemsetAsync(offdiag.p, 0, sizeof(int2) * ((size_t)(nnz - n) + 4), st));
-    if ((rc = launch_build_offdiag(n, rp, col, val, offdiag.as<int2>(), sm_count, st, &launches))) return rc;
+    if ((rc = launch_build_offdiag(n, rp, col, val, offdiag.as<int2>(), roff.as<int>(), kRoffPad, sm_count, st,
+                                   &launches)))
+        return rc;
     CUDA_TRY(cudaStreamSynchronize(st));
     have_offdiag = true;
     return 0;
@@ -392,6 +396,8 @@ int Handle::refine_args(const sptrsv_opts& o, const double* b, double* x, int rh
     r.invd = invd.as<double>();
     r.invd32 = invd32.as<float>();
     r.off = (have_offdiag && rhs == 1) ? offdiag.as<int2>() : nullptr;
+    r.roff = (have_offdiag && rhs == 1) ? roff.as<int>() : nullptr;
+    r.sweep_kernel = sweep_kernel;
     r.b = b;
     r.x = x;
     r.r32 = r32.as<float>();
@@ -644,7 +650,7 @@ Handle::~Handle() {
     if (prof0) cudaEventDestroy(prof0);
     DevBuf* bufs[] = {&own_rp, &own_col, &own_val, &val32, &invd, &invd32, &in_degree, &levels, &level_ptr,
                       &level_rows, &stats, &csc_ptr, &csc_row, &csc_val, &scratch, &xw, &bw, &r32, &d32a, &d32b,
-                      &norms, &indeg_work, &left, &db, &dx, &flush, &offdiag};
+                      &norms, &indeg_work, &left, &db, &dx, &flush, &offdiag, &roff};
     for (DevBuf* b : bufs) b->release();
     if (ctl) cudaFree(ctl);
     if (ev0) cudaEventDestroy(ev0);
@@ -724,6 +730,8 @@ int sptrsv_create(sptrsv_handle* out, int device) {
     if (rc) { delete h; return rc; }
     const char* g = getenv("SPTRSV_NO_GRAPH");
     h->use_graphs = !(g && g[0] == '1');
+    const char* sk = getenv("SPTRSV_SWEEP_KERNEL");  // tuning override: "tile" = plain-load tiles
+    h->sweep_kernel = (sk && strcmp(sk, "tile") == 0) ? 1 : 0;
     *out = reinterpret_cast<sptrsv_handle>(h);
     return 0;
 }

@@ -48,6 +48,7 @@ struct Handle {
     int64_t launches = 0;
     Ctl* ctl = nullptr;
     bool use_graphs = true;
+    int sweep_kernel = 0;   // 0 bulk-copy pipelined sweeps, 1 warp tiles with plain loads
     int warps_override = 0;
 
     // matrix (device; either owned copies or caller-owned pointers)
@@ -66,6 +67,7 @@ struct Handle {
     DevBuf csc_ptr, csc_row, csc_val;
     bool have_csc = false;
     DevBuf offdiag;        // interleaved FP32 off-diagonals for the Jacobi sweeps
+    DevBuf roff;           // per-row first off-diagonal slot, padded by kRoffPad
     bool have_offdiag = false;
 
     // work

@@ -81,6 +81,8 @@ struct RefineArgs {
     const double* invd;
     const float* invd32;
     const int2* off;   // interleaved (column, FP32 value) off-diagonals, or nullptr
+    const int* roff;   // first off-diagonal slot of every row (rp[i] - i), padded, or nullptr
+    int sweep_kernel;  // 0 bulk-copy pipeline, 1 warp tiles with plain loads
     const double* b;   // row-major n x rhs
     double* x;         // row-major n x rhs
     float* r32;        // n x rhs
@@ -94,8 +96,8 @@ struct RefineArgs {
     cudaStream_t st;
     int64_t* launches;
 };
-int launch_build_offdiag(int n, const int* rp, const int* col, const double* val, int2* off, int sm_count,
-                         cudaStream_t st, int64_t* launches);
+int launch_build_offdiag(int n, const int* rp, const int* col, const double* val, int2* off, int* roff,
+                         int roff_pad, int sm_count, cudaStream_t st, int64_t* launches);
 int launch_refine_init(const RefineArgs& a);
 int launch_residual(const RefineArgs& a, bool jacobi_seed, int final_check);
 int launch_check(const RefineArgs& a, int step, bool reset_ticket);

@@ -78,8 +78,16 @@ __global__ void k_build_offdiag(int n, const int* __restrict__ rp, const int* __
             off[k - i - 1] = make_int2(col[k], __float_as_int((float)val[k]));
 }
 
-__device__ __forceinline__ void seed_out(int seed, float* d0, size_t p, double r, double invd) {
-    if (seed == 1) d0[p] = (float)(r * invd);
+// roff[i] = first off-diagonal slot of row i = rp[i] - i, padded past n with its end value.
+__global__ void k_build_roff(int n, int pad, const int* __restrict__ rp, int* __restrict__ roff) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i <= n + pad; i += gridDim.x * blockDim.x)
+        roff[i] = (i <= n) ? rp[i] - i : rp[n] - n;
+}
+
+// Jacobi seed d0 = D^-1 r from the FP32 residual and FP32 reciprocal (FP32 pipe; the FP64 pipe
+// is the residual kernels' bottleneck on this GPU), or the pending fill for an exact inner solve.
+__device__ __forceinline__ void seed_out(int seed, float* d0, size_t p, float r32, float invd32) {
+    if (seed == 1) d0[p] = r32 * invd32;
     else if (seed == 2) d0[p] = __uint_as_float(kPend32);
 }
 
@@ -87,7 +95,7 @@ __device__ __forceinline__ void seed_out(int seed, float* d0, size_t p, double r
 __global__ void __launch_bounds__(kResWarps * 32) k_residual_tile(int n, const int* __restrict__ rp,
                                                                   const int* __restrict__ col,
                                                                   const double* __restrict__ val,
-                                                                  const double* __restrict__ invd,
+                                                                  const float* __restrict__ invd,
                                                                   const double* __restrict__ b,
                                                                   const double* __restrict__ x, float* __restrict__ r32,
                                                                   float* __restrict__ d0, int seed,
@@ -125,9 +133,10 @@ __global__ void __launch_bounds__(kResWarps * 32) k_residual_tile(int n, const i
         }
         if (i < n) {
             const double r = b[i] - sum;
-            r32[i] = (float)r;
-            seed_out(seed, d0, i, r, invd[i]);
-            acc += r * r;
+            const float rf = (float)r;
+            r32[i] = rf;
+            seed_out(seed, d0, i, rf, invd[i]);
+            acc = fma(r, r, acc);
         }
     }
     acc = warp_sum(acc);
@@ -139,7 +148,7 @@ __global__ void __launch_bounds__(kResWarps * 32) k_residual_tile(int n, const i
 // r = b - U x (rhs == 1), LPR lanes per row (long rows).
 template <int LPR>
 __global__ void __launch_bounds__(256) k_residual_v(int n, const int* __restrict__ rp, const int* __restrict__ col,
-                                                    const double* __restrict__ val, const double* __restrict__ invd,
+                                                    const double* __restrict__ val, const float* __restrict__ invd,
                                                     const double* __restrict__ b, const double* __restrict__ x,
                                                     float* __restrict__ r32, float* __restrict__ d0, int seed,
                                                     double* __restrict__ rn2, const Ctl* ctl) {
@@ -161,9 +170,10 @@ __global__ void __launch_bounds__(256) k_residual_v(int n, const int* __restrict
         for (int o = LPR / 2; o > 0; o >>= 1) sum += __shfl_xor_sync(gmask, sum, o);
         if (gl == 0) {
             const double r = b[i] - sum;
-            r32[i] = (float)r;
-            seed_out(seed, d0, i, r, invd[i]);
-            acc += r * r;
+            const float rf = (float)r;
+            r32[i] = rf;
+            seed_out(seed, d0, i, rf, invd[i]);
+            acc = fma(r, r, acc);
         }
     }
     acc = warp_sum(acc);
@@ -175,7 +185,7 @@ __global__ void __launch_bounds__(256) k_residual_v(int n, const int* __restrict
 // rhs > 1: warp per row, lanes over RHS columns, entries sequential.
 __global__ void __launch_bounds__(256) k_residual_m(int n, int rhs, const int* __restrict__ rp,
                                                     const int* __restrict__ col, const double* __restrict__ val,
-                                                    const double* __restrict__ invd, const double* __restrict__ b,
+                                                    const float* __restrict__ invd, const double* __restrict__ b,
                                                     const double* __restrict__ x, float* __restrict__ r32,
                                                     float* __restrict__ d0, int seed, double* __restrict__ rn2,
                                                     const Ctl* ctl) {
@@ -188,14 +198,15 @@ __global__ void __launch_bounds__(256) k_residual_m(int n, int rhs, const int* _
     const long long ws = ((long long)gridDim.x * blockDim.x) >> 5;
     for (long long i = w; i < n; i += ws) {
         const int s = rp[i], e = rp[i + 1];
-        const double di = invd[i];
+        const float di = invd[i];
         for (int c = lane; c < rhs; c += 32) {
             double sum = 0.0;
             for (int k = s; k < e; ++k) sum = fma(val[k], x[(size_t)col[k] * rhs + c], sum);
             const size_t p = (size_t)i * rhs + c;
             const double r = b[p] - sum;
-            r32[p] = (float)r;
-            seed_out(seed, d0, p, r, di);
+            const float rf = (float)r;
+            r32[p] = rf;
+            seed_out(seed, d0, p, rf, di);
             atomicAdd(&s_accm[c], r * r);
         }
     }
@@ -337,6 +348,166 @@ __global__ void __launch_bounds__(kJacWarps * 32) k_jacobi_tile(int n, const int
     if (stats) reduce_stats(dmax, dchg, ctl, s_max);
 }
 
+// ---------------------------------------------------------------------------------------
+// Bulk-copy pipelined sweep.  Each warp walks its tiles (32 rows each) with a kStages-deep
+// pipeline: lane 0 issues cp.async.bulk copies of the next tiles' row offsets and interleaved
+// off-diagonals into the warp's shared-memory stages (completion counted in bytes on an
+// mbarrier), while the lanes compute on the current tile.  No registers hold in-flight data,
+// so every SM keeps tens of KB of matrix traffic in flight.  Copies start on 16-byte
+// boundaries (even int2 index, 32-row aligned offset rows) and move multiples of 16 bytes;
+// `off` and `roff` carry padding so the rounded-up ranges stay inside their allocations.
+// Tiles larger than a stage are read straight from global memory.  Every mbarrier wait is
+// bounded by the spin budget.
+constexpr int kStages = 4;
+constexpr int kTmaWarps = 4;
+constexpr int kStageEntries = 384;  // int2 entries per stage (3 KiB)
+
+struct __align__(128) TmaStage {
+    int2 off[kStageEntries];
+    int roff[36];  // 36 ints = 144 bytes: the tile's 33 row offsets, rounded up to 16 bytes
+};
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, uint64_t* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// bounded wait for phase `parity` of *bar; false on timeout or abort (error recorded)
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, Ctl* ctl, int64_t budget) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const uint64_t t0 = gtimer();
+    for (;;) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if (aborted(ctl)) return false;
+        if ((int64_t)(gtimer() - t0) > budget) { record_error(ctl, SPTRSV_ERR_TIMEOUT); return false; }
+    }
+}
+
+__global__ void __launch_bounds__(kTmaWarps * 32) k_jacobi_tma(int n, const int* __restrict__ roff,
+                                                              const int2* __restrict__ off,
+                                                              const float* __restrict__ invd,
+                                                              const float* __restrict__ r,
+                                                              const float* __restrict__ src, float* __restrict__ dst,
+                                                              double* __restrict__ x, int last, int stats, Ctl* ctl,
+                                                              int64_t budget) {
+    extern __shared__ __align__(128) unsigned char tma_smem[];
+    TmaStage(*stages)[kStages] = reinterpret_cast<TmaStage(*)[kStages]>(tma_smem);
+    __shared__ __align__(8) uint64_t bars[kTmaWarps][kStages];
+    __shared__ unsigned s_max[2];
+    if (is_done(ctl)) return;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (threadIdx.x < 2) s_max[threadIdx.x] = 0u;
+    if (lane == 0)
+        for (int q = 0; q < kStages; ++q) mbar_init(&bars[w][q], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    __syncthreads();
+    const int ntiles = (n + 31) >> 5;
+    const int nw = gridDim.x * kTmaWarps;
+    const int first = blockIdx.x * kTmaWarps + w;
+    TmaStage* st = stages[w];
+    uint64_t* bar = bars[w];
+    // issue tile j (the j-th tile of this warp) into stage j % kStages; returns its mode:
+    // 1 staged, 2 direct (too large for a stage), 0 none (past the end)
+    auto issue = [&](int j) -> int {
+        const int t = first + j * nw;
+        if (t >= ntiles) return 0;
+        const int e0 = roff[32 * t], e1 = roff[32 * t + 32];
+        const int a0 = e0 & ~1, a1 = (e1 + 1) & ~1;
+        TmaStage& S = st[j % kStages];
+        uint64_t* b = &bar[j % kStages];
+        if (a1 - a0 > kStageEntries) return 2;
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        const unsigned bytes = (unsigned)(a1 - a0) * 8u;
+        mbar_expect_tx(b, bytes + 144u);
+        bulk_g2s(S.roff, roff + 32 * t, 144u, b);
+        if (bytes) bulk_g2s(S.off, off + a0, bytes, b);
+        return 1;
+    };
+    // per-stage mode (2 bits each: 0 none, 1 staged, 2 direct) and mbarrier phase bits
+    unsigned modes = 0u, phases = 0u, pending = 0u;
+    auto set_mode = [&](int q, int md) {
+        modes = (modes & ~(3u << (2 * q))) | ((unsigned)md << (2 * q));
+        if (md == 1) pending |= 1u << q;
+    };
+    // prologue: fill the pipeline (lane 0 issues, the mode is broadcast)
+    for (int j = 0; j < kStages - 1; ++j) {
+        int md = 0;
+        if (lane == 0) md = issue(j);
+        set_mode(j % kStages, __shfl_sync(0xffffffffu, md, 0));
+    }
+    float dmax = 0.f, dchg = 0.f;
+    bool ok = true;
+    for (int j = 0;; ++j) {
+        const int t = first + j * nw;
+        if (t >= ntiles) break;
+        {   // keep kStages - 1 tiles in flight ahead of the one being computed
+            int md = 0;
+            if (lane == 0) md = issue(j + kStages - 1);
+            set_mode((j + kStages - 1) % kStages, __shfl_sync(0xffffffffu, md, 0));
+        }
+        const int q = j % kStages;
+        const int r0 = t * 32, i = r0 + lane;
+        float sum = 0.f;
+        const int mq = (modes >> (2 * q)) & 3u;
+        if (mq == 1) {
+            ok = mbar_wait(&bar[q], (phases >> q) & 1u, ctl, budget);
+            phases ^= 1u << q;
+            pending &= ~(1u << q);
+            if (!__all_sync(0xffffffffu, ok)) break;
+            const TmaStage& S = st[q];
+            const int a0 = S.roff[0] & ~1;
+            if (i < n) {
+                const int s = S.roff[lane] - a0, e = S.roff[lane + 1] - a0;
+#pragma unroll 4
+                for (int k = s; k < e; ++k) {
+                    const int2 p = S.off[k];
+                    sum = fmaf(__int_as_float(p.y), __ldg(src + p.x), sum);
+                }
+            }
+        } else if (i < n) {
+            const int s = roff[i], e = roff[i + 1];
+            for (int k = s; k < e; ++k) {
+                const int2 p = __ldg(off + k);
+                sum = fmaf(__int_as_float(p.y), __ldg(src + p.x), sum);
+            }
+        }
+        __syncwarp();  // every lane is done with stage q before it is refilled
+        if (i < n) {
+            const float d = (r[i] - sum) * invd[i];
+            if (stats) {
+                dmax = fmaxf(dmax, fabsf(d));
+                dchg = fmaxf(dchg, fabsf(d - src[i]));
+            }
+            if (last) x[i] += (double)d;
+            else dst[i] = d;
+        }
+    }
+    // drain: copies issued but not consumed (only after an aborted wait) complete before the
+    // block exits, each wait again bounded by the budget
+    for (int q = 0; q < kStages; ++q)
+        if (pending & (1u << q)) (void)mbar_wait(&bar[q], (phases >> q) & 1u, ctl, budget);
+    if (stats) reduce_stats(dmax, dchg, ctl, s_max);
+}
+
 // Same sweep, LPR lanes per row over the CSR FP32 values (long rows).
 template <int LPR>
 __global__ void __launch_bounds__(256) k_jacobi_v(int n, const int* __restrict__ rp, const int* __restrict__ col,
@@ -438,11 +609,16 @@ static int resident_grid(const void* fn, int block, int sm_count) {
     return per_sm * sm_count;
 }
 
-int launch_build_offdiag(int n, const int* rp, const int* col, const double* val, int2* off, int sm_count,
-                         cudaStream_t st, int64_t* launches) {
+static size_t tma_smem_bytes() { return sizeof(TmaStage) * kStages * kTmaWarps; }
+
+int launch_build_offdiag(int n, const int* rp, const int* col, const double* val, int2* off, int* roff,
+                         int roff_pad, int sm_count, cudaStream_t st, int64_t* launches) {
     k_build_offdiag<<<sm_count * 8, 256, 0, st>>>(n, rp, col, val, off);
-    ++*launches;
+    k_build_roff<<<sm_count * 4, 256, 0, st>>>(n, roff_pad, rp, roff);
+    *launches += 2;
     CUDA_TRY(cudaGetLastError());
+    // opt in to the sweep kernel's dynamic shared memory here, outside any stream capture
+    CUDA_TRY(cudaFuncSetAttribute(k_jacobi_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tma_smem_bytes()));
     return 0;
 }
 
@@ -463,17 +639,17 @@ int launch_residual(const RefineArgs& a, bool jacobi_seed, int final_check) {
     if (short_rows(a)) {
         static int grid_rt = 0;
         if (!grid_rt) grid_rt = resident_grid((const void*)k_residual_tile, kResWarps * 32, a.sm_count);
-        k_residual_tile<<<grid_rt, kResWarps * 32, 0, a.st>>>(a.n, a.rp, a.col, a.val, a.invd, a.b, a.x,
+        k_residual_tile<<<grid_rt, kResWarps * 32, 0, a.st>>>(a.n, a.rp, a.col, a.val, a.invd32, a.b, a.x,
                                                                       a.r32, a.d32[0], seed, a.rn2, a.ctl);
     } else if (a.rhs == 1) {
         switch (lpr_for(a.n, a.nnz)) {
-            case 4: k_residual_v<4><<<grid, 256, 0, a.st>>>(a.n, a.rp, a.col, a.val, a.invd, a.b, a.x, a.r32, a.d32[0], seed, a.rn2, a.ctl); break;
-            case 8: k_residual_v<8><<<grid, 256, 0, a.st>>>(a.n, a.rp, a.col, a.val, a.invd, a.b, a.x, a.r32, a.d32[0], seed, a.rn2, a.ctl); break;
-            case 16: k_residual_v<16><<<grid, 256, 0, a.st>>>(a.n, a.rp, a.col, a.val, a.invd, a.b, a.x, a.r32, a.d32[0], seed, a.rn2, a.ctl); break;
-            default: k_residual_v<32><<<grid, 256, 0, a.st>>>(a.n, a.rp, a.col, a.val, a.invd, a.b, a.x, a.r32, a.d32[0], seed, a.rn2, a.ctl); break;
+            case 4: k_residual_v<4><<<grid, 256, 0, a.st>>>(a.n, a.rp, a.col, a.val, a.invd32, a.b, a.x, a.r32, a.d32[0], seed, a.rn2, a.ctl); break;
+            case 8: k_residual_v<8><<<grid, 256, 0, a.st>>>(a.n, a.rp, a.col, a.val, a.invd32, a.b, a.x, a.r32, a.d32[0], seed, a.rn2, a.ctl); break;
+            case 16: k_residual_v<16><<<grid, 256, 0, a.st>>>(a.n, a.rp, a.col, a.val, a.invd32, a.b, a.x, a.r32, a.d32[0], seed, a.rn2, a.ctl); break;
+            default: k_residual_v<32><<<grid, 256, 0, a.st>>>(a.n, a.rp, a.col, a.val, a.invd32, a.b, a.x, a.r32, a.d32[0], seed, a.rn2, a.ctl); break;
         }
     } else {
-        k_residual_m<<<grid, 256, sizeof(double) * a.rhs, a.st>>>(a.n, a.rhs, a.rp, a.col, a.val, a.invd, a.b, a.x,
+        k_residual_m<<<grid, 256, sizeof(double) * a.rhs, a.st>>>(a.n, a.rhs, a.rp, a.col, a.val, a.invd32, a.b, a.x,
                                                                   a.r32, a.d32[0], seed, a.rn2, a.ctl);
     }
     ++*a.launches;
@@ -508,7 +684,18 @@ int launch_jacobi_sweep(const RefineArgs& a, int src, bool last, bool stats) {
     const float* s = a.d32[src];
     float* d = a.d32[src ^ 1];
     const int st_flag = stats ? 1 : 0;
-    if (use_tiles(a)) {
+    if (use_tiles(a) && a.roff && a.sweep_kernel != 1) {
+        static int grid_tma = 0;
+        if (!grid_tma) {
+            int per_sm = 0;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_jacobi_tma, kTmaWarps * 32,
+                                                              tma_smem_bytes()) != cudaSuccess || per_sm < 1)
+                per_sm = 1;
+            grid_tma = per_sm * a.sm_count;
+        }
+        k_jacobi_tma<<<grid_tma, kTmaWarps * 32, tma_smem_bytes(), a.st>>>(a.n, a.roff, a.off, a.invd32, a.r32, s, d,
+                                                                         a.x, last, st_flag, a.ctl, a.budget);
+    } else if (use_tiles(a)) {
         static int grid_jt = 0;
         if (!grid_jt) grid_jt = resident_grid((const void*)k_jacobi_tile, kJacWarps * 32, a.sm_count);
         k_jacobi_tile<<<grid_jt, kJacWarps * 32, 0, a.st>>>(a.n, a.rp, a.off, a.invd32, a.r32, s, d, a.x, last,
