@@ -289,13 +289,14 @@ __device__ __forceinline__ void reduce_stats(float dmax, float dchg, Ctl* ctl, u
 
 // One FP32 Jacobi sweep over warp tiles: dst = D^-1 (r - N src), or x += that when `last`.
 // stats: accumulate max|d| and max|d - src| (non-negative floats order like their bits).
-__global__ void __launch_bounds__(kJacWarps * 32) k_jacobi_tile(int n, const int* __restrict__ rp,
+template <int TMAX, int MINB>
+__global__ void __launch_bounds__(kJacWarps * 32, MINB) k_jacobi_tile(int n, const int* __restrict__ rp,
                                                                 const int2* __restrict__ off,
                                                                 const float* __restrict__ invd,
                                                                 const float* __restrict__ r,
                                                                 const float* __restrict__ src, float* __restrict__ dst,
                                                                 double* __restrict__ x, int last, int stats, Ctl* ctl) {
-    __shared__ __align__(16) int2 stage[kJacWarps][kTileMax];
+    __shared__ __align__(16) int2 stage[kJacWarps][TMAX];
     __shared__ unsigned s_max[2];
     if (is_done(ctl)) return;
     if (threadIdx.x < 2) s_max[threadIdx.x] = 0u;
@@ -315,7 +316,7 @@ __global__ void __launch_bounds__(kJacWarps * 32) k_jacobi_tile(int n, const int
         const int E0 = __shfl_sync(0xffffffffu, s, 0), E1 = __shfl_sync(0xffffffffu, e, 31);
         float sum = 0.f;
         const int a0 = E0 & ~1;  // 16-byte aligned start (pairs of int2)
-        if (E1 - a0 <= kTileMax) {
+        if (E1 - a0 <= TMAX) {
             const int npair = (E1 - a0 + 1) >> 1;
             const int4* v4 = reinterpret_cast<const int4*>(off + a0);
             int4* s4 = reinterpret_cast<int4*>(sb);
@@ -344,6 +345,38 @@ __global__ void __launch_bounds__(kJacWarps * 32) k_jacobi_tile(int n, const int
             if (last) x[i] += (double)d;
             else dst[i] = d;
         }
+    }
+    if (stats) reduce_stats(dmax, dchg, ctl, s_max);
+}
+
+// Lane-per-row sweep reading the interleaved off-diagonals straight from global memory (L1 keeps
+// the lines a warp's 32 neighbouring rows share); bounded to 32 registers for full occupancy.
+__global__ void __launch_bounds__(256, 8) k_jacobi_direct(int n, const int* __restrict__ roff,
+                                                         const int2* __restrict__ off,
+                                                         const float* __restrict__ invd,
+                                                         const float* __restrict__ r, const float* __restrict__ src,
+                                                         float* __restrict__ dst, double* __restrict__ x, int last,
+                                                         int stats, Ctl* ctl) {
+    __shared__ unsigned s_max[2];
+    if (is_done(ctl)) return;
+    if (threadIdx.x < 2) s_max[threadIdx.x] = 0u;
+    __syncthreads();
+    float dmax = 0.f, dchg = 0.f;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int s = __ldg(roff + i), e = __ldg(roff + i + 1);
+        float sum = 0.f;
+#pragma unroll 4
+        for (int k = s; k < e; ++k) {
+            const int2 p = __ldg(off + k);
+            sum = fmaf(__int_as_float(p.y), __ldg(src + p.x), sum);
+        }
+        const float d = (r[i] - sum) * invd[i];
+        if (stats) {
+            dmax = fmaxf(dmax, fabsf(d));
+            dchg = fmaxf(dchg, fabsf(d - src[i]));
+        }
+        if (last) x[i] += (double)d;
+        else dst[i] = d;
     }
     if (stats) reduce_stats(dmax, dchg, ctl, s_max);
 }
@@ -427,10 +460,18 @@ __global__ void __launch_bounds__(kTmaWarps * 32) k_jacobi_tma(int n, const int*
     uint64_t* bar = bars[w];
     // issue tile j (the j-th tile of this warp) into stage j % kStages; returns its mode:
     // 1 staged, 2 direct (too large for a stage), 0 none (past the end)
+    // lane 0 keeps the row-offset bounds of the next tile to issue in registers, loaded one
+    // iteration before they are needed, so the issue never waits on a global load
+    int nx_e0 = 0, nx_e1 = 0;
+    auto fetch = [&](int j) {
+        const int t = first + j * nw;
+        if (t < ntiles) { nx_e0 = __ldg(roff + 32 * t); nx_e1 = __ldg(roff + 32 * t + 32); }
+    };
     auto issue = [&](int j) -> int {
         const int t = first + j * nw;
         if (t >= ntiles) return 0;
-        const int e0 = roff[32 * t], e1 = roff[32 * t + 32];
+        const int e0 = nx_e0, e1 = nx_e1;
+        fetch(j + 1);
         const int a0 = e0 & ~1, a1 = (e1 + 1) & ~1;
         TmaStage& S = st[j % kStages];
         uint64_t* b = &bar[j % kStages];
@@ -449,6 +490,7 @@ __global__ void __launch_bounds__(kTmaWarps * 32) k_jacobi_tma(int n, const int*
         if (md == 1) pending |= 1u << q;
     };
     // prologue: fill the pipeline (lane 0 issues, the mode is broadcast)
+    if (lane == 0) fetch(0);
     for (int j = 0; j < kStages - 1; ++j) {
         int md = 0;
         if (lane == 0) md = issue(j);
@@ -684,7 +726,16 @@ int launch_jacobi_sweep(const RefineArgs& a, int src, bool last, bool stats) {
     const float* s = a.d32[src];
     float* d = a.d32[src ^ 1];
     const int st_flag = stats ? 1 : 0;
-    if (use_tiles(a) && a.roff && a.sweep_kernel != 1) {
+    if (use_tiles(a) && a.roff && a.sweep_kernel == 2) {
+        static int grid_d = 0;
+        if (!grid_d) grid_d = resident_grid((const void*)k_jacobi_direct, 256, a.sm_count);
+        k_jacobi_direct<<<grid_d, 256, 0, a.st>>>(a.n, a.roff, a.off, a.invd32, a.r32, s, d, a.x, last, st_flag, a.ctl);
+    } else if (use_tiles(a) && a.sweep_kernel == 3) {
+        static int grid_t8 = 0;
+        if (!grid_t8) grid_t8 = resident_grid((const void*)k_jacobi_tile<384, 8>, kJacWarps * 32, a.sm_count);
+        k_jacobi_tile<384, 8><<<grid_t8, kJacWarps * 32, 0, a.st>>>(a.n, a.rp, a.off, a.invd32, a.r32, s, d, a.x,
+                                                                   last, st_flag, a.ctl);
+    } else if (use_tiles(a) && a.roff && a.sweep_kernel == 0) {
         static int grid_tma = 0;
         if (!grid_tma) {
             int per_sm = 0;
@@ -697,8 +748,8 @@ int launch_jacobi_sweep(const RefineArgs& a, int src, bool last, bool stats) {
                                                                          a.x, last, st_flag, a.ctl, a.budget);
     } else if (use_tiles(a)) {
         static int grid_jt = 0;
-        if (!grid_jt) grid_jt = resident_grid((const void*)k_jacobi_tile, kJacWarps * 32, a.sm_count);
-        k_jacobi_tile<<<grid_jt, kJacWarps * 32, 0, a.st>>>(a.n, a.rp, a.off, a.invd32, a.r32, s, d, a.x, last,
+        if (!grid_jt) grid_jt = resident_grid((const void*)k_jacobi_tile<kTileMax, 1>, kJacWarps * 32, a.sm_count);
+        k_jacobi_tile<kTileMax, 1><<<grid_jt, kJacWarps * 32, 0, a.st>>>(a.n, a.rp, a.off, a.invd32, a.r32, s, d, a.x, last,
                                                                   st_flag, a.ctl);
     } else if (a.rhs == 1) {
         switch (lpr_for(a.n, a.nnz)) {
