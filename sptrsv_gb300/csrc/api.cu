@@ -730,12 +730,13 @@ int sptrsv_create(sptrsv_handle* out, int device) {
     if (rc) { delete h; return rc; }
     const char* g = getenv("SPTRSV_NO_GRAPH");
     h->use_graphs = !(g && g[0] == '1');
-    // tuning override of the Jacobi sweep kernel: tma (default), tile, direct, tile8
+    // tuning override of the Jacobi sweep kernel: direct (default), tile, tile8, direct2, tma
     const char* sk = getenv("SPTRSV_SWEEP_KERNEL");
     h->sweep_kernel = 0;
     if (sk && strcmp(sk, "tile") == 0) h->sweep_kernel = 1;
-    if (sk && strcmp(sk, "direct") == 0) h->sweep_kernel = 2;
     if (sk && strcmp(sk, "tile8") == 0) h->sweep_kernel = 3;
+    if (sk && strcmp(sk, "direct2") == 0) h->sweep_kernel = 4;
+    if (sk && strcmp(sk, "tma") == 0) h->sweep_kernel = 5;
     *out = reinterpret_cast<sptrsv_handle>(h);
     return 0;
 }

@@ -82,7 +82,7 @@ struct RefineArgs {
     const float* invd32;
     const int2* off;   // interleaved (column, FP32 value) off-diagonals, or nullptr
     const int* roff;   // first off-diagonal slot of every row (rp[i] - i), padded, or nullptr
-    int sweep_kernel;  // 0 bulk-copy pipeline, 1 warp tiles, 2 lane per row direct, 3 tiles at 8 blocks/SM
+    int sweep_kernel;  // 0 lane per row (default), 1 warp tiles, 3 tiles at 8 blocks/SM, 4 two rows per lane, 5 bulk-copy pipeline
     const double* b;   // row-major n x rhs
     double* x;         // row-major n x rhs
     float* r32;        // n x rhs

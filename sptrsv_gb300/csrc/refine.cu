@@ -381,6 +381,59 @@ __global__ void __launch_bounds__(256, 8) k_jacobi_direct(int n, const int* __re
     if (stats) reduce_stats(dmax, dchg, ctl, s_max);
 }
 
+// Same, two rows per thread per iteration (i and i + half the grid): two independent load chains
+// in flight per thread.
+__global__ void __launch_bounds__(256, 8) k_jacobi_direct2(int n, const int* __restrict__ roff,
+                                                          const int2* __restrict__ off,
+                                                          const float* __restrict__ invd,
+                                                          const float* __restrict__ r, const float* __restrict__ src,
+                                                          float* __restrict__ dst, double* __restrict__ x, int last,
+                                                          int stats, Ctl* ctl) {
+    __shared__ unsigned s_max[2];
+    if (is_done(ctl)) return;
+    if (threadIdx.x < 2) s_max[threadIdx.x] = 0u;
+    __syncthreads();
+    float dmax = 0.f, dchg = 0.f;
+    const int stride = gridDim.x * blockDim.x;
+    for (int i0 = blockIdx.x * blockDim.x + threadIdx.x; i0 < n; i0 += 2 * stride) {
+        const int i1 = i0 + stride;
+        const bool has1 = i1 < n;
+        const int s0 = __ldg(roff + i0), e0 = __ldg(roff + i0 + 1);
+        const int s1 = has1 ? __ldg(roff + i1) : 0, e1 = has1 ? __ldg(roff + i1 + 1) : 0;
+        float sum0 = 0.f, sum1 = 0.f;
+        const int l0 = e0 - s0, l1 = e1 - s1;
+        const int lmax = l0 > l1 ? l0 : l1;
+#pragma unroll 2
+        for (int q = 0; q < lmax; ++q) {
+            if (q < l0) {
+                const int2 p = __ldg(off + s0 + q);
+                sum0 = fmaf(__int_as_float(p.y), __ldg(src + p.x), sum0);
+            }
+            if (q < l1) {
+                const int2 p = __ldg(off + s1 + q);
+                sum1 = fmaf(__int_as_float(p.y), __ldg(src + p.x), sum1);
+            }
+        }
+        const float d0 = (r[i0] - sum0) * invd[i0];
+        if (stats) {
+            dmax = fmaxf(dmax, fabsf(d0));
+            dchg = fmaxf(dchg, fabsf(d0 - src[i0]));
+        }
+        if (last) x[i0] += (double)d0;
+        else dst[i0] = d0;
+        if (has1) {
+            const float d1 = (r[i1] - sum1) * invd[i1];
+            if (stats) {
+                dmax = fmaxf(dmax, fabsf(d1));
+                dchg = fmaxf(dchg, fabsf(d1 - src[i1]));
+            }
+            if (last) x[i1] += (double)d1;
+            else dst[i1] = d1;
+        }
+    }
+    if (stats) reduce_stats(dmax, dchg, ctl, s_max);
+}
+
 // ---------------------------------------------------------------------------------------
 // Bulk-copy pipelined sweep.  Each warp walks its tiles (32 rows each) with a kStages-deep
 // pipeline: lane 0 issues cp.async.bulk copies of the next tiles' row offsets and interleaved
@@ -726,7 +779,16 @@ int launch_jacobi_sweep(const RefineArgs& a, int src, bool last, bool stats) {
     const float* s = a.d32[src];
     float* d = a.d32[src ^ 1];
     const int st_flag = stats ? 1 : 0;
-    if (use_tiles(a) && a.roff && a.sweep_kernel == 2) {
+    if (use_tiles(a) && a.roff && a.sweep_kernel == 4) {
+        static int grid_d2 = 0;
+        if (!grid_d2) grid_d2 = resident_grid((const void*)k_jacobi_direct2, 256, a.sm_count);
+        k_jacobi_direct2<<<grid_d2, 256, 0, a.st>>>(a.n, a.roff, a.off, a.invd32, a.r32, s, d, a.x, last, st_flag,
+                                                   a.ctl);
+    } else if (use_tiles(a) && a.roff && a.sweep_kernel == 0) {
+        static int grid_d = 0;
+        if (!grid_d) grid_d = resident_grid((const void*)k_jacobi_direct, 256, a.sm_count);
+        k_jacobi_direct<<<grid_d, 256, 0, a.st>>>(a.n, a.roff, a.off, a.invd32, a.r32, s, d, a.x, last, st_flag, a.ctl);
+    } else if (use_tiles(a) && a.roff && a.sweep_kernel == 2) {
         static int grid_d = 0;
         if (!grid_d) grid_d = resident_grid((const void*)k_jacobi_direct, 256, a.sm_count);
         k_jacobi_direct<<<grid_d, 256, 0, a.st>>>(a.n, a.roff, a.off, a.invd32, a.r32, s, d, a.x, last, st_flag, a.ctl);
@@ -735,7 +797,7 @@ int launch_jacobi_sweep(const RefineArgs& a, int src, bool last, bool stats) {
         if (!grid_t8) grid_t8 = resident_grid((const void*)k_jacobi_tile<384, 8>, kJacWarps * 32, a.sm_count);
         k_jacobi_tile<384, 8><<<grid_t8, kJacWarps * 32, 0, a.st>>>(a.n, a.rp, a.off, a.invd32, a.r32, s, d, a.x,
                                                                    last, st_flag, a.ctl);
-    } else if (use_tiles(a) && a.roff && a.sweep_kernel == 0) {
+    } else if (use_tiles(a) && a.roff && a.sweep_kernel == 5) {
         static int grid_tma = 0;
         if (!grid_tma) {
             int per_sm = 0;
