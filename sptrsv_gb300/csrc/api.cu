@@ -371,6 +371,26 @@ int Handle::resident_warps(const sptrsv_opts& o) const {
 int Handle::ensure_offdiag() {
     if (have_offdiag) return 0;
     int rc;
+    if (sweep_kernel == 0) {
+        // SELL slices: the default sweep layout
+        const int nslices = sell_slices(n);
+        if ((rc = sell_perm.ensure(sizeof(int) * (size_t)nslices * 32))) return rc;
+        if ((rc = sell_len.ensure(sizeof(int) * (size_t)nslices))) return rc;
+        if ((rc = sell_ptr.ensure(sizeof(int) * ((size_t)nslices + 1)))) return rc;
+        if ((rc = scratch.ensure(sizeof(int) * (size_t)(scan_partials_needed(nslices) + 64)))) return rc;
+        int total = 0;
+        if ((rc = sell_prepare(n, rp, sell_perm.as<int>(), sell_len.as<int>(), sell_ptr.as<int>(), (int*)scratch.p,
+                               sm_count, st, &launches, &total)))
+            return rc;
+        if ((rc = sell.ensure(sizeof(int2) * ((size_t)total + 32)))) return rc;
+        if ((rc = sell_fill(n, rp, col, val, sell_perm.as<int>(), sell_len.as<int>(), sell_ptr.as<int>(),
+                            sell.as<int2>(), sm_count, st, &launches)))
+            return rc;
+        CUDA_TRY(cudaStreamSynchronize(st));
+        sell_nslices = nslices;
+        have_offdiag = true;
+        return 0;
+    }
     const int kRoffPad = 64;
     if ((rc = offdiag.ensure(sizeof(int2) * ((size_t)(nnz - n) + 4)))) return rc;
     if ((rc = roff.ensure(sizeof(int) * ((size_t)n + 1 + kRoffPad)))) return rc;
@@ -395,9 +415,15 @@ int Handle::refine_args(const sptrsv_opts& o, const double* b, double* x, int rh
     r.val32 = val32.as<float>();
     r.invd = invd.as<double>();
     r.invd32 = invd32.as<float>();
-    r.off = (have_offdiag && rhs == 1) ? offdiag.as<int2>() : nullptr;
-    r.roff = (have_offdiag && rhs == 1) ? roff.as<int>() : nullptr;
+    const bool sl = have_offdiag && rhs == 1 && sweep_kernel == 0;
+    r.off = (have_offdiag && rhs == 1 && !sl) ? offdiag.as<int2>() : nullptr;
+    r.roff = (have_offdiag && rhs == 1 && !sl) ? roff.as<int>() : nullptr;
     r.sweep_kernel = sweep_kernel;
+    r.nslices = sl ? sell_nslices : 0;
+    r.sell_perm = sl ? sell_perm.as<int>() : nullptr;
+    r.sell_len = sl ? sell_len.as<int>() : nullptr;
+    r.sell_ptr = sl ? sell_ptr.as<int>() : nullptr;
+    r.sell = sl ? sell.as<int2>() : nullptr;
     r.b = b;
     r.x = x;
     r.r32 = r32.as<float>();
@@ -650,7 +676,7 @@ Handle::~Handle() {
     if (prof0) cudaEventDestroy(prof0);
     DevBuf* bufs[] = {&own_rp, &own_col, &own_val, &val32, &invd, &invd32, &in_degree, &levels, &level_ptr,
                       &level_rows, &stats, &csc_ptr, &csc_row, &csc_val, &scratch, &xw, &bw, &r32, &d32a, &d32b,
-                      &norms, &indeg_work, &left, &db, &dx, &flush, &offdiag, &roff};
+                      &norms, &indeg_work, &left, &db, &dx, &flush, &offdiag, &roff, &sell, &sell_perm, &sell_len, &sell_ptr};
     for (DevBuf* b : bufs) b->release();
     if (ctl) cudaFree(ctl);
     if (ev0) cudaEventDestroy(ev0);
@@ -730,10 +756,11 @@ int sptrsv_create(sptrsv_handle* out, int device) {
     if (rc) { delete h; return rc; }
     const char* g = getenv("SPTRSV_NO_GRAPH");
     h->use_graphs = !(g && g[0] == '1');
-    // tuning override of the Jacobi sweep kernel: direct (default), tile, tile8, direct2, tma
+    // tuning override of the Jacobi sweep kernel: sell (default), tile, direct, tile8, direct2, tma
     const char* sk = getenv("SPTRSV_SWEEP_KERNEL");
     h->sweep_kernel = 0;
     if (sk && strcmp(sk, "tile") == 0) h->sweep_kernel = 1;
+    if (sk && strcmp(sk, "direct") == 0) h->sweep_kernel = 2;
     if (sk && strcmp(sk, "tile8") == 0) h->sweep_kernel = 3;
     if (sk && strcmp(sk, "direct2") == 0) h->sweep_kernel = 4;
     if (sk && strcmp(sk, "tma") == 0) h->sweep_kernel = 5;

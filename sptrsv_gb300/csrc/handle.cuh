@@ -68,6 +68,8 @@ struct Handle {
     bool have_csc = false;
     DevBuf offdiag;        // interleaved FP32 off-diagonals for the Jacobi sweeps
     DevBuf roff;           // per-row first off-diagonal slot, padded by kRoffPad
+    DevBuf sell, sell_perm, sell_len, sell_ptr;  // SELL-32-256 copy of the off-diagonals
+    int sell_nslices = 0;
     bool have_offdiag = false;
 
     // work

@@ -82,7 +82,13 @@ struct RefineArgs {
     const float* invd32;
     const int2* off;   // interleaved (column, FP32 value) off-diagonals, or nullptr
     const int* roff;   // first off-diagonal slot of every row (rp[i] - i), padded, or nullptr
-    int sweep_kernel;  // 0 lane per row (default), 1 warp tiles, 3 tiles at 8 blocks/SM, 4 two rows per lane, 5 bulk-copy pipeline
+    int sweep_kernel;  // 0 SELL slices (default), 1 warp tiles, 2 lane per row, 3 tiles at 8 blocks/SM,
+                       // 4 two rows per lane, 5 bulk-copy pipeline
+    int nslices;       // SELL: slices of 32 rows
+    const int* sell_perm;  // SELL: row of every slice lane (-1 = padding)
+    const int* sell_len;   // SELL: entries per lane of every slice
+    const int* sell_ptr;   // SELL: first entry of every slice
+    const int2* sell;      // SELL: column-major slice entries
     const double* b;   // row-major n x rhs
     double* x;         // row-major n x rhs
     float* r32;        // n x rhs
@@ -98,6 +104,11 @@ struct RefineArgs {
 };
 int launch_build_offdiag(int n, const int* rp, const int* col, const double* val, int2* off, int* roff,
                          int roff_pad, int sm_count, cudaStream_t st, int64_t* launches);
+int sell_prepare(int n, const int* rp, int* perm, int* slen, int* sptr, int* part, int sm_count, cudaStream_t st,
+                 int64_t* launches, int* total);
+int sell_fill(int n, const int* rp, const int* col, const double* val, const int* perm, const int* slen,
+              const int* sptr, int2* sell, int sm_count, cudaStream_t st, int64_t* launches);
+int sell_slices(int n);
 int launch_refine_init(const RefineArgs& a);
 int launch_residual(const RefineArgs& a, bool jacobi_seed, int final_check);
 int launch_check(const RefineArgs& a, int step, bool reset_ticket);

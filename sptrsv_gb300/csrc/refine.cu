@@ -435,6 +435,125 @@ __global__ void __launch_bounds__(256, 8) k_jacobi_direct2(int n, const int* __r
 }
 
 // ---------------------------------------------------------------------------------------
+// SELL-32-256 copy of the off-diagonals for the sweeps: rows are sorted by off-diagonal count
+// (descending, stable) inside windows of 256 rows and grouped into slices of 32; a slice stores
+// entry k of its 32 rows contiguously (column-major inside the slice) and is padded to its
+// longest row with (column = the row itself, value 0).  A warp sweeps a slice with every load
+// coalesced (256 bytes per instruction) and no divergence.
+constexpr int kSellWin = 256;
+
+// One block of 256 threads per window: bitonic sort of (count, row) by count descending, row
+// ascending (stable order), then slice lengths.
+__global__ void __launch_bounds__(kSellWin) k_sell_sort(int n, const int* __restrict__ rp, int* __restrict__ perm,
+                                                        int* __restrict__ slen) {
+    __shared__ int key[kSellWin], idx[kSellWin];
+    const int w = blockIdx.x, t = threadIdx.x;
+    const int row = w * kSellWin + t;
+    key[t] = row < n ? rp[row + 1] - rp[row] - 1 : -1;  // padding rows sort last
+    idx[t] = row;
+    __syncthreads();
+    for (int k = 2; k <= kSellWin; k <<= 1) {
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            const int p = t ^ j;
+            if (p > t) {
+                const bool up = (t & k) == 0;  // this pair sorts "descending by key, ascending by row"
+                const int ka = key[t], kb = key[p], ia = idx[t], ib = idx[p];
+                const bool a_first = ka > kb || (ka == kb && ia < ib);
+                if (a_first != up) {
+                    key[t] = kb; key[p] = ka;
+                    idx[t] = ib; idx[p] = ia;
+                }
+            }
+            __syncthreads();
+        }
+    }
+    perm[row] = idx[t] < n ? idx[t] : -1;
+    if ((t & 31) == 0) slen[row >> 5] = key[t] > 0 ? key[t] : 0;  // first row of a slice is its longest
+}
+
+__global__ void k_sell_sizes(int nslices, const int* __restrict__ slen, int* __restrict__ sz) {
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nslices; s += gridDim.x * blockDim.x) sz[s] = 32 * slen[s];
+}
+
+__global__ void k_sell_fill(int nslices, const int* __restrict__ rp, const int* __restrict__ col,
+                            const double* __restrict__ val, const int* __restrict__ perm, const int* __restrict__ slen,
+                            const int* __restrict__ sptr, int2* __restrict__ sell) {
+    const int lane = threadIdx.x & 31;
+    for (int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < nslices; s += (gridDim.x * blockDim.x) >> 5) {
+        const int row = perm[32 * s + lane];
+        const int len = slen[s];
+        const int base = sptr[s];
+        const int b = row >= 0 ? rp[row] + 1 : 0, e = row >= 0 ? rp[row + 1] : 0;
+        for (int k = 0; k < len; ++k) {
+            int2 v = make_int2(row >= 0 ? row : 0, 0);  // padding: 0 * x[row]
+            if (b + k < e) v = make_int2(col[b + k], __float_as_int((float)val[b + k]));
+            sell[base + 32 * k + lane] = v;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256, 8) k_jacobi_sell(int nslices, const int* __restrict__ perm,
+                                                       const int* __restrict__ slen, const int* __restrict__ sptr,
+                                                       const int2* __restrict__ sell,
+                                                       const float* __restrict__ invd, const float* __restrict__ r,
+                                                       const float* __restrict__ src, float* __restrict__ dst,
+                                                       double* __restrict__ x, int last, int stats, Ctl* ctl) {
+    __shared__ unsigned s_max[2];
+    if (is_done(ctl)) return;
+    if (threadIdx.x < 2) s_max[threadIdx.x] = 0u;
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    float dmax = 0.f, dchg = 0.f;
+    for (int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < nslices; s += (gridDim.x * blockDim.x) >> 5) {
+        const int row = __ldg(perm + 32 * s + lane);
+        const int len = __ldg(slen + s);
+        const int2* p = sell + __ldg(sptr + s) + lane;
+        float sum = 0.f;
+#pragma unroll 4
+        for (int k = 0; k < len; ++k) {
+            const int2 v = __ldg(p + 32 * k);
+            sum = fmaf(__int_as_float(v.y), __ldg(src + v.x), sum);
+        }
+        if (row >= 0) {
+            const float d = (r[row] - sum) * invd[row];
+            if (stats) {
+                dmax = fmaxf(dmax, fabsf(d));
+                dchg = fmaxf(dchg, fabsf(d - src[row]));
+            }
+            if (last) x[row] += (double)d;
+            else dst[row] = d;
+        }
+    }
+    if (stats) reduce_stats(dmax, dchg, ctl, s_max);
+}
+
+// SELL build, first half: window sorts, slice lengths and slice offsets; returns the entry count.
+int sell_prepare(int n, const int* rp, int* perm, int* slen, int* sptr, int* part, int sm_count, cudaStream_t st,
+                 int64_t* launches, int* total) {
+    const int nwin = (n + kSellWin - 1) / kSellWin;
+    const int nslices = nwin * (kSellWin / 32);
+    k_sell_sort<<<nwin, kSellWin, 0, st>>>(n, rp, perm, slen);
+    k_sell_sizes<<<sm_count * 4, 256, 0, st>>>(nslices, slen, sptr);
+    *launches += 2;
+    int rc = scan_exclusive(sptr, sptr, nslices, part, st, launches);
+    if (rc) return rc;
+    CUDA_TRY(cudaMemcpyAsync(total, sptr + nslices, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    return 0;
+}
+
+// SELL build, second half: the slices' column-major entries (`sell` holds `total` entries).
+int sell_fill(int n, const int* rp, const int* col, const double* val, const int* perm, const int* slen,
+              const int* sptr, int2* sell, int sm_count, cudaStream_t st, int64_t* launches) {
+    const int nslices = ((n + kSellWin - 1) / kSellWin) * (kSellWin / 32);
+    k_sell_fill<<<sm_count * 8, 256, 0, st>>>(nslices, rp, col, val, perm, slen, sptr, sell);
+    ++*launches;
+    CUDA_TRY(cudaGetLastError());
+    return 0;
+}
+int sell_slices(int n) { return ((n + kSellWin - 1) / kSellWin) * (kSellWin / 32); }
+
+// ---------------------------------------------------------------------------------------
 // Bulk-copy pipelined sweep.  Each warp walks its tiles (32 rows each) with a kStages-deep
 // pipeline: lane 0 issues cp.async.bulk copies of the next tiles' row offsets and interleaved
 // off-diagonals into the warp's shared-memory stages (completion counted in bytes on an
@@ -779,15 +898,16 @@ int launch_jacobi_sweep(const RefineArgs& a, int src, bool last, bool stats) {
     const float* s = a.d32[src];
     float* d = a.d32[src ^ 1];
     const int st_flag = stats ? 1 : 0;
-    if (use_tiles(a) && a.roff && a.sweep_kernel == 4) {
+    if (a.rhs == 1 && a.sell && a.sweep_kernel == 0) {
+        static int grid_s = 0;
+        if (!grid_s) grid_s = resident_grid((const void*)k_jacobi_sell, 256, a.sm_count);
+        k_jacobi_sell<<<grid_s, 256, 0, a.st>>>(a.nslices, a.sell_perm, a.sell_len, a.sell_ptr, a.sell, a.invd32, a.r32,
+                                                s, d, a.x, last, st_flag, a.ctl);
+    } else if (use_tiles(a) && a.roff && a.sweep_kernel == 4) {
         static int grid_d2 = 0;
         if (!grid_d2) grid_d2 = resident_grid((const void*)k_jacobi_direct2, 256, a.sm_count);
         k_jacobi_direct2<<<grid_d2, 256, 0, a.st>>>(a.n, a.roff, a.off, a.invd32, a.r32, s, d, a.x, last, st_flag,
                                                    a.ctl);
-    } else if (use_tiles(a) && a.roff && a.sweep_kernel == 0) {
-        static int grid_d = 0;
-        if (!grid_d) grid_d = resident_grid((const void*)k_jacobi_direct, 256, a.sm_count);
-        k_jacobi_direct<<<grid_d, 256, 0, a.st>>>(a.n, a.roff, a.off, a.invd32, a.r32, s, d, a.x, last, st_flag, a.ctl);
     } else if (use_tiles(a) && a.roff && a.sweep_kernel == 2) {
         static int grid_d = 0;
         if (!grid_d) grid_d = resident_grid((const void*)k_jacobi_direct, 256, a.sm_count);
