@@ -371,8 +371,8 @@ int Handle::resident_warps(const sptrsv_opts& o) const {
 int Handle::ensure_offdiag() {
     if (have_offdiag) return 0;
     int rc;
-    if (sweep_kernel == 0) {
-        // SELL slices: the default sweep layout
+    if (sweep_kernel == 6) {
+        // SELL slices
         const int nslices = sell_slices(n);
         if ((rc = sell_perm.ensure(sizeof(int) * (size_t)nslices * 32))) return rc;
         if ((rc = sell_len.ensure(sizeof(int) * (size_t)nslices))) return rc;
@@ -415,7 +415,7 @@ int Handle::refine_args(const sptrsv_opts& o, const double* b, double* x, int rh
     r.val32 = val32.as<float>();
     r.invd = invd.as<double>();
     r.invd32 = invd32.as<float>();
-    const bool sl = have_offdiag && rhs == 1 && sweep_kernel == 0;
+    const bool sl = have_offdiag && rhs == 1 && sweep_kernel == 6;
     r.off = (have_offdiag && rhs == 1 && !sl) ? offdiag.as<int2>() : nullptr;
     r.roff = (have_offdiag && rhs == 1 && !sl) ? roff.as<int>() : nullptr;
     r.sweep_kernel = sweep_kernel;
@@ -756,9 +756,10 @@ int sptrsv_create(sptrsv_handle* out, int device) {
     if (rc) { delete h; return rc; }
     const char* g = getenv("SPTRSV_NO_GRAPH");
     h->use_graphs = !(g && g[0] == '1');
-    // tuning override of the Jacobi sweep kernel: sell (default), tile, direct, tile8, direct2, tma
+    // tuning override of the Jacobi sweep kernel: direct (default), tile, tile8, direct2, tma, sell
     const char* sk = getenv("SPTRSV_SWEEP_KERNEL");
     h->sweep_kernel = 0;
+    if (sk && strcmp(sk, "sell") == 0) h->sweep_kernel = 6;
     if (sk && strcmp(sk, "tile") == 0) h->sweep_kernel = 1;
     if (sk && strcmp(sk, "direct") == 0) h->sweep_kernel = 2;
     if (sk && strcmp(sk, "tile8") == 0) h->sweep_kernel = 3;

@@ -82,8 +82,8 @@ struct RefineArgs {
     const float* invd32;
     const int2* off;   // interleaved (column, FP32 value) off-diagonals, or nullptr
     const int* roff;   // first off-diagonal slot of every row (rp[i] - i), padded, or nullptr
-    int sweep_kernel;  // 0 SELL slices (default), 1 warp tiles, 2 lane per row, 3 tiles at 8 blocks/SM,
-                       // 4 two rows per lane, 5 bulk-copy pipeline
+    int sweep_kernel;  // 0/2 lane per row (default), 1 warp tiles, 3 tiles at 8 blocks/SM,
+                       // 4 two rows per lane, 5 bulk-copy pipeline, 6 SELL slices
     int nslices;       // SELL: slices of 32 rows
     const int* sell_perm;  // SELL: row of every slice lane (-1 = padding)
     const int* sell_len;   // SELL: entries per lane of every slice

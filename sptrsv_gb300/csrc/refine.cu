@@ -898,7 +898,7 @@ int launch_jacobi_sweep(const RefineArgs& a, int src, bool last, bool stats) {
     const float* s = a.d32[src];
     float* d = a.d32[src ^ 1];
     const int st_flag = stats ? 1 : 0;
-    if (a.rhs == 1 && a.sell && a.sweep_kernel == 0) {
+    if (a.rhs == 1 && a.sell && a.sweep_kernel == 6) {
         static int grid_s = 0;
         if (!grid_s) grid_s = resident_grid((const void*)k_jacobi_sell, 256, a.sm_count);
         k_jacobi_sell<<<grid_s, 256, 0, a.st>>>(a.nslices, a.sell_perm, a.sell_len, a.sell_ptr, a.sell, a.invd32, a.r32,
@@ -908,7 +908,7 @@ int launch_jacobi_sweep(const RefineArgs& a, int src, bool last, bool stats) {
         if (!grid_d2) grid_d2 = resident_grid((const void*)k_jacobi_direct2, 256, a.sm_count);
         k_jacobi_direct2<<<grid_d2, 256, 0, a.st>>>(a.n, a.roff, a.off, a.invd32, a.r32, s, d, a.x, last, st_flag,
                                                    a.ctl);
-    } else if (use_tiles(a) && a.roff && a.sweep_kernel == 2) {
+    } else if (use_tiles(a) && a.roff && (a.sweep_kernel == 0 || a.sweep_kernel == 2)) {
         static int grid_d = 0;
         if (!grid_d) grid_d = resident_grid((const void*)k_jacobi_direct, 256, a.sm_count);
         k_jacobi_direct<<<grid_d, 256, 0, a.st>>>(a.n, a.roff, a.off, a.invd32, a.r32, s, d, a.x, last, st_flag, a.ctl);
