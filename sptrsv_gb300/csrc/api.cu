@@ -760,6 +760,8 @@ int sptrsv_create(sptrsv_handle* out, int device) {
     const char* sk = getenv("SPTRSV_SWEEP_KERNEL");
     h->sweep_kernel = 0;
     if (sk && strcmp(sk, "sell") == 0) h->sweep_kernel = 6;
+    if (sk && strcmp(sk, "batch4") == 0) h->sweep_kernel = 7;
+    if (sk && strcmp(sk, "batch8") == 0) h->sweep_kernel = 8;
     if (sk && strcmp(sk, "tile") == 0) h->sweep_kernel = 1;
     if (sk && strcmp(sk, "direct") == 0) h->sweep_kernel = 2;
     if (sk && strcmp(sk, "tile8") == 0) h->sweep_kernel = 3;

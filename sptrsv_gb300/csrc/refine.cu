@@ -381,6 +381,55 @@ __global__ void __launch_bounds__(256, 8) k_jacobi_direct(int n, const int* __re
     if (stats) reduce_stats(dmax, dchg, ctl, s_max);
 }
 
+// Lane-per-row sweep with explicit load batching: the next row's offsets are fetched while the
+// current row is summed, and each batch of B entries issues all B entry loads, then all B
+// gathers, then the B FMAs (in entry order, so the sum is the same as the sequential loop's).
+template <int B, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_jacobi_batched(int n, const int* __restrict__ roff,
+                                                             const int2* __restrict__ off,
+                                                             const float* __restrict__ invd,
+                                                             const float* __restrict__ r,
+                                                             const float* __restrict__ src, float* __restrict__ dst,
+                                                             double* __restrict__ x, int last, int stats, Ctl* ctl) {
+    __shared__ unsigned s_max[2];
+    if (is_done(ctl)) return;
+    if (threadIdx.x < 2) s_max[threadIdx.x] = 0u;
+    __syncthreads();
+    float dmax = 0.f, dchg = 0.f;
+    const int stride = gridDim.x * blockDim.x;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int s = 0, e = 0;
+    if (i < n) { s = __ldg(roff + i); e = __ldg(roff + i + 1); }
+    while (i < n) {
+        const int inext = i + stride;
+        int sn = 0, en = 0;
+        if (inext < n) { sn = __ldg(roff + inext); en = __ldg(roff + inext + 1); }
+        const float ri = r[i], di = invd[i];
+        float sum = 0.f;
+        for (int k0 = s; k0 < e; k0 += B) {
+            int2 p[B];
+            float g[B];
+#pragma unroll
+            for (int j = 0; j < B; ++j) p[j] = (k0 + j < e) ? __ldg(off + k0 + j) : make_int2(i, 0);
+#pragma unroll
+            for (int j = 0; j < B; ++j) g[j] = (k0 + j < e) ? __ldg(src + p[j].x) : 0.f;
+#pragma unroll
+            for (int j = 0; j < B; ++j) sum = fmaf(__int_as_float(p[j].y), g[j], sum);
+        }
+        const float d = (ri - sum) * di;
+        if (stats) {
+            dmax = fmaxf(dmax, fabsf(d));
+            dchg = fmaxf(dchg, fabsf(d - src[i]));
+        }
+        if (last) x[i] += (double)d;
+        else dst[i] = d;
+        i = inext;
+        s = sn;
+        e = en;
+    }
+    if (stats) reduce_stats(dmax, dchg, ctl, s_max);
+}
+
 // Same, two rows per thread per iteration (i and i + half the grid): two independent load chains
 // in flight per thread.
 __global__ void __launch_bounds__(256, 8) k_jacobi_direct2(int n, const int* __restrict__ roff,
@@ -898,7 +947,17 @@ int launch_jacobi_sweep(const RefineArgs& a, int src, bool last, bool stats) {
     const float* s = a.d32[src];
     float* d = a.d32[src ^ 1];
     const int st_flag = stats ? 1 : 0;
-    if (a.rhs == 1 && a.sell && a.sweep_kernel == 6) {
+    if (use_tiles(a) && a.roff && a.sweep_kernel == 7) {
+        static int grid_b4 = 0;
+        if (!grid_b4) grid_b4 = resident_grid((const void*)k_jacobi_batched<4, 8>, 256, a.sm_count);
+        k_jacobi_batched<4, 8><<<grid_b4, 256, 0, a.st>>>(a.n, a.roff, a.off, a.invd32, a.r32, s, d, a.x, last,
+                                                         st_flag, a.ctl);
+    } else if (use_tiles(a) && a.roff && a.sweep_kernel == 8) {
+        static int grid_b8 = 0;
+        if (!grid_b8) grid_b8 = resident_grid((const void*)k_jacobi_batched<8, 6>, 256, a.sm_count);
+        k_jacobi_batched<8, 6><<<grid_b8, 256, 0, a.st>>>(a.n, a.roff, a.off, a.invd32, a.r32, s, d, a.x, last,
+                                                         st_flag, a.ctl);
+    } else if (a.rhs == 1 && a.sell && a.sweep_kernel == 6) {
         static int grid_s = 0;
         if (!grid_s) grid_s = resident_grid((const void*)k_jacobi_sell, 256, a.sm_count);
         k_jacobi_sell<<<grid_s, 256, 0, a.st>>>(a.nslices, a.sell_perm, a.sell_len, a.sell_ptr, a.sell, a.invd32, a.r32,
