@@ -318,7 +318,7 @@ int Handle::enqueue(const sptrsv_opts& o, const double* b, double* x, int rhs, i
         RefineArgs ra{};
         if ((rc = refine_args(o, brm, xrm, rhs, &ra))) return rc;
         const bool jac = o.inner == SPTRSV_SCHED_JACOBI;
-        if ((rc = launch_refine_init(ra))) return rc;
+        if ((rc = launch_refine_init(ra, true))) return rc;
         if ((rc = mark(SPTRSV_K_INIT))) return rc;
         for (int s = 0; s < o.max_refine; ++s) {
             if ((rc = launch_residual(ra, jac, 0))) return rc;
@@ -492,7 +492,7 @@ int Handle::build_cond_graph(const sptrsv_opts& o, const double* b, double* x, i
     if (e == cudaSuccess) {
         if (!rc && conv) rc = launch_transpose(true, b, bw.as<double>(), n, rhs, st, &scratch_launches);
         if (!rc && cudaMemsetAsync(ctl, 0, sizeof(Ctl), st) != cudaSuccess) rc = SPTRSV_ERR_CUDA;
-        if (!rc) rc = launch_refine_init(ra);
+        if (!rc) rc = launch_refine_init(ra, true);
         if (!rc && add_while(g, ho, &obody) != cudaSuccess) rc = SPTRSV_ERR_CUDA;
         if (!rc && conv) rc = launch_transpose(false, xrm, x, n, rhs, st, &scratch_launches);
         cudaGraph_t g2 = nullptr;
@@ -756,7 +756,8 @@ int sptrsv_create(sptrsv_handle* out, int device) {
     if (rc) { delete h; return rc; }
     const char* g = getenv("SPTRSV_NO_GRAPH");
     h->use_graphs = !(g && g[0] == '1');
-    // tuning override of the Jacobi sweep kernel: direct (default), tile, tile8, direct2, tma, sell
+    // tuning override of the Jacobi sweep kernel: batch8 (default), batch4, direct, tile, tile8, direct2, tma,
+    // sell
     const char* sk = getenv("SPTRSV_SWEEP_KERNEL");
     h->sweep_kernel = 0;
     if (sk && strcmp(sk, "sell") == 0) h->sweep_kernel = 6;

@@ -41,6 +41,7 @@ struct Ctl {
     unsigned int dchg_bits;  // MIXED + JACOBI: max |d_new - d_old| of the last checked sweep
     int inner_count;       // MIXED + JACOBI: sweeps of the current inner solve
     int inner_total;       // MIXED + JACOBI: sweeps over the whole solve
+    int x_zero;            // MIXED: x is still the zero start vector (the residual is b)
 };
 
 template <typename T> struct Pend;

@@ -109,7 +109,7 @@ int sell_prepare(int n, const int* rp, int* perm, int* slen, int* sptr, int* par
 int sell_fill(int n, const int* rp, const int* col, const double* val, const int* perm, const int* slen,
               const int* sptr, int2* sell, int sm_count, cudaStream_t st, int64_t* launches);
 int sell_slices(int n);
-int launch_refine_init(const RefineArgs& a);
+int launch_refine_init(const RefineArgs& a, bool mark_zero);
 int launch_residual(const RefineArgs& a, bool jacobi_seed, int final_check);
 int launch_check(const RefineArgs& a, int step, bool reset_ticket);
 int launch_check_outer(const RefineArgs& a, int max_refine, cudaGraphConditionalHandle ho,

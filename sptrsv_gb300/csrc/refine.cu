@@ -91,6 +91,24 @@ __device__ __forceinline__ void seed_out(int seed, float* d0, size_t p, float r3
     else if (seed == 2) d0[p] = __uint_as_float(kPend32);
 }
 
+// r = b when x = 0 (the first correction of a solve): the matrix is not read.
+__device__ __forceinline__ void residual_of_b(int n, const double* __restrict__ b, const float* __restrict__ invd,
+                                              float* __restrict__ r32, float* __restrict__ d0, int seed,
+                                              double* __restrict__ rn2, double* s_acc) {
+    double acc = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double r = b[i];
+        const float rf = (float)r;
+        r32[i] = rf;
+        seed_out(seed, d0, i, rf, invd[i]);
+        acc = fma(r, r, acc);
+    }
+    acc = warp_sum(acc);
+    if ((threadIdx.x & 31) == 0) atomicAdd(s_acc, acc);
+    __syncthreads();
+    if (threadIdx.x == 0) atomicAdd(rn2, *s_acc);
+}
+
 // r = b - U x (rhs == 1), warp tiles of 32 rows staged in shared memory.
 __global__ void __launch_bounds__(kResWarps * 32) k_residual_tile(int n, const int* __restrict__ rp,
                                                                   const int* __restrict__ col,
@@ -106,6 +124,10 @@ __global__ void __launch_bounds__(kResWarps * 32) k_residual_tile(int n, const i
     if (is_done(ctl)) return;
     if (threadIdx.x == 0) s_acc = 0.0;
     __syncthreads();
+    if (*(volatile const int*)&ctl->x_zero) {
+        residual_of_b(n, b, invd, r32, d0, seed, rn2, &s_acc);
+        return;
+    }
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     int* sc = s_col[w];
     double* sv = s_val[w];
@@ -228,6 +250,7 @@ __device__ __forceinline__ double rel_of(int rhs, double* rn2, const double* bn2
 // Flat graphs: the convergence test of step `step`.
 __global__ void k_check(int rhs, double* rn2, const double* bn2, Ctl* ctl, double tol, int step, int reset_ticket) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    ctl->x_zero = 0;
     if (ctl->done) return;
     const double rel = rel_of(rhs, rn2, bn2);
     ctl->rel_res = rel;
@@ -245,6 +268,7 @@ __global__ void k_check_outer(int rhs, double* rn2, const double* bn2, Ctl* ctl,
     ctl->rel_res = rel;
     const int step = ctl->steps;
     const bool stop = rel <= tol || step >= max_refine;
+    ctl->x_zero = 0;
     if (rel <= tol) ctl->done = 1;
     ctl->inner_count = 0;
     ctl->dmax_bits = 0u;
@@ -885,8 +909,18 @@ int launch_build_offdiag(int n, const int* rp, const int* col, const double* val
     return 0;
 }
 
-int launch_refine_init(const RefineArgs& a) {
+__global__ void k_mark_x_zero(Ctl* ctl) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) ctl->x_zero = 1;
+}
+
+// x = 0, ||b_c||^2; the device-looped graphs also mark x as zero so that their first residual
+// is taken from b without reading the matrix.
+int launch_refine_init(const RefineArgs& a, bool mark_zero) {
     CUDA_TRY(cudaMemsetAsync(a.x, 0, sizeof(double) * (size_t)a.n * a.rhs, a.st));
+    if (mark_zero) {
+        k_mark_x_zero<<<1, 32, 0, a.st>>>(a.ctl);
+        ++*a.launches;
+    }
     CUDA_TRY(cudaMemsetAsync(a.rn2, 0, sizeof(double) * a.rhs, a.st));
     CUDA_TRY(cudaMemsetAsync(a.bn2, 0, sizeof(double) * a.rhs, a.st));
     k_colnorm2<<<stream_grid(a.sm_count), 256, sizeof(double) * a.rhs, a.st>>>(a.n, a.rhs, a.b, a.bn2);
@@ -947,12 +981,12 @@ int launch_jacobi_sweep(const RefineArgs& a, int src, bool last, bool stats) {
     const float* s = a.d32[src];
     float* d = a.d32[src ^ 1];
     const int st_flag = stats ? 1 : 0;
-    if (use_tiles(a) && a.roff && a.sweep_kernel == 7) {
+    if (use_tiles(a) && a.roff && (a.sweep_kernel == 7)) {
         static int grid_b4 = 0;
         if (!grid_b4) grid_b4 = resident_grid((const void*)k_jacobi_batched<4, 8>, 256, a.sm_count);
         k_jacobi_batched<4, 8><<<grid_b4, 256, 0, a.st>>>(a.n, a.roff, a.off, a.invd32, a.r32, s, d, a.x, last,
                                                          st_flag, a.ctl);
-    } else if (use_tiles(a) && a.roff && a.sweep_kernel == 8) {
+    } else if (use_tiles(a) && a.roff && (a.sweep_kernel == 8 || a.sweep_kernel == 0)) {
         static int grid_b8 = 0;
         if (!grid_b8) grid_b8 = resident_grid((const void*)k_jacobi_batched<8, 6>, 256, a.sm_count);
         k_jacobi_batched<8, 6><<<grid_b8, 256, 0, a.st>>>(a.n, a.roff, a.off, a.invd32, a.r32, s, d, a.x, last,
@@ -967,7 +1001,7 @@ int launch_jacobi_sweep(const RefineArgs& a, int src, bool last, bool stats) {
         if (!grid_d2) grid_d2 = resident_grid((const void*)k_jacobi_direct2, 256, a.sm_count);
         k_jacobi_direct2<<<grid_d2, 256, 0, a.st>>>(a.n, a.roff, a.off, a.invd32, a.r32, s, d, a.x, last, st_flag,
                                                    a.ctl);
-    } else if (use_tiles(a) && a.roff && (a.sweep_kernel == 0 || a.sweep_kernel == 2)) {
+    } else if (use_tiles(a) && a.roff && a.sweep_kernel == 2) {
         static int grid_d = 0;
         if (!grid_d) grid_d = resident_grid((const void*)k_jacobi_direct, 256, a.sm_count);
         k_jacobi_direct<<<grid_d, 256, 0, a.st>>>(a.n, a.roff, a.off, a.invd32, a.r32, s, d, a.x, last, st_flag, a.ctl);
