@@ -56,7 +56,8 @@ enum sptrsv_schedule {
     SPTRSV_SCHED_SYNCFREE_CSC = 3,  /* CSC push with per-row in-degree counters (kernel_full.cl family) */
     SPTRSV_SCHED_LEVELSET = 4,      /* persistent kernel, one grid barrier per level */
     SPTRSV_SCHED_JACOBI = 5,        /* iterative sweeps x <- D^-1 (b - N x); mixed precision only */
-    SPTRSV_SCHED_SUPERNODAL = 6     /* dense supernode blocks on tensor cores */
+    SPTRSV_SCHED_SUPERNODAL = 6,    /* dense supernode blocks on tensor cores */
+    SPTRSV_SCHED_SYNCFREE_BLOCK = 7 /* CSR pull, 512-row blocks per CTA with their x in shared memory */
 };
 
 enum sptrsv_precision {
@@ -82,7 +83,8 @@ enum sptrsv_kernel_kind {
     SPTRSV_K_JACOBI = 9,       /* FP32 Jacobi sweep */
     SPTRSV_K_INNER = 10,       /* exact FP32 inner solve */
     SPTRSV_K_AXPY = 11,        /* x += d */
-    SPTRSV_K_TRANSPOSE = 12    /* column-major <-> row-major */
+    SPTRSV_K_TRANSPOSE = 12,   /* column-major <-> row-major */
+    SPTRSV_K_PULL_BLOCK = 13   /* sync-free CSR pull, shared-memory blocks */
 };
 
 typedef struct sptrsv_opts {

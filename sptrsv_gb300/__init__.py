@@ -19,7 +19,7 @@ from . import _lib
 from ._lib import Opts
 
 SCHED = {"auto": 0, "syncfree_warp": 1, "syncfree_thread": 2, "syncfree_csc": 3, "levelset": 4, "jacobi": 5,
-         "supernodal": 6}
+         "supernodal": 6, "syncfree_block": 7}
 PREC = {"fp64": 0, "mixed": 1}
 COL_MAJOR, ROW_MAJOR = 0, 1
 

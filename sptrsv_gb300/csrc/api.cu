@@ -299,6 +299,19 @@ int Handle::enqueue(const sptrsv_opts& o, const double* b, double* x, int rhs, i
                 if ((rc = launch_pull_warp(false, a, o.rows_per_warp, o.rhs_tile))) return rc;
                 if ((rc = mark(SPTRSV_K_PULL_WARP))) return rc;
                 break;
+            case SPTRSV_SCHED_SYNCFREE_BLOCK:
+                if (rhs == 1) {
+                    if ((rc = launch_fill_pending(false, xrm, (size_t)n * rhs, st, &launches))) return rc;
+                    if ((rc = mark(SPTRSV_K_FILL))) return rc;
+                    if ((rc = launch_bsf(false, a))) return rc;
+                    if ((rc = mark(SPTRSV_K_PULL_BLOCK))) return rc;
+                    break;
+                }
+                if ((rc = launch_fill_pending(false, xrm, (size_t)n * rhs, st, &launches))) return rc;
+                if ((rc = mark(SPTRSV_K_FILL))) return rc;
+                if ((rc = launch_pull_warp(false, a, o.rows_per_warp, o.rhs_tile))) return rc;
+                if ((rc = mark(SPTRSV_K_PULL_WARP))) return rc;
+                break;
             case SPTRSV_SCHED_SYNCFREE_CSC:
                 CUDA_TRY(cudaMemcpyAsync(indeg_work.p, in_degree.p, sizeof(int) * (size_t)n, cudaMemcpyDeviceToDevice, st));
                 CUDA_TRY(cudaMemsetAsync(left.p, 0, sizeof(double) * (size_t)n * rhs, st));

@@ -65,6 +65,7 @@ struct SolveArgs {
 int launch_fill_pending(bool f32, void* x, size_t count, cudaStream_t st, int64_t* launches);
 int launch_pull_warp(bool f32, const SolveArgs& a, int rows_per_warp, int rhs_tile);
 int launch_pull_thread(bool f32, const SolveArgs& a);
+int launch_bsf(bool f32, const SolveArgs& a);
 int launch_push_csc(const SolveArgs& a, const int* cp, const int* crow, const double* cval, int* indeg_work,
                     double* left_sum);
 int launch_levelset(bool f32, const SolveArgs& a, int max_level, const int* lptr, const int* lrows);

@@ -134,6 +134,76 @@ __global__ void __launch_bounds__(256) k_pull_thread(int n, const int* __restric
     }
 }
 
+// Block sync-free (SYNCFREE_BLOCK): a CTA claims a block of kBsfRows consecutive rows (blocks in
+// decreasing order through the ticket) and solves it with one thread per row, each walking its
+// row from the right.  The block's own x values live in shared memory, so a dependency inside
+// the block is a shared-memory poll (~90 ns on this GPU) instead of an L2 round trip (~375 ns);
+// dependencies on higher blocks use the self-flagging global x.  Forward progress: a block only
+// waits on higher blocks (claimed earlier by running CTAs) and on higher rows of its own block
+// (threads of the same CTA, which never wait on lower rows).  The final update is a single FMA
+// with b_i * invd_i precomputed, which shortens the FP64 chain after the last dependency.
+constexpr int kBsfRows = 512;
+
+template <typename T>
+__global__ void __launch_bounds__(kBsfRows) k_bsf(int n, const int* __restrict__ rp, const int* __restrict__ col,
+                                                  const T* __restrict__ val, const T* __restrict__ invd,
+                                                  const T* __restrict__ b, T* x, Ctl* ctl, int64_t budget) {
+    __shared__ T xs[kBsfRows];
+    __shared__ unsigned s_ticket;
+    const int nblk = (n + kBsfRows - 1) / kBsfRows;
+    for (;;) {
+        // thread 0 decides for the whole CTA (a uniform exit keeps the barriers matched)
+        if (threadIdx.x == 0) s_ticket = aborted(ctl) ? 0xFFFFFFFFu : atomicAdd(&ctl->ticket, 1u);
+        __syncthreads();
+        const unsigned t = s_ticket;
+        if (t >= (unsigned)nblk) break;
+        const int blk = nblk - 1 - (int)t;
+        const int lo = blk * kBsfRows, hi = min(n, lo + kBsfRows);
+        xs[threadIdx.x] = Pend<T>::value();
+        __syncthreads();
+        const int i = hi - 1 - (int)threadIdx.x;  // thread 0 takes the block's highest row
+        bool ok = true;
+        if (i >= lo) {
+            const int s = rp[i], e = rp[i + 1];
+            const T di = invd[i];
+            const T bd = b[i] * di;
+            T sum = T(0);
+            for (int k = e - 1; k > s && ok; --k) {
+                const int c = col[k];
+                T xv;
+                if (c >= hi) {
+                    ok = wait_ready<T>(x + c, xv, ctl, budget);
+                } else {
+                    volatile T* p = xs + (c - lo);
+                    xv = *p;
+                    if (Pend<T>::is(xv)) {
+                        const uint64_t t0 = gtimer();
+                        unsigned polls = 0;
+                        while (Pend<T>::is(xv = *p)) {
+                            if ((++polls & 63u) == 0) {
+                                if (aborted(ctl)) { ok = false; break; }
+                                if ((int64_t)(gtimer() - t0) > budget) {
+                                    record_error(ctl, SPTRSV_ERR_TIMEOUT);
+                                    ok = false;
+                                    break;
+                                }
+                            }
+                        }
+                    }
+                }
+                if (ok) sum = fma_t(val[k], xv, sum);
+            }
+            if (ok) {
+                const T xi = Pend<T>::fix(fma_t(-sum, di, bd));
+                ((volatile T*)xs)[i - lo] = xi;
+                st_relaxed(x + i, xi);
+            }
+        }
+        __syncthreads();
+        if (__syncthreads_or(!ok)) break;
+    }
+}
+
 __global__ void __launch_bounds__(256) k_push_csc(int n, int rhs, const int* __restrict__ cp,
                                                   const int* __restrict__ crow, const double* __restrict__ cval,
                                                   const double* __restrict__ invd, const double* __restrict__ b,
@@ -319,6 +389,28 @@ static int pull_thread_t(const SolveArgs& a) {
 int launch_pull_thread(bool f32, const SolveArgs& a) {
     if (a.rhs != 1) return SPTRSV_ERR_UNSUPPORTED;
     return f32 ? pull_thread_t<float>(a) : pull_thread_t<double>(a);
+}
+
+template <typename T>
+static int bsf_t(const SolveArgs& a) {
+    const void* fn = (const void*)k_bsf<T>;
+    const int nblk = (a.n + kBsfRows - 1) / kBsfRows;
+    int grid = grid_for(fn, kBsfRows, a.sm_count, a.warps);
+    if (grid > nblk) grid = nblk;
+    const T* val = (const T*)a.val;
+    const T* invd = (const T*)a.invd;
+    const T* b = (const T*)a.b;
+    T* x = (T*)a.x;
+    void* args[] = {(void*)&a.n, (void*)&a.rp, (void*)&a.col, (void*)&val, (void*)&invd, (void*)&b, (void*)&x,
+                    (void*)&a.ctl, (void*)&a.budget};
+    CUDA_TRY(cudaLaunchKernel(fn, grid, kBsfRows, args, 0, a.st));
+    ++*a.launches;
+    return 0;
+}
+
+int launch_bsf(bool f32, const SolveArgs& a) {
+    if (a.rhs != 1) return SPTRSV_ERR_UNSUPPORTED;
+    return f32 ? bsf_t<float>(a) : bsf_t<double>(a);
 }
 
 int launch_push_csc(const SolveArgs& a, const int* cp, const int* crow, const double* cval, int* indeg_work,

@@ -23,7 +23,7 @@ RES_TOL = 1e-12
 MIXED_ELEM_TOL = 1e-8
 GOLDEN_CASES = ["csr_5_upper", "csr_6_upper", "rand3000", "lap12", "chain500", "snr800"]
 FP64_SCHEDULES = [("syncfree_warp", 1), ("syncfree_warp", 2), ("syncfree_warp", 4), ("syncfree_warp", 8),
-                  ("syncfree_thread", 0), ("syncfree_csc", 0), ("levelset", 0)]
+                  ("syncfree_thread", 0), ("syncfree_block", 0), ("syncfree_csc", 0), ("levelset", 0)]
 
 
 def _case(g, tag):
@@ -76,7 +76,7 @@ def test_fp64_schedules_match_reference(golden, orc, solver, tag, sched, rpw):
     rp, col, val, b, rhs = _case(golden, tag)
     solver.analyse(rp, col, val)
     ref = golden[tag + "/base"]
-    if sched == "syncfree_thread":
+    if sched in ("syncfree_thread", "syncfree_block"):
         rhs_run, bb, ref = 1, b[: len(rp) - 1], ref[: len(rp) - 1]
     else:
         rhs_run, bb = rhs, b
@@ -101,11 +101,11 @@ def test_multi_rhs(orc, solver, rhs, layout, sched):
     assert elem_err(x, ref) <= ELEM_TOL
 
 
-@pytest.mark.parametrize("inner", ["jacobi", "syncfree_warp", "syncfree_thread", "levelset"])
+@pytest.mark.parametrize("inner", ["jacobi", "syncfree_warp", "syncfree_thread", "syncfree_block", "levelset"])
 @pytest.mark.parametrize("tag", ["rand3000", "lap12", "snr800"])
 def test_mixed_refinement_reaches_1e12(golden, orc, solver, inner, tag):
     rp, col, val, b, rhs = _case(golden, tag)
-    rhs_run = 1 if inner == "syncfree_thread" else rhs
+    rhs_run = 1 if inner in ("syncfree_thread", "syncfree_block") else rhs
     bb = b[: (len(rp) - 1) * rhs_run]
     solver.analyse(rp, col, val)
     x = solver.solve(bb, rhs=rhs_run, precision="mixed", schedule=inner, max_refine=20)
@@ -263,10 +263,11 @@ def test_spin_budget_timeout_then_recovery(orc, solver):
     val[1::2] = -1.0
     solver.analyse(rp, col, val)
     b = np.ones(n)
-    with pytest.raises(sp.SptrsvError) as e:
-        solver.solve(b, schedule="syncfree_warp", spin_budget_ns=1)
-    assert e.value.status == -9
-    x = solver.solve(b, schedule="syncfree_warp")
+    for sched in ("syncfree_warp", "syncfree_block"):
+        with pytest.raises(sp.SptrsvError) as e:
+            solver.solve(b, schedule=sched, spin_budget_ns=1)
+        assert e.value.status == -9
+    x = solver.solve(b, schedule="syncfree_block")
     ref = orc.base_gauss_upper(rp.astype(np.uint64), col, val, b, 1)
     assert elem_err(x, ref) <= ELEM_TOL
 
@@ -292,8 +293,9 @@ def test_irregular_2m_full(orc, solver):
     m, xs, b = gen.irregular_case()
     solver.analyse(m.row_ptr, m.col, m.val)
     ref = orc.base_gauss_upper(m.row_ptr.astype(np.uint64), m.col, m.val, b, 1)
-    x = solver.solve(b, schedule="syncfree_warp")
-    assert elem_err(x, ref) <= ELEM_TOL
+    for sched in ("syncfree_warp", "syncfree_block"):
+        x = solver.solve(b, schedule=sched)
+        assert elem_err(x, ref) <= ELEM_TOL, sched
     x = solver.solve(b, precision="mixed", schedule="jacobi")
     steps, res = solver.last_refine()
     assert res <= RES_TOL
