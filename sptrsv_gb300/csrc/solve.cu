@@ -162,44 +162,51 @@ __global__ void __launch_bounds__(kBsfRows) k_bsf(int n, const int* __restrict__
         xs[threadIdx.x] = Pend<T>::value();
         __syncthreads();
         const int i = hi - 1 - (int)threadIdx.x;  // thread 0 takes the block's highest row
-        bool ok = true;
-        if (i >= lo) {
-            const int s = rp[i], e = rp[i + 1];
-            const T di = invd[i];
-            const T bd = b[i] * di;
-            T sum = T(0);
-            for (int k = e - 1; k > s && ok; --k) {
+        bool ok = true, done = i < lo;
+        int k = 0, s = 0;
+        T sum = T(0), di = T(0), bd = T(0);
+        if (!done) {
+            s = rp[i];
+            k = rp[i + 1] - 1;
+            di = invd[i];
+            bd = b[i] * di;
+            // phase 1: entries in higher blocks (rightmost in the row) through the global x
+            for (; k > s; --k) {
                 const int c = col[k];
+                if (c < hi) break;
                 T xv;
-                if (c >= hi) {
-                    ok = wait_ready<T>(x + c, xv, ctl, budget);
-                } else {
-                    volatile T* p = xs + (c - lo);
-                    xv = *p;
-                    if (Pend<T>::is(xv)) {
-                        const uint64_t t0 = gtimer();
-                        unsigned polls = 0;
-                        while (Pend<T>::is(xv = *p)) {
-                            if ((++polls & 63u) == 0) {
-                                if (aborted(ctl)) { ok = false; break; }
-                                if ((int64_t)(gtimer() - t0) > budget) {
-                                    record_error(ctl, SPTRSV_ERR_TIMEOUT);
-                                    ok = false;
-                                    break;
-                                }
-                            }
-                        }
-                    }
-                }
-                if (ok) sum = fma_t(val[k], xv, sum);
-            }
-            if (ok) {
-                const T xi = Pend<T>::fix(fma_t(-sum, di, bd));
-                ((volatile T*)xs)[i - lo] = xi;
-                st_relaxed(x + i, xi);
+                if (!wait_ready<T>(x + c, xv, ctl, budget)) { ok = false; break; }
+                sum = fma_t(val[k], xv, sum);
             }
         }
-        __syncthreads();
+        // phase 2: entries inside the block, in warp lockstep: every lane consumes whatever is
+        // ready, then the warp polls again together (no lane spins alone in divergent code)
+        const uint64_t t0 = gtimer();
+        unsigned iter = 0;
+        if (!ok) done = true;
+        while (!__all_sync(0xffffffffu, done)) {
+            if (!done) {
+                for (; k > s; --k) {
+                    const T xv = ((volatile T*)xs)[col[k] - lo];
+                    if (Pend<T>::is(xv)) break;
+                    sum = fma_t(val[k], xv, sum);
+                }
+                if (k == s) {
+                    const T xi = Pend<T>::fix(fma_t(-sum, di, bd));
+                    ((volatile T*)xs)[i - lo] = xi;
+                    st_relaxed(x + i, xi);
+                    done = true;
+                }
+            }
+            if ((++iter & 255u) == 0) {
+                if (aborted(ctl)) { ok = false; done = true; }
+                else if ((int64_t)(gtimer() - t0) > budget) {
+                    record_error(ctl, SPTRSV_ERR_TIMEOUT);
+                    ok = false;
+                    done = true;
+                }
+            }
+        }
         if (__syncthreads_or(!ok)) break;
     }
 }
