@@ -203,8 +203,10 @@ sptrsv_opts Handle::resolve(const sptrsv_opts* o, int rhs) const {
         if (r.precision == SPTRSV_PREC_MIXED) {
             r.schedule = SPTRSV_SCHED_JACOBI;
         } else {
-            r.schedule = (levels_ready && width >= 2048.0 && max_level <= 2000) ? SPTRSV_SCHED_LEVELSET
-                                                                                  : SPTRSV_SCHED_SYNCFREE_WARP;
+            // wide, shallow DAGs: one grid barrier per level is cheap; otherwise the block
+            // sync-free kernel for one RHS and the RHS-tiled warp kernel for several
+            if (levels_ready && width >= 2048.0 && max_level <= 2000) r.schedule = SPTRSV_SCHED_LEVELSET;
+            else r.schedule = rhs == 1 ? SPTRSV_SCHED_SYNCFREE_BLOCK : SPTRSV_SCHED_SYNCFREE_WARP;
         }
     }
     if (r.precision == SPTRSV_PREC_MIXED) {
@@ -220,7 +222,6 @@ sptrsv_opts Handle::resolve(const sptrsv_opts* o, int rhs) const {
         const double m = mean_len;
         r.rows_per_warp = m <= 6 ? 8 : (m <= 12 ? 4 : (m <= 24 ? 2 : 1));
     }
-    (void)rhs;
     return r;
 }
 
