@@ -103,3 +103,144 @@ def irregular_case(n=2_000_000, seed=1):
     m = random_upper(n, 8.0, 0.9, 64, seed)
     xs, b = system(m, seed)
     return m, xs, b
+
+
+# --------------------------------------------------------------------------------------------
+# 3D Laplacian, nested dissection, supernodal Cholesky (the supernodal workload)
+
+def _nd_tree(g, leaf):
+    """Geometric nested dissection of the g^3 grid: recursive bisection of the longest side at its
+    middle plane until no side exceeds `leaf`.  Returns (order, nodes): order[k] = grid index of
+    the k-th unknown; nodes = postordered list of (first, last+1, parent) pivot ranges."""
+    order = []
+    nodes = []
+
+    def rec(box):
+        (x0, x1), (y0, y1), (z0, z1) = box
+        sides = (x1 - x0, y1 - y0, z1 - z0)
+        if min(sides) <= 0:
+            return None
+        if max(sides) <= leaf:
+            first = len(order)
+            for z in range(z0, z1):
+                for y in range(y0, y1):
+                    for x in range(x0, x1):
+                        order.append((z * g + y) * g + x)
+            nodes.append([first, len(order), -1])
+            return len(nodes) - 1
+        d = sides.index(max(sides))
+        lo, hi = box[d]
+        m = (lo + hi) // 2
+        left = list(box)
+        right = list(box)
+        sep = list(box)
+        left[d] = (lo, m)
+        right[d] = (m + 1, hi)
+        sep[d] = (m, m + 1)
+        kids = [k for k in (rec(tuple(left)), rec(tuple(right))) if k is not None]
+        first = len(order)
+        (sx0, sx1), (sy0, sy1), (sz0, sz1) = sep
+        for z in range(sz0, sz1):
+            for y in range(sy0, sy1):
+                for x in range(sx0, sx1):
+                    order.append((z * g + y) * g + x)
+        nodes.append([first, len(order), -1])
+        me = len(nodes) - 1
+        for k in kids:
+            nodes[k][2] = me
+        return me
+
+    rec(((0, g), (0, g), (0, g)))
+    return np.array(order, dtype=np.int64), nodes
+
+
+def laplace3d_nd_cholesky(g=40, leaf=8, max_width=400):
+    """Exact upper Cholesky factor U (A = U^T U) of the 7-point 3D Laplacian (diag 6, off -1) on a
+    g^3 grid under geometric nested dissection (recursive coordinate-plane bisection down to
+    leaf^3 boxes), with its supernode partition.  Multifrontal factorisation over the dissection
+    tree with dense fronts; every front's pivot block is a supernode (dense triangle plus one
+    shared set of columns to its right), split into chunks of at most `max_width` rows."""
+    import scipy.linalg as sla
+    order, nodes = _nd_tree(g, leaf)
+    n = g ** 3
+    inv = np.empty(n, dtype=np.int64)
+    inv[order] = np.arange(n)
+
+    def neighbours(p):
+        z, rem = divmod(int(p), g * g)
+        y, x = divmod(rem, g)
+        out = []
+        for dz, dy, dx in ((1, 0, 0), (-1, 0, 0), (0, 1, 0), (0, -1, 0), (0, 0, 1), (0, 0, -1)):
+            zz, yy, xx = z + dz, y + dy, x + dx
+            if 0 <= zz < g and 0 <= yy < g and 0 <= xx < g:
+                out.append(inv[(zz * g + yy) * g + xx])
+        return out
+
+    children = [[] for _ in nodes]
+    for k, (_, _, par) in enumerate(nodes):
+        if par >= 0:
+            children[par].append(k)
+    upd = [None] * len(nodes)       # (structure, dense update matrix) handed to the parent
+    cols = {}                       # pivot column -> (row indices, values) of L
+    for t, (f0, f1, _) in enumerate(nodes):
+        piv = np.arange(f0, f1)
+        below = set()
+        for p in piv:
+            for q in neighbours(order[p]):
+                if q >= f1:
+                    below.add(int(q))
+        for c in children[t]:
+            below.update(int(v) for v in upd[c][0] if v >= f1)
+        S = np.concatenate([piv, np.array(sorted(below), dtype=np.int64)])
+        m, w = len(S), f1 - f0
+        F = np.zeros((m, m))
+        pos = {int(v): k for k, v in enumerate(S)}
+        for k, p in enumerate(piv):
+            F[k, k] = 6.0
+            for q in neighbours(order[p]):
+                if q >= f0:
+                    j = pos[int(q)]
+                    F[j, k] = -1.0
+                    F[k, j] = -1.0
+        for c in children[t]:
+            cs, cu = upd[c]
+            idx = np.searchsorted(S, cs)
+            for r in range(len(idx)):  # extend-add, one row at a time
+                F[idx[r], idx] += cu[r]
+            upd[c] = None
+        L11 = sla.cholesky(F[:w, :w], lower=True)
+        if m > w:
+            L21 = sla.solve_triangular(L11, F[w:, :w].T, lower=True).T
+            upd[t] = (S[w:], F[w:, w:] - L21 @ L21.T)
+            Lcol = np.vstack([L11, L21])
+        else:
+            upd[t] = (S[w:], np.zeros((0, 0)))
+            Lcol = L11
+        for k in range(w):
+            rows = S[k:]
+            cols[f0 + k] = (rows, Lcol[k:, k])
+    lens = np.array([len(cols[i][0]) for i in range(n)], dtype=np.int64)
+    row_ptr = np.concatenate([[0], np.cumsum(lens)])
+    col = np.empty(row_ptr[-1], dtype=np.int32)
+    val = np.empty(row_ptr[-1])
+    for i in range(n):
+        r, v = cols[i]
+        col[row_ptr[i]:row_ptr[i + 1]] = r
+        val[row_ptr[i]:row_ptr[i + 1]] = v
+    sn = [0]
+    for f0, f1, _ in nodes:
+        w = f1 - f0
+        k = -(-w // max_width)
+        step = -(-w // k)
+        for a in range(f0, f1, step):
+            sn.append(min(f1, a + step))
+    m = Csr(row_ptr, col, val, np.array(sn, dtype=np.int32))
+    m.perm = order
+    return m
+
+
+def supernodal_case(g=40, rhs=1, seed=3):
+    """The supernodal workload: 40^3 3D Laplacian factor under nested dissection, B ~ U[-1,1]."""
+    m = laplace3d_nd_cholesky(g)
+    xs = uniform((int(seed) + XSTAR_SALT) % (1 << 64), m.n * rhs)
+    return m, xs, spmv(m, xs, rhs)
