@@ -84,7 +84,8 @@ enum sptrsv_kernel_kind {
     SPTRSV_K_INNER = 10,       /* exact FP32 inner solve */
     SPTRSV_K_AXPY = 11,        /* x += d */
     SPTRSV_K_TRANSPOSE = 12,   /* column-major <-> row-major */
-    SPTRSV_K_PULL_BLOCK = 13   /* sync-free CSR pull, shared-memory blocks */
+    SPTRSV_K_PULL_BLOCK = 13,  /* sync-free CSR pull, shared-memory blocks */
+    SPTRSV_K_SUPERNODAL = 14   /* supernode panel products (FP64, or BF16x3 tensor cores) */
 };
 
 typedef struct sptrsv_opts {
@@ -121,6 +122,13 @@ SPTRSV_API int sptrsv_analyse_host(sptrsv_handle h, int n, int64_t nnz, const in
 /* Same on caller-owned device arrays (int32 row pointer); the handle keeps the pointers. */
 SPTRSV_API int sptrsv_analyse_device(sptrsv_handle h, int n, int nnz, const int* d_row_ptr, const int* d_col,
                           const double* d_val);
+
+/* Supernode partition of the analysed matrix (host array of sn+1 row boundaries, 0 ... n), as in
+ * supernodal_upper (core.h:12, core.cpp:80-92): every row of a supernode holds the dense upper
+ * triangle of the supernode followed by one column set shared by the whole supernode.  Builds
+ * the dense panels [T^-1 | -T^-1 Rect] (FP64 and BF16 hi/lo) for SPTRSV_SCHED_SUPERNODAL; AUTO then
+ * picks that schedule.  SPTRSV_ERR_SUPERNODES when the matrix does not have the layout. */
+SPTRSV_API int sptrsv_set_supernodes(sptrsv_handle h, int sn, const int* supernodes);
 
 /* Analysis results copied to host memory. */
 SPTRSV_API int sptrsv_info(sptrsv_handle h, int* n, int* nnz, int* max_level);

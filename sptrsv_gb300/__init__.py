@@ -178,6 +178,12 @@ class Solver:
         self.n, self.nnz = n, nnz
         return self
 
+    def set_supernodes(self, supernodes):
+        """Supernode partition (sn+1 boundaries); enables the supernodal schedule."""
+        sn = _c(supernodes, np.int32)
+        _check(_lib.lib().sptrsv_set_supernodes(self._h, len(sn) - 1, sn), "set_supernodes")
+        return self
+
     def info(self):
         n, nnz, ml = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
         _check(_lib.lib().sptrsv_info(self._h, ctypes.byref(n), ctypes.byref(nnz), ctypes.byref(ml)), "info")

@@ -73,6 +73,7 @@ C_API = {
     "sptrsv_destroy": ([c_vp], c_int),
     "sptrsv_analyse_host": ([c_vp, c_int, c_i64, i64, i32, f64], c_int),
     "sptrsv_analyse_device": ([c_vp, c_int, c_int, c_vp, c_vp, c_vp], c_int),
+    "sptrsv_set_supernodes": ([c_vp, c_int, i32], c_int),
     "sptrsv_info": ([c_vp, _c_int_p, _c_int_p, _c_int_p], c_int),
     "sptrsv_get_levels": ([c_vp, u64], c_int),
     "sptrsv_get_in_degree": ([c_vp, i32], c_int),

@@ -83,6 +83,7 @@ void Handle::drop_matrix() {
     levels_ready = false;
     have_csc = false;
     have_offdiag = false;
+    have_supernodes = false;
     n = nnz = max_level = 0;
     rp = col = nullptr;
     val = nullptr;
@@ -200,7 +201,9 @@ sptrsv_opts Handle::resolve(const sptrsv_opts* o, int rhs) const {
     if (r.max_refine <= 0) r.max_refine = 8;
     const double width = (double)n / (max_level > 0 ? max_level : 1);
     if (r.schedule == SPTRSV_SCHED_AUTO) {
-        if (r.precision == SPTRSV_PREC_MIXED) {
+        if (have_supernodes) {
+            r.schedule = SPTRSV_SCHED_SUPERNODAL;
+        } else if (r.precision == SPTRSV_PREC_MIXED) {
             r.schedule = SPTRSV_SCHED_JACOBI;
         } else {
             // wide, shallow DAGs: one grid barrier per level is cheap; otherwise the block
@@ -325,6 +328,13 @@ int Handle::enqueue(const sptrsv_opts& o, const double* b, double* x, int rhs, i
                 if ((rc = launch_levelset(false, a, max_level, level_ptr.as<int>(), level_rows.as<int>()))) return rc;
                 if ((rc = mark(SPTRSV_K_LEVELSET))) return rc;
                 break;
+            case SPTRSV_SCHED_SUPERNODAL:
+                if (!have_supernodes) return SPTRSV_ERR_SUPERNODES;
+                if ((rc = launch_fill_pending(false, xrm, (size_t)n * rhs, st, &launches))) return rc;
+                if ((rc = mark(SPTRSV_K_FILL))) return rc;
+                if ((rc = launch_sn_solve(*this, false, brm, xrm, rhs, o.spin_budget_ns, &launches))) return rc;
+                if ((rc = mark(SPTRSV_K_SUPERNODAL))) return rc;
+                break;
             default:
                 return SPTRSV_ERR_UNSUPPORTED;
         }
@@ -351,6 +361,12 @@ int Handle::enqueue(const sptrsv_opts& o, const double* b, double* x, int rhs, i
                         src ^= 1;
                     }
                 }
+            } else if (o.inner == SPTRSV_SCHED_SUPERNODAL) {
+                if (!have_supernodes) return SPTRSV_ERR_SUPERNODES;
+                if ((rc = launch_sn_solve(*this, true, ra.r32, ra.d32[0], rhs, o.spin_budget_ns, &launches))) return rc;
+                if ((rc = mark(SPTRSV_K_SUPERNODAL))) return rc;
+                if ((rc = launch_axpy_pending(ra, 0))) return rc;
+                if ((rc = mark(SPTRSV_K_AXPY))) return rc;
             } else {
                 if ((rc = launch_exact_inner(ra, o.inner, o.rows_per_warp, 0, max_level, level_ptr.as<int>(),
                                              level_rows.as<int>(), resident_warps(o))))
@@ -690,7 +706,9 @@ Handle::~Handle() {
     if (prof0) cudaEventDestroy(prof0);
     DevBuf* bufs[] = {&own_rp, &own_col, &own_val, &val32, &invd, &invd32, &in_degree, &levels, &level_ptr,
                       &level_rows, &stats, &csc_ptr, &csc_row, &csc_val, &scratch, &xw, &bw, &r32, &d32a, &d32b,
-                      &norms, &indeg_work, &left, &db, &dx, &flush, &offdiag, &roff, &sell, &sell_perm, &sell_len, &sell_ptr};
+                      &norms, &indeg_work, &left, &db, &dx, &flush, &offdiag, &roff, &sell, &sell_perm, &sell_len, &sell_ptr,
+                      &sn_start, &sn_m, &sn_roff, &sn_rect, &sn_goff, &sn_ld, &sn_colbase, &sn_outbase, &sn_items,
+                      &sn_G, &sn_Ghi, &sn_Glo};
     for (DevBuf* b : bufs) b->release();
     if (ctl) cudaFree(ctl);
     if (ev0) cudaEventDestroy(ev0);
@@ -818,6 +836,11 @@ int sptrsv_analyse_device(sptrsv_handle hh, int n, int nnz, const int* d_row_ptr
     int rc = h->analyse();
     if (rc) return rc;
     return h->ensure_levels();
+}
+
+int sptrsv_set_supernodes(sptrsv_handle hh, int sn, const int* supernodes) {
+    H();
+    return h->set_supernodes(sn, supernodes);
 }
 
 int sptrsv_info(sptrsv_handle hh, int* n, int* nnz, int* max_level) {

@@ -186,8 +186,10 @@ static double supernodal_inplace(size_t sn, int* supernodes, double* x, double* 
     if (c.status) return fail(c.status);
     std::vector<double> bcopy(x, x + (size_t)n * rhs);
     double secs = 0;
-    if ((rc = solve_host_timed(h, fp64(SPTRSV_SCHED_AUTO), bcopy.data(), x, rhs, SPTRSV_COL_MAJOR, &secs)))
-        return fail(rc);
+    // dense supernode panels when every supernode's rows share one rectangle; otherwise (the
+    // reference also accepts rows with their own rectangle entries) the general FP64 solve
+    const int sched = h->set_supernodes((int)sn, supernodes) == 0 ? SPTRSV_SCHED_SUPERNODAL : SPTRSV_SCHED_AUTO;
+    if ((rc = solve_host_timed(h, fp64(sched), bcopy.data(), x, rhs, SPTRSV_COL_MAJOR, &secs))) return fail(rc);
     set_last_status(0);
     return secs;
 }
@@ -243,8 +245,8 @@ static double blas_padded(int n, int nz, size_t sn, int* supernodes, double* x, 
     if ((rc = h->analyse())) return fail(rc);
     std::vector<double> bcopy(x, x + (size_t)n * rhs);
     double secs = 0;
-    if ((rc = solve_host_timed(h, fp64(SPTRSV_SCHED_AUTO), bcopy.data(), x, rhs, SPTRSV_COL_MAJOR, &secs)))
-        return fail(rc);
+    const int sched = h->set_supernodes((int)sn, supernodes) == 0 ? SPTRSV_SCHED_SUPERNODAL : SPTRSV_SCHED_AUTO;
+    if ((rc = solve_host_timed(h, fp64(sched), bcopy.data(), x, rhs, SPTRSV_COL_MAJOR, &secs))) return fail(rc);
     set_last_status(0);
     return secs;
 }

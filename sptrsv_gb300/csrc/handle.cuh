@@ -70,6 +70,10 @@ struct Handle {
     DevBuf roff;           // per-row first off-diagonal slot, padded by kRoffPad
     DevBuf sell, sell_perm, sell_len, sell_ptr;  // SELL-32-256 copy of the off-diagonals
     int sell_nslices = 0;
+    // supernode partition and its dense panels (supernodal.cu)
+    DevBuf sn_start, sn_m, sn_roff, sn_rect, sn_goff, sn_ld, sn_colbase, sn_outbase, sn_items, sn_G, sn_Ghi, sn_Glo;
+    int sn_count = 0, sn_nitems = 0;
+    bool have_supernodes = false;
     bool have_offdiag = false;
 
     // work
@@ -110,10 +114,13 @@ struct Handle {
     int build_cond_graph(const sptrsv_opts& o, const double* b, double* x, int rhs, int layout,
                          cudaGraphExec_t* out, int64_t* fixed_kernels);
     int resident_warps(const sptrsv_opts& o) const;
+    int set_supernodes(int sn, const int* snodes_host);
+    SnArgs sn_args() const;
     int solve(const sptrsv_opts* o, const double* b, double* x, int rhs, int layout);
     int sync();
 };
 
 void set_last_status(int s);
+int launch_sn_solve(const Handle& h, bool mixed, const void* b, void* x, int rhs, int64_t budget, int64_t* launches);
 
 }  // namespace sptrsv

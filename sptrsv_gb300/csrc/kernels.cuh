@@ -72,6 +72,19 @@ int launch_levelset(bool f32, const SolveArgs& a, int max_level, const int* lptr
 int launch_transpose(bool to_row_major, const double* src, double* dst, int n, int rhs, cudaStream_t st,
                      int64_t* launches);
 
+// supernodal.cu -- the panel work list and dense panels of a supernode partition
+struct SnArgs {
+    int nitems;
+    const int* item_s;     // supernode of every work item (ticket order: supernodes in reverse)
+    const int* item_p;     // 64-row panel of every work item
+    const int* sstart;     // supernode chunk boundaries
+    const int* mrect;      // rectangle width of every chunk
+    const int* roff;       // first rectangle column of every chunk in rect_cols
+    const int* rect_cols;  // rectangle column indices
+    const long long* goff; // first element of every chunk's G = [T^-1 | -T^-1 Rect] (row-major)
+    const int* ld;         // leading dimension of every chunk's G (w + m rounded up to 16)
+};
+
 // refine.cu
 struct RefineArgs {
     int n, nnz, rhs;
