@@ -53,6 +53,10 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=2_000_000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="irregular2m", choices=["irregular2m", "batch"],
+                    help="irregular2m: the 2M-row single solve (default); batch: the 512-system uneven mix")
+    ap.add_argument("--count", type=int, default=512, help="batch: number of systems")
+    ap.add_argument("--nmax", type=int, default=200_000, help="batch: largest n")
     return ap.parse_args()
 
 
@@ -205,9 +209,36 @@ def cpu_paths(m, b, budget_s=8.0):
             "paths": res, "best": best, "fn": serial if best.startswith("serial") else levelset}
 
 
+def run_reference_batch(args):
+    """The reference's serial solve over the batched mix: each step solves a bounded random
+    sample of the systems (about 10 s) and is projected to the whole mix by nnz x rhs."""
+    from sptrsv_gb300 import gen
+    M = gen.mix(count=args.count, seed=2, nmin=1000, nmax=args.nmax)
+    for k in range(args.warmup):
+        batch_cpu_sample(M, budget_s=2.0, seed=100 + k)
+    vals, t_all = [], time.perf_counter()
+    cb = None
+    for k in range(args.steps):
+        cb = batch_cpu_sample(M, budget_s=10.0, seed=k)
+        vals.append(cb["value"])
+    el = time.perf_counter() - t_all
+    v = float(len(vals) / np.sum(1.0 / np.array(vals)))  # harmonic mean of the projected rates
+    cb["value"] = v
+    line = {"metric": METRIC, "value": v, "unit": "solves/s", "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * args.count / v,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": BATCH_WORKLOAD.format(count=args.count, nmax=args.nmax), "systems": args.count},
+            "cpu_baseline": cb, "wall_s": el,
+            "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    M.close()
+
+
 def run_reference(args, dist):
     if dist.rank != 0:
         return
+    if args.workload == "batch":
+        return run_reference_batch(args)
     from sptrsv_gb300 import gen
     from oracle import oracle
     oracle.build()
@@ -414,12 +445,180 @@ def run_ours(args, dist):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------------------------------
+BATCH_WORKLOAD = ("batched uneven mix: {count} systems, n log-uniform in [1k, {nmax}], even ones 2D-Laplacian "
+                  "Cholesky factors (grid side round(sqrt n), full band), odd ones random diagonally dominant (the "
+                  "irregular generator, Poisson mean U[4,16]), RHS U{{1..16}} per system, b = U x*, seed 2")
+
+
+def batch_fp64_bytes(M):
+    """Algorithmic bytes of one FP64 pass over the whole mix (the per-system FP64 unit summed)."""
+    return int(np.sum(12 * M.nnz + 4 * (M.n.astype(np.int64) + 1) + 16 * M.n.astype(np.int64) * M.rhs))
+
+
+def batch_cpu_sample(M, budget_s=12.0, seed=0):
+    """Serial backward substitution (the reference's base_gauss_upper, else the oracle's
+    restatement) over a seeded random sample of the systems until budget_s; returns the
+    projected solves/s for the whole mix (count / (mean time per system * count))."""
+    from oracle import oracle
+    oracle.build()
+    R = oracle.ref()
+    order = np.random.default_rng(seed).permutation(M.count)
+    t_sum, done, work_done = 0.0, 0, 0.0
+    work = M.nnz.astype(np.float64) * M.rhs
+    t0 = time.perf_counter()
+    for s in order:
+        m, _, b = M.system(int(s))
+        r = int(M.rhs[s])
+        bcm = np.ascontiguousarray(np.asarray(b).reshape(m.n, r).T).reshape(-1)
+        x = np.zeros(m.n * r)
+        rpu = m.row_ptr.astype(np.uint64)
+        col = np.ascontiguousarray(m.col)
+        val = np.ascontiguousarray(m.val)
+        t1 = time.perf_counter()
+        if R is not None:
+            R.ref_base_gauss_upper(m.n, val, rpu, col, x, bcm, r)
+        else:
+            oracle.lib().orc_base_gauss_upper(m.n, val, rpu, col, x, bcm, r)
+        t_sum += time.perf_counter() - t1
+        work_done += work[s]
+        done += 1
+        if time.perf_counter() - t0 > budget_s and done >= 8:
+            break
+    # project by work (nnz x rhs): the sample's time per unit of work times the mix's work
+    est_total = t_sum / work_done * float(np.sum(work))
+    return {"value": M.count / est_total, "unit": "solves/s", "cores": 1,
+            "kind": "reference" if R is not None else "port",
+            "sample": f"serial base_gauss_upper on {done} randomly chosen systems of the mix ({t_sum:.1f} s), "
+                      f"projected to all {M.count} by nnz x rhs ({os.uname().machine} host)"}
+
+
+def run_batch(args, dist):
+    import ctypes
+    import sptrsv_gb300 as sp
+    from sptrsv_gb300 import gen
+    from sptrsv_gb300 import selector as sel
+    L = sp._lib.lib()
+    t_gen = time.time()
+    M = gen.mix(count=args.count, seed=2, nmin=1000, nmax=args.nmax)
+    t_gen = time.time() - t_gen
+    B = sp.Batch.from_mix(M, device=dist.local)
+    info = B.info()
+    # chosen schedules: the trained selector's picks when its weights are present, else the analysis default
+    wpath = os.path.join(ROOT, "sptrsv_gb300", "data", "selector_gb300.npz")
+    picked_by = "analysis default"
+    if os.path.exists(wpath):
+        mlp = sel.Mlp.load(wpath, device=dist.local)
+        B.schedule = sel.batch_schedule(B, mlp)
+        picked_by = "MLP selector"
+    sched = B.schedule
+    s = sp.Solver(dist.local)
+    h = s.handle
+    nb = 8 * int(info["x_elems"])
+    d_b, d_x = ctypes.c_void_p(), ctypes.c_void_p()
+    assert L.sptrsv_device_alloc(h, nb, ctypes.byref(d_b)) == 0
+    assert L.sptrsv_device_alloc(h, nb, ctypes.byref(d_x)) == 0
+    L.sptrsv_copy_h2d(h, d_b, M.b.ctypes.data, nb)
+    assert s.sync() == 0
+
+    def run(mode, steps):
+        ms, ks = [], []
+        for _ in range(steps):
+            B.timer_begin()
+            B.solve_device(d_b.value, d_x.value, mode)
+            ms.append(B.timer_end())
+            ks.append(B.sync())
+        return ms, ks
+
+    # correctness of both modes before timing
+    x = np.empty(int(info["x_elems"]))
+    worst = {}
+    for mode in ("plain", "chosen"):
+        run(mode, 1)
+        L.sptrsv_copy_d2h(h, x.ctypes.data, d_x, nb)
+        assert s.sync() == 0
+        worst[mode] = float(np.max(np.abs(x - M.xstar)))
+    st = B.stats()
+    if np.any(st["status"] != 0) or not np.all(st["rel"][sched != 0] <= RES_TOL):
+        raise SystemExit("batched chosen form missed the tolerance")
+    run("chosen", args.warmup)
+    clocks = Clocks(dist.local)
+    dist.barrier()
+    clocks.start()
+    ms, ks = run("chosen", args.steps)
+    ck = clocks.stop()
+    dist.barrier()
+    total_s = dist.max(sum(ms) / 1e3)
+    value = dist.ws * args.count * args.steps / total_s
+    run("plain", 1)
+    psteps = max(2, min(args.steps, 3))
+    pms, _ = run("plain", psteps)
+    plain_sps = args.count * psteps / (sum(pms) / 1e3)
+    # e2e: host b -> device, solve, x -> host, per step (pinned host buffers)
+    hb, hx = ctypes.c_void_p(), ctypes.c_void_p()
+    assert L.sptrsv_host_alloc(h, nb, ctypes.byref(hb)) == 0
+    assert L.sptrsv_host_alloc(h, nb, ctypes.byref(hx)) == 0
+    ctypes.memmove(hb, M.b.ctypes.data, nb)
+    e2e_ms = []
+    for k in range(args.warmup + args.steps):
+        B.timer_begin()
+        B.solve_host(hb.value, hx.value, "chosen")
+        t = B.timer_end()
+        B.sync()
+        if k >= args.warmup:
+            e2e_ms.append(t)
+    e2e_value = dist.ws * args.count * args.steps / dist.max(sum(e2e_ms) / 1e3)
+    cpu = None
+    if dist.rank == 0 and not args.no_cpu_baseline:
+        try:
+            cpu = batch_cpu_sample(M)
+        except Exception as e:
+            cpu = {"value": None, "unit": "solves/s", "error": str(e)[:200]}
+    L.sptrsv_host_free(h, hb)
+    L.sptrsv_host_free(h, hx)
+    L.sptrsv_device_free(h, d_b)
+    L.sptrsv_device_free(h, d_x)
+    if dist.rank != 0:
+        return
+    fb = batch_fp64_bytes(M)
+    peak, peak_src = measured_peak()
+    ms_step = 1e3 * total_s / args.steps
+    counts = {k: int(np.sum(sched == v)) for k, v in sp.BATCH_SCHED.items()}
+    line = {
+        "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": dist.ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+        "config": {"workload": BATCH_WORKLOAD.format(count=args.count, nmax=args.nmax), "systems": args.count,
+                   "rows": info["rows"], "nnz": info["nnz"], "rhs_columns": int(np.sum(M.rhs)),
+                   "schedules": counts, "picked_by": picked_by, "generation_s": t_gen,
+                   "l2": "no flush: the arena (%.1f GB) is far larger than L2" % (fb / 1e9),
+                   "parallelism": f"replicas x{dist.ws}"},
+        "solve_unit": "one system with all its right-hand sides",
+        "hbm_gbs": fb / (ms_step * 1e-3) / 1e9,
+        "plain_fp64_syncfree": {"solves_per_s": plain_sps, "ms_per_batch": 1e3 * args.count / plain_sps,
+                                "hbm_gbs": fb * plain_sps / args.count / 1e9},
+        "speedup_vs_plain": value / dist.ws / plain_sps,
+        "max_abs_err_vs_xstar": worst,
+        "refine_steps_max": int(np.max(st["steps"])), "rel_residual_max": float(np.max(st["rel"])),
+        "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": nb, "d2h_bytes_per_step": nb},
+        "roofline": {"bound": "hbm", "kernel": "whole batched solve", "achieved": fb / (ms_step * 1e-3) / 1e9,
+                     "peak": peak, "unit": "GB/s", "frac": fb / (ms_step * 1e-3) / 1e9 / peak,
+                     "peak_source": peak_src, "traffic": None, "algorithmic_bytes_per_launch": fb},
+        "gpu_launches": int(sum(ks)),
+        "clocks": ck,
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     dist = Dist()
     try:
         if args.impl == "reference":
             run_reference(args, dist)
+        elif args.workload == "batch":
+            run_batch(args, dist)
         else:
             run_ours(args, dist)
     finally:

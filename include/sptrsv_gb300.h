@@ -130,6 +130,27 @@ SPTRSV_API int sptrsv_analyse_device(sptrsv_handle h, int n, int nnz, const int*
  * picks that schedule.  SPTRSV_ERR_SUPERNODES when the matrix does not have the layout. */
 SPTRSV_API int sptrsv_set_supernodes(sptrsv_handle h, int sn, const int* supernodes);
 
+/* Autotuner: times every applicable candidate schedule (table indices 0 .. SPTRSV_TUNE_CANDIDATES-1,
+ * see sptrsv_candidate) on the resident matrix with a seeded random right-hand side of `rhs`
+ * columns (device buffers, CUDA events), each run capped at cap_ms after its first run and
+ * repeated `reps` times otherwise; writes every candidate's best time in ms (INFINITY when not
+ * applicable or failed) to cand_ms[SPTRSV_TUNE_CANDIDATES], the winner's index and options, and
+ * caches the winner for the RHS class (1, 2-8, 9-32, >32), where SPTRSV_SCHED_AUTO uses it. */
+#define SPTRSV_TUNE_CANDIDATES 16
+#define SPTRSV_FEATURES 24
+SPTRSV_API int sptrsv_autotune(sptrsv_handle h, int rhs, float cap_ms, int reps, float* cand_ms, int* best_id,
+                               sptrsv_opts* best);
+/* Options of candidate `id` of the autotuner's table. */
+SPTRSV_API int sptrsv_candidate(int id, sptrsv_opts* o);
+/* 1 when candidate `id` can run on the resident matrix with `rhs` columns. */
+SPTRSV_API int sptrsv_candidate_applicable(sptrsv_handle h, int id, int rhs);
+/* The SPTRSV_FEATURES features the learned selector reads: the resident matrix's (sizes
+ * log2-scaled, level-width and supernode-width histograms, row-length moments, dominance) and
+ * log2(rhs) last. */
+SPTRSV_API int sptrsv_features(sptrsv_handle h, int rhs, float* features);
+/* Cache a schedule for the RHS class of `rhs` (what the selector does with its pick). */
+SPTRSV_API int sptrsv_set_tuned(sptrsv_handle h, int rhs, const sptrsv_opts* o);
+
 /* Analysis results copied to host memory. */
 SPTRSV_API int sptrsv_info(sptrsv_handle h, int* n, int* nnz, int* max_level);
 SPTRSV_API int sptrsv_get_levels(sptrsv_handle h, uint64_t* levels);       /* core.cpp:244-270 values */
@@ -186,6 +207,74 @@ SPTRSV_API int sptrsv_profile_enable(sptrsv_handle h, int enable);
 /* After a profiled solve: per-step kinds (enum sptrsv_kernel_kind) and device times in ms, in
  * launch order; returns the number of steps written (at most cap).  Synchronises. */
 SPTRSV_API int sptrsv_profile_read(sptrsv_handle h, int* kinds, float* ms, int cap);
+
+/* ---------------------------------------------------------------------------------------
+ * Batched systems (no counterpart in the reference, which solves one system per call):
+ * `count` independent upper-triangular systems of uneven n and RHS count in one packed arena.
+ * Host input: n[s], rhs[s]; row_ptr = each system's local row pointer (n[s]+1 entries starting at
+ * 0) one after another; col (indices local to the system) and val likewise.  The same CSR rules
+ * as sptrsv_analyse_host apply per system.  Right-hand sides and solutions are row-major
+ * n[s] x rhs[s] per system, one system after another (sum n[s] rhs[s] doubles).
+ * Schedules per system: SPTRSV_BATCH_PLAIN (exact FP64 sync-free), _JACOBI (FP32 Jacobi inside
+ * the FP64 refinement), _PANEL (BF16x3 tensor-core dense 64-row panels inside the refinement;
+ * rows must form skyline or supernode chunks), _SF32 (FP32 sync-free inside the refinement).
+ * Mode 0 solves every system with the plain FP64 schedule in one persistent launch; mode 1
+ * solves each with its own schedule (set_schedule; the default comes from the analysis), the
+ * mixed ones until ||b - U x||_F <= tol ||b||_F per system. */
+typedef struct sptrsv_batch_s* sptrsv_batch;
+#define SPTRSV_BATCH_PLAIN 0
+#define SPTRSV_BATCH_JACOBI 1
+#define SPTRSV_BATCH_PANEL 2
+#define SPTRSV_BATCH_SF32 3
+SPTRSV_API int sptrsv_batch_create(sptrsv_batch* out, int device, int count, const int* n, const int* rhs,
+                                   const int64_t* row_ptr, const int* col, const double* val);
+SPTRSV_API int sptrsv_batch_destroy(sptrsv_batch b);
+SPTRSV_API int sptrsv_batch_get_schedule(sptrsv_batch b, int* sched);
+/* sched[s] = -1 keeps system s's schedule; PANEL on a system without panel structure returns
+ * SPTRSV_ERR_SUPERNODES, JACOBI on one without row dominance SPTRSV_ERR_UNSUPPORTED. */
+SPTRSV_API int sptrsv_batch_set_schedule(sptrsv_batch b, const int* sched);
+/* tol (default 1e-12), max refinement steps (20), inner change-test exponent (6), wait budget. */
+SPTRSV_API int sptrsv_batch_set_options(sptrsv_batch b, double tol, int max_refine, int inner_tol_exp,
+                                        int64_t spin_budget_ns);
+/* Device arena vectors; enqueued on the batch's stream (one CUDA graph launch). */
+SPTRSV_API int sptrsv_batch_solve(sptrsv_batch b, int mode, const double* d_b, double* d_x);
+/* Host vectors (pinned for overlap): host->device copy, solve, device->host copy, enqueued. */
+SPTRSV_API int sptrsv_batch_solve_host(sptrsv_batch b, int mode, const double* h_b, double* h_x);
+/* Waits; returns the first error; *kernels = kernel launches of the last solve. */
+SPTRSV_API int sptrsv_batch_sync(sptrsv_batch b, int64_t* kernels);
+/* Per system, of the last chosen-mode solve: status, refinement steps, relative residual, sweeps. */
+SPTRSV_API int sptrsv_batch_stats(sptrsv_batch b, int* status, int* steps, double* rel_res, int* sweeps);
+/* totals = {sum n, sum nnz, sum n*rhs, count}; ratio[s] = max row sum|off|/|diag|. */
+SPTRSV_API int sptrsv_batch_info(sptrsv_batch b, int64_t* totals, float* ratio);
+/* The selector's SPTRSV_FEATURES features of system s (with its own rhs). */
+SPTRSV_API int sptrsv_batch_features(sptrsv_batch b, int s, float* features);
+SPTRSV_API int sptrsv_batch_timer_begin(sptrsv_batch b);
+SPTRSV_API int sptrsv_batch_timer_end(sptrsv_batch b, float* ms);
+SPTRSV_API int64_t sptrsv_batch_launches(sptrsv_batch b);
+
+/* ---------------------------------------------------------------------------------------
+ * The learned schedule selector's network (no counterpart in the reference): an FP32 MLP
+ * in -> h1 -> h2 -> out with ReLU hidden layers that predicts each candidate schedule's log
+ * runtime from the matrix features (sptrsv_features).  Trained on the GPU by the library's own
+ * forward, backward and Adam kernels.  Parameters are one flat array: W1 (h1 x in, row-major),
+ * b1, W2 (h2 x h1), b2, W3 (out x h2), b3.  Inputs are standardised as (x - mean) * scale.
+ * Loss: sum mask (P - Y)^2 / sum mask over a batch (mask 0 = not measured).  All arrays are
+ * host, row-major, one sample per row. */
+typedef struct sptrsv_mlp_s* sptrsv_mlp;
+SPTRSV_API int sptrsv_mlp_create(sptrsv_mlp* out, int device, int in, int h1, int h2, int nout, uint64_t seed);
+SPTRSV_API int sptrsv_mlp_destroy(sptrsv_mlp m);
+SPTRSV_API int sptrsv_mlp_num_params(sptrsv_mlp m);
+SPTRSV_API int sptrsv_mlp_get_params(sptrsv_mlp m, float* params);
+SPTRSV_API int sptrsv_mlp_set_params(sptrsv_mlp m, const float* params);
+SPTRSV_API int sptrsv_mlp_set_norm(sptrsv_mlp m, const float* mean, const float* scale);
+/* Full-batch loss and gradient (no update). */
+SPTRSV_API int sptrsv_mlp_grad(sptrsv_mlp m, int n, const float* x, const float* y, const float* mask, float* grad,
+                               float* loss);
+/* Adam over `epochs` shuffled passes (mt19937_64(seed)) in mini-batches; loss_out[epochs]. */
+SPTRSV_API int sptrsv_mlp_train(sptrsv_mlp m, int n, const float* x, const float* y, const float* mask, int epochs,
+                                int batch, float lr, uint64_t seed, float* loss_out);
+SPTRSV_API int sptrsv_mlp_predict(sptrsv_mlp m, int n, const float* x, float* y);
+SPTRSV_API int64_t sptrsv_mlp_launches(sptrsv_mlp m);
 
 #ifdef __cplusplus
 }

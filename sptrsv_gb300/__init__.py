@@ -60,6 +60,17 @@ def make_opts(schedule="auto", precision="fp64", rows_per_warp=None, rhs_tile=No
     return o
 
 
+N_CANDIDATES = 16
+N_FEATURES = 24
+
+
+def candidate(cand_id):
+    """sptrsv_opts of entry `cand_id` of the autotuner's candidate table."""
+    o = Opts()
+    _check(_lib.lib().sptrsv_candidate(int(cand_id), ctypes.byref(o)), "candidate")
+    return o
+
+
 def _c(a, dt):
     return np.ascontiguousarray(a, dtype=dt)
 
@@ -184,6 +195,26 @@ class Solver:
         _check(_lib.lib().sptrsv_set_supernodes(self._h, len(sn) - 1, sn), "set_supernodes")
         return self
 
+    def autotune(self, rhs=1, cap_ms=50.0, reps=2):
+        """Exhaustive tuning over the candidate table; returns (best id, times in ms per candidate).
+        The winner is cached for this RHS class and used by schedule="auto"."""
+        ms = np.zeros(N_CANDIDATES, dtype=np.float32)
+        best = ctypes.c_int(-1)
+        _check(_lib.lib().sptrsv_autotune(self._h, rhs, cap_ms, reps, ms, ctypes.byref(best), None), "autotune")
+        return best.value, ms
+
+    def features(self, rhs=1):
+        f = np.zeros(N_FEATURES, dtype=np.float32)
+        _check(_lib.lib().sptrsv_features(self._h, int(rhs), f), "features")
+        return f
+
+    def applicable(self, cand_id, rhs=1):
+        return bool(_lib.lib().sptrsv_candidate_applicable(self._h, cand_id, rhs))
+
+    def set_tuned(self, cand_id, rhs=1):
+        o = candidate(cand_id)
+        _check(_lib.lib().sptrsv_set_tuned(self._h, rhs, ctypes.byref(o)), "set_tuned")
+
     def info(self):
         n, nnz, ml = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
         _check(_lib.lib().sptrsv_info(self._h, ctypes.byref(n), ctypes.byref(nnz), ctypes.byref(ml)), "info")
@@ -258,3 +289,124 @@ class Solver:
             raise SptrsvError(k, "profile_read")
         return list(zip(kinds[:k].tolist(), ms[:k].tolist()))
 
+
+
+BATCH_SCHED = {"plain": 0, "jacobi": 1, "panel": 2, "sf32": 3}
+BATCH_MODE = {"plain": 0, "chosen": 1}
+
+
+class Batch:
+    """Independent systems of uneven n and RHS count solved together (sptrsv_batch_* in
+    include/sptrsv_gb300.h).  Inputs are the packed host arena: per-system n and rhs, the local
+    row pointers one after another (int64), columns and values one after another.  Right-hand
+    sides and solutions are row-major n x rhs per system, concatenated.
+
+    mode "plain": every system by the exact FP64 sync-free pull in one persistent launch;
+    mode "chosen": each system by its own schedule (``schedule``), the mixed ones inside the FP64
+    refinement to ||b - U x||_F <= tol ||b||_F."""
+
+    def __init__(self, n, rhs, row_ptr, col, val, device=0):
+        self._h = None
+        self.n = np.ascontiguousarray(n, dtype=np.int32)
+        self.rhs = np.ascontiguousarray(rhs, dtype=np.int32)
+        self.count = len(self.n)
+        self.xb_off = np.concatenate([[0], np.cumsum(self.n.astype(np.int64) * self.rhs)]).astype(np.int64)
+        h = ctypes.c_void_p()
+        _check(_lib.lib().sptrsv_batch_create(ctypes.byref(h), int(device), self.count, self.n, self.rhs,
+                                              np.ascontiguousarray(row_ptr, dtype=np.int64),
+                                              np.ascontiguousarray(col, dtype=np.int32),
+                                              np.ascontiguousarray(val, dtype=np.float64)), "batch_create")
+        self._h = h
+
+    @classmethod
+    def from_mix(cls, mix, device=0):
+        return cls(mix.n, mix.rhs, mix.row_ptr, mix.col, mix.val, device)
+
+    def close(self):
+        if self._h:
+            _lib.lib().sptrsv_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def schedule(self):
+        out = np.zeros(self.count, dtype=np.int32)
+        _check(_lib.lib().sptrsv_batch_get_schedule(self._h, out), "batch_get_schedule")
+        return out
+
+    @schedule.setter
+    def schedule(self, sched):
+        a = np.array([BATCH_SCHED[v] if isinstance(v, str) else int(v) for v in sched], dtype=np.int32)
+        _check(_lib.lib().sptrsv_batch_set_schedule(self._h, a), "batch_set_schedule")
+
+    def set_options(self, tol=0.0, max_refine=0, inner_tol_exp=0, spin_budget_ns=0):
+        _check(_lib.lib().sptrsv_batch_set_options(self._h, float(tol), int(max_refine), int(inner_tol_exp),
+                                                   int(spin_budget_ns)), "batch_set_options")
+
+    def info(self):
+        t = np.zeros(4, dtype=np.int64)
+        r = np.zeros(self.count, dtype=np.float32)
+        _check(_lib.lib().sptrsv_batch_info(self._h, t, r), "batch_info")
+        return {"rows": int(t[0]), "nnz": int(t[1]), "x_elems": int(t[2]), "count": int(t[3]), "ratio": r}
+
+    def solve(self, b, mode="chosen"):
+        """Host b (all systems) -> host x, through the host-buffer entry point."""
+        b = np.ascontiguousarray(b, dtype=np.float64).reshape(-1)
+        if b.size != self.xb_off[-1]:
+            raise ValueError("b must hold sum n*rhs values")
+        x = np.empty_like(b)
+        self.solve_host(b.ctypes.data, x.ctypes.data, mode)
+        self.sync()
+        return x
+
+    def solve_host(self, h_b, h_x, mode="chosen"):
+        _check(_lib.lib().sptrsv_batch_solve_host(self._h, BATCH_MODE.get(mode, mode), ctypes.c_void_p(h_b),
+                                                  ctypes.c_void_p(h_x)), "batch_solve_host")
+
+    def solve_device(self, d_b, d_x, mode="chosen"):
+        _check(_lib.lib().sptrsv_batch_solve(self._h, BATCH_MODE.get(mode, mode), ctypes.c_void_p(d_b),
+                                             ctypes.c_void_p(d_x)), "batch_solve")
+
+    def sync(self):
+        k = ctypes.c_int64()
+        _check(_lib.lib().sptrsv_batch_sync(self._h, ctypes.byref(k)), "batch_sync")
+        return k.value
+
+    def stats(self):
+        st = np.zeros(self.count, dtype=np.int32)
+        steps = np.zeros(self.count, dtype=np.int32)
+        rel = np.zeros(self.count, dtype=np.float64)
+        sw = np.zeros(self.count, dtype=np.int32)
+        _check(_lib.lib().sptrsv_batch_stats(self._h, st, steps, rel, sw), "batch_stats")
+        return {"status": st, "steps": steps, "rel": rel, "sweeps": sw}
+
+    def features(self, s):
+        f = np.zeros(N_FEATURES, dtype=np.float32)
+        _check(_lib.lib().sptrsv_batch_features(self._h, int(s), f), "batch_features")
+        return f
+
+    def timer_begin(self):
+        _check(_lib.lib().sptrsv_batch_timer_begin(self._h), "batch_timer")
+
+    def timer_end(self):
+        ms = ctypes.c_float()
+        _check(_lib.lib().sptrsv_batch_timer_end(self._h, ctypes.byref(ms)), "batch_timer")
+        return ms.value
+
+    def launches(self):
+        return int(_lib.lib().sptrsv_batch_launches(self._h))
+
+    def split(self, x):
+        """Per-system views (n x rhs) of a concatenated solution."""
+        return [x[self.xb_off[s]:self.xb_off[s + 1]].reshape(int(self.n[s]), int(self.rhs[s])) for s in range(self.count)]

@@ -17,6 +17,7 @@ f64 = _P(dtype=np.float64, flags="C_CONTIGUOUS")
 i64 = _P(dtype=np.int64, flags="C_CONTIGUOUS")
 u64 = _P(dtype=np.uint64, flags="C_CONTIGUOUS")
 i32 = _P(dtype=np.int32, flags="C_CONTIGUOUS")
+f32 = _P(dtype=np.float32, flags="C_CONTIGUOUS")
 c_int, c_dbl, c_sz, c_i64, c_vp = ctypes.c_int, ctypes.c_double, ctypes.c_size_t, ctypes.c_int64, ctypes.c_void_p
 
 
@@ -74,6 +75,12 @@ C_API = {
     "sptrsv_analyse_host": ([c_vp, c_int, c_i64, i64, i32, f64], c_int),
     "sptrsv_analyse_device": ([c_vp, c_int, c_int, c_vp, c_vp, c_vp], c_int),
     "sptrsv_set_supernodes": ([c_vp, c_int, i32], c_int),
+    "sptrsv_autotune": ([c_vp, c_int, ctypes.c_float, c_int, _P(dtype=np.float32, flags="C_CONTIGUOUS"), _c_int_p,
+                         ctypes.POINTER(Opts)], c_int),
+    "sptrsv_candidate": ([c_int, ctypes.POINTER(Opts)], c_int),
+    "sptrsv_candidate_applicable": ([c_vp, c_int, c_int], c_int),
+    "sptrsv_features": ([c_vp, c_int, _P(dtype=np.float32, flags="C_CONTIGUOUS")], c_int),
+    "sptrsv_set_tuned": ([c_vp, c_int, ctypes.POINTER(Opts)], c_int),
     "sptrsv_info": ([c_vp, _c_int_p, _c_int_p, _c_int_p], c_int),
     "sptrsv_get_levels": ([c_vp, u64], c_int),
     "sptrsv_get_in_degree": ([c_vp, i32], c_int),
@@ -97,6 +104,30 @@ C_API = {
     "sptrsv_solve_noalloc": ([c_int, c_int, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp], c_int),
     "sptrsv_profile_enable": ([c_vp, c_int], c_int),
     "sptrsv_profile_read": ([c_vp, i32, _P(dtype=np.float32, flags="C_CONTIGUOUS"), c_int], c_int),
+    "sptrsv_batch_create": ([ctypes.POINTER(c_vp), c_int, c_int, i32, i32, i64, i32, f64], c_int),
+    "sptrsv_batch_destroy": ([c_vp], c_int),
+    "sptrsv_batch_get_schedule": ([c_vp, i32], c_int),
+    "sptrsv_batch_set_schedule": ([c_vp, i32], c_int),
+    "sptrsv_batch_set_options": ([c_vp, c_dbl, c_int, c_int, c_i64], c_int),
+    "sptrsv_batch_solve": ([c_vp, c_int, c_vp, c_vp], c_int),
+    "sptrsv_batch_solve_host": ([c_vp, c_int, c_vp, c_vp], c_int),
+    "sptrsv_batch_sync": ([c_vp, ctypes.POINTER(c_i64)], c_int),
+    "sptrsv_batch_stats": ([c_vp, i32, i32, f64, i32], c_int),
+    "sptrsv_batch_info": ([c_vp, i64, _P(dtype=np.float32, flags="C_CONTIGUOUS")], c_int),
+    "sptrsv_batch_features": ([c_vp, c_int, _P(dtype=np.float32, flags="C_CONTIGUOUS")], c_int),
+    "sptrsv_batch_timer_begin": ([c_vp], c_int),
+    "sptrsv_batch_timer_end": ([c_vp, ctypes.POINTER(ctypes.c_float)], c_int),
+    "sptrsv_batch_launches": ([c_vp], c_i64),
+    "sptrsv_mlp_create": ([ctypes.POINTER(c_vp), c_int, c_int, c_int, c_int, c_int, ctypes.c_uint64], c_int),
+    "sptrsv_mlp_destroy": ([c_vp], c_int),
+    "sptrsv_mlp_num_params": ([c_vp], c_int),
+    "sptrsv_mlp_get_params": ([c_vp, f32], c_int),
+    "sptrsv_mlp_set_params": ([c_vp, f32], c_int),
+    "sptrsv_mlp_set_norm": ([c_vp, f32, f32], c_int),
+    "sptrsv_mlp_grad": ([c_vp, c_int, f32, f32, f32, f32, f32], c_int),
+    "sptrsv_mlp_train": ([c_vp, c_int, f32, f32, f32, c_int, c_int, ctypes.c_float, ctypes.c_uint64, f32], c_int),
+    "sptrsv_mlp_predict": ([c_vp, c_int, f32, f32], c_int),
+    "sptrsv_mlp_launches": ([c_vp], c_i64),
 }
 
 GEN_API = {
@@ -111,6 +142,9 @@ GEN_API = {
     "sptrsv_gen_supernodal_random": ([c_int, c_int, c_int, c_dbl, c_dbl, c_int, ctypes.c_uint64,
                                       ctypes.POINTER(ctypes.POINTER(c_int)), ctypes.POINTER(c_int)], c_vp),
     "sptrsv_gen_free_ints": ([c_vp], None),
+    "sptrsv_gen_mix": ([c_int, ctypes.c_uint64, c_int, c_int, c_dbl, c_dbl, c_int, c_int], c_vp),
+    "sptrsv_gen_mix_array": ([c_vp, c_int, ctypes.POINTER(c_vp), ctypes.POINTER(c_i64)], c_int),
+    "sptrsv_gen_mix_free": ([c_vp], None),
 }
 
 _lib = None

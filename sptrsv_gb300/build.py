@@ -62,7 +62,7 @@ def build(verbose=False, force=False):
             raise RuntimeError("link failed")
     gsrc = os.path.join(CSRC, "gen.cpp")
     if force or not os.path.exists(GEN) or os.path.getmtime(GEN) < os.path.getmtime(gsrc):
-        cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-o", GEN, gsrc]
+        cmd = ["g++", "-O3", "-ffp-contract=off", "-std=c++17", "-fPIC", "-shared", "-pthread", "-o", GEN, gsrc]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode:
             print(" ".join(cmd), r.stdout, r.stderr)

@@ -84,6 +84,7 @@ void Handle::drop_matrix() {
     have_csc = false;
     have_offdiag = false;
     have_supernodes = false;
+    for (bool& v : tuned_valid) v = false;
     n = nnz = max_level = 0;
     rp = col = nullptr;
     val = nullptr;
@@ -196,6 +197,15 @@ sptrsv_opts Handle::resolve(const sptrsv_opts* o, int rhs) const {
     sptrsv_opts r;
     sptrsv_default_opts(&r);
     if (o) r = *o;
+    // a schedule chosen by the autotuner or the learned selector for this RHS class replaces AUTO
+    // (schedule and precision: every candidate meets the accuracy contract)
+    if (r.schedule == SPTRSV_SCHED_AUTO && tuned_valid[rhs_class(rhs)]) {
+        const sptrsv_opts t = tuned[rhs_class(rhs)];
+        r.schedule = t.schedule;
+        r.precision = t.precision;
+        r.rows_per_warp = t.rows_per_warp;
+        r.inner_tol_exp = t.inner_tol_exp;
+    }
     if (r.spin_budget_ns <= 0) r.spin_budget_ns = kDefaultBudgetNs;
     if (r.tol <= 0) r.tol = 1e-12;
     if (r.max_refine <= 0) r.max_refine = 8;
@@ -708,7 +718,7 @@ Handle::~Handle() {
                       &level_rows, &stats, &csc_ptr, &csc_row, &csc_val, &scratch, &xw, &bw, &r32, &d32a, &d32b,
                       &norms, &indeg_work, &left, &db, &dx, &flush, &offdiag, &roff, &sell, &sell_perm, &sell_len, &sell_ptr,
                       &sn_start, &sn_m, &sn_roff, &sn_rect, &sn_goff, &sn_ld, &sn_colbase, &sn_outbase, &sn_items,
-                      &sn_G, &sn_Ghi, &sn_Glo};
+                      &sn_G, &sn_Ghi, &sn_Glo, &tune_b, &tune_x};
     for (DevBuf* b : bufs) b->release();
     if (ctl) cudaFree(ctl);
     if (ev0) cudaEventDestroy(ev0);

@@ -1,0 +1,1380 @@
+// batch.cu -- many independent upper-triangular systems of uneven size and RHS count solved
+// together from one packed device arena.
+//
+// Arena: the systems' CSR matrices one after another (each with its own local int32 row
+// pointer, column indices local to the system), FP32 copies of the values, the inverse
+// diagonals, and per-system descriptors (BSys) with the offsets of every part.  Right-hand sides
+// and solutions are row-major n x rhs per system, one system after another.
+//
+// Two solve modes, each one CUDA graph:
+//   * plain: every system by the FP64 sync-free pull (warp per row, RHS columns across lanes)
+//     in ONE persistent launch over a device work queue that interleaves the systems row by row
+//     from their last rows (queue position t holds row n_s - 1 - t of every system still that
+//     long), so all systems advance together and the longest chain sets the makespan;
+//   * chosen: every system by its own schedule (BS_*), the mixed ones inside one device-driven
+//     FP64 iterative refinement (conditional WHILE nodes): per step an FP32 inner solve (Jacobi
+//     sweeps to a relative change test, BF16x3 tensor-core products over dense panels, or the
+//     FP32 sync-free pull), x += d in FP64 and the FP64 residual r = b - U x, until every
+//     system's ||r||_F / ||b||_F <= tol.  Converged systems drop out of the later steps.
+//     Systems scheduled BS_PLAIN are solved exactly in FP64 first, by the same persistent pull.
+//
+// Every wait is a bounded pending-sentinel poll (common.cuh); per-system reductions are flushed
+// once per run of rows of one system, so no address sees one atomic per row.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+#include <cuda_bf16.h>
+#include "common.cuh"
+#include "kernels.cuh"
+#include "handle.cuh"
+#include "mma.cuh"
+
+namespace sptrsv {
+
+enum { BS_PLAIN = 0, BS_JACOBI = 1, BS_PANEL = 2, BS_SF32 = 3, BS_COUNT = 4 };
+
+constexpr int kBPanel = 64;     // rows per panel work item (4 warps x 16-row MMA tiles)
+constexpr int kBKc = 128;       // K rows staged per chunk
+constexpr int kBNc = 32;        // right-hand-side columns per pass
+constexpr int kBRowChunk = 32;  // rows per warp task in the row kernels
+
+struct BSys {
+    int n, rhs, sched, pad;
+    long long rp0, nz0, row0, xb0;
+};
+
+struct BState {
+    double bnorm2, rnorm2, rel;
+    int done;  // 0 refining, 1 converged, 2 gave up
+    int steps, status;
+    int inner_done, inner_count, final_idx;
+    unsigned dmax_bits, dchg_bits;
+    unsigned ratio_bits;  // analysis: max_i sum|off| / |diag| (float bits)
+    int sweeps;           // Jacobi sweeps over the whole solve
+    int gapped;           // analysis: some row is not one contiguous column range from its diagonal
+    int pad;
+};
+
+struct BCtl {
+    Ctl c;
+    int active;      // mixed systems still refining
+    int jac_active;  // Jacobi systems still sweeping in this step
+    int sweep_k;     // sweep index inside the current inner solve
+    int outer;       // refinement steps taken
+    int total_sweeps;
+    int nmixed;
+};
+
+struct BChunk {
+    int sys, a, w, m, ld, pad;
+    const __nv_bfloat16* ghi;
+    const __nv_bfloat16* glo;
+    const int* rect;
+};
+
+// A list of systems with the prefix of their row (or element) counts.
+struct SegList {
+    const int* sys;
+    const long long* off;  // nseg + 1 entries
+    int nseg;
+    long long total;
+};
+
+struct BArgs {
+    const BSys* sys;
+    BState* st;
+    BCtl* bc;
+    const int* rp;
+    const int* col;
+    const double* val;
+    const float* val32;
+    double* invd;
+    float* invd32;
+    const double* b;
+    double* x;
+    float* r32;
+    float* d0;
+    float* d1;
+    int64_t budget;
+    double tol;
+    float inner_eps;
+    int max_refine, max_sweeps;
+};
+
+__device__ __forceinline__ int seg_find(const SegList& L, long long q) {
+    int lo = 0, hi = L.nseg - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (L.off[mid] <= q) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Lanes of a warp on one row: nc RHS columns side by side, `groups` (a power of two) strided
+// walks over the row's entries; lane = g * nc + c.
+__device__ __forceinline__ void lane_split(int nc, int& groups, int& g, int& c) {
+    int gr = 32 / nc;
+    gr = 1 << (31 - __clz(gr));
+    groups = gr;
+    const int lane = threadIdx.x & 31;
+    g = lane / nc;
+    c = lane - g * nc;
+}
+
+template <typename T>
+__device__ __forceinline__ T group_sum(T v, int groups, int nc) {
+    for (int off = groups >> 1; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off * nc);
+    return v;
+}
+
+__device__ __forceinline__ float warp_max(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// Warp-wide iteration over a row list in tasks of kBRowChunk consecutive rows; f(seg, sys, i)
+// per row, flush(sys) whenever the system changes and at the end of each task.
+template <typename F, typename Flush>
+__device__ __forceinline__ void for_rows(const SegList& rows, F f, Flush flush) {
+    const long long gw = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+    const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long t = gw; t * kBRowChunk < rows.total; t += nw) {
+        const long long q0 = t * kBRowChunk, q1 = min(rows.total, q0 + kBRowChunk);
+        int seg = seg_find(rows, q0);
+        int cur = rows.sys[seg];
+        for (long long q = q0; q < q1; ++q) {
+            while (q >= rows.off[seg + 1]) ++seg;
+            const int s = rows.sys[seg];
+            if (s != cur) { flush(cur); cur = s; }
+            f(s, (int)(q - rows.off[seg]));
+        }
+        flush(cur);
+    }
+}
+
+// --- analysis ----------------------------------------------------------------------------------
+
+// Warp per row of every system: diagonal first and nonzero, off-diagonals strictly right of it
+// and inside the system; inverse diagonals (FP64, FP32); per-system max row ratio.
+__global__ void __launch_bounds__(256) k_b_setup(BArgs A, SegList rows) {
+    const int lane = threadIdx.x & 31;
+    float rmax = 0.f;
+    for_rows(
+        rows,
+        [&](int s, int i) {
+            const BSys S = A.sys[s];
+            const int* rp = A.rp + S.rp0;
+            const int beg = rp[i], end = rp[i + 1];
+            const int* cl = A.col + S.nz0;
+            const double* vl = A.val + S.nz0;
+            int bad = end <= beg ? SPTRSV_ERR_MISSING_DIAG : 0;
+            double off = 0.0;
+            int gap = 0;
+            if (!bad) {
+                for (int k = beg + 1 + lane; k < end; k += 32) {
+                    const int j = cl[k];
+                    if (j <= i) bad = SPTRSV_ERR_NOT_UPPER;
+                    else if (j >= S.n) bad = SPTRSV_ERR_COL_RANGE;
+                    gap |= j != i + (k - beg);
+                    off += fabs(vl[k]);
+                }
+            }
+            bad = __reduce_min_sync(0xffffffffu, bad);  // statuses are negative: min = any error
+            gap = __reduce_or_sync(0xffffffffu, gap);
+            off = warp_sum(off);
+            if (gap && lane == 0 && !A.st[s].gapped) A.st[s].gapped = 1;
+            if (!bad) {
+                if (cl[beg] != i) bad = SPTRSV_ERR_MISSING_DIAG;
+                else if (vl[beg] == 0.0) bad = SPTRSV_ERR_ZERO_PIVOT;
+            }
+            if (bad) {
+                if (lane == 0) {
+                    atomicCAS(&A.st[s].status, 0, bad);
+                    atomicCAS(&A.bc->c.status, 0, bad);
+                }
+                return;
+            }
+            const double d = vl[beg];
+            if (lane == 0) {
+                A.invd[S.row0 + i] = 1.0 / d;
+                A.invd32[S.row0 + i] = (float)(1.0 / d);
+            }
+            rmax = fmaxf(rmax, (float)(off / fabs(d)));
+        },
+        [&](int s) {
+            if (lane == 0 && rmax > 0.f) atomicMax(&A.st[s].ratio_bits, __float_as_uint(rmax));
+            rmax = 0.f;
+        });
+}
+
+// --- element kernels ---------------------------------------------------------------------------
+
+// x := pending sentinel over a list of systems' solution elements (all of them, or only the
+// systems still refining when `only_active`).
+template <typename T>
+__global__ void k_b_fill_pending(BArgs A, SegList el, T* x, bool only_active) {
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < el.total;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int seg = seg_find(el, e);
+        const int s = el.sys[seg];
+        if (only_active && A.st[s].done) continue;
+        x[A.sys[s].xb0 + (e - el.off[seg])] = Pend<T>::value();
+    }
+}
+
+// Mixed systems: x = 0, r = b (in FP32: the first inner right-hand side), ||b||^2 per system.
+__global__ void k_b_init_mixed(BArgs A, SegList el) {
+    const int lane = threadIdx.x & 31;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const long long base0 = blockIdx.x * (long long)blockDim.x + (threadIdx.x & ~31);
+    for (long long wb = base0; wb < el.total; wb += stride) {  // warp-uniform trip count
+        const long long e = wb + lane;
+        int s = -1;
+        double v = 0.0;
+        if (e < el.total) {
+            const int seg = seg_find(el, e);
+            s = el.sys[seg];
+            const long long o = A.sys[s].xb0 + (e - el.off[seg]);
+            const double bv = A.b[o];
+            A.x[o] = 0.0;
+            A.r32[o] = (float)bv;
+            v = bv * bv;
+        }
+        const int s0 = __shfl_sync(0xffffffffu, s, 0);
+        if (__all_sync(0xffffffffu, s == s0)) {
+            v = warp_sum(v);
+            if (lane == 0 && s0 >= 0) atomicAdd(&A.st[s0].bnorm2, v);
+        } else if (s >= 0) {
+            atomicAdd(&A.st[s].bnorm2, v);
+        }
+    }
+}
+
+// x += d (the correction buffer that finished the system's inner solve), systems still refining.
+__global__ void k_b_axpy(BArgs A, SegList el) {
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < el.total;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int seg = seg_find(el, e);
+        const int s = el.sys[seg];
+        const BState& S = A.st[s];
+        if (S.done) continue;
+        const long long o = A.sys[s].xb0 + (e - el.off[seg]);
+        const float d = (S.final_idx ? A.d1 : A.d0)[o];
+        A.x[o] += (double)d;
+    }
+}
+
+// --- FP64 / FP32 sync-free pull (persistent, ticketed work queue) -------------------------------
+
+// Warp per row taken from `order` by ticket; the row waits on its solved columns (pending-sentinel
+// polls), sums in its lane groups, and publishes x_i = (b_i - sum) * invd_i.  Rows of one system
+// appear in the queue after every row they depend on, so the ticket order alone guarantees
+// progress.
+template <typename T>
+__global__ void __launch_bounds__(256) k_b_pull(BArgs A, const int2* __restrict__ order, unsigned count,
+                                                const T* __restrict__ bsrc, T* xdst, const T* __restrict__ vals,
+                                                const T* __restrict__ invd, int which_ticket, bool skip_done) {
+    Ctl* ctl = &A.bc->c;
+    unsigned* ticket = which_ticket ? &ctl->ticket2 : &ctl->ticket;
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        unsigned t = 0;
+        if (lane == 0) t = aborted(ctl) ? 0xFFFFFFFFu : atomicAdd(ticket, 1u);
+        t = __shfl_sync(0xffffffffu, t, 0);
+        if (t >= count) break;
+        const int2 it = order[t];
+        if (skip_done && A.st[it.x].done) continue;
+        const BSys S = A.sys[it.x];
+        const int i = it.y, r = S.rhs;
+        const int* rp = A.rp + S.rp0;
+        const int beg = __ldg(rp + i), end = __ldg(rp + i + 1);
+        const int* cl = A.col + S.nz0;
+        const T* vl = vals + S.nz0;
+        const T* bb = bsrc + S.xb0;
+        T* xx = xdst + S.xb0;
+        const T dinv = invd[S.row0 + i];
+        bool ok = true;
+        for (int c0 = 0; c0 < r; c0 += 32) {
+            const int nc = min(32, r - c0);
+            int groups, g, c;
+            lane_split(nc, groups, g, c);
+            T sum = 0;
+            bool lok = true;
+            if (g < groups) {
+                for (int k = beg + 1 + g; k < end; k += groups) {
+                    T xv;
+                    if (!wait_ready<T>(xx + (size_t)__ldg(cl + k) * r + c0 + c, xv, ctl, A.budget)) {
+                        lok = false;
+                        break;
+                    }
+                    sum = fma(__ldg(vl + k), xv, sum);
+                }
+            }
+            sum = group_sum(sum, groups, nc);
+            if (__any_sync(0xffffffffu, !lok)) { ok = false; break; }
+            if (lane < nc) {
+                const size_t o = (size_t)i * r + c0 + lane;
+                st_relaxed(xx + o, Pend<T>::fix((bb[o] - sum) * dinv));
+            }
+        }
+        if (!ok) break;
+    }
+}
+
+// --- BF16x3 panel products (persistent) -------------------------------------------------------
+
+// One 64-row panel of a dense chunk G = [T^-1 | -T^-1 Rect] per work item: d[rows] = G [r ; d_R].
+// K chunks are taken farthest-first, so the columns solved last (the nearest rows) are waited on
+// last.  Items of converged systems are skipped (nobody waits on them: only the same system's
+// panels read its rows).
+__global__ void __launch_bounds__(128) k_b_panels(BArgs A, const int2* __restrict__ items, unsigned nitems,
+                                                  const BChunk* __restrict__ chunks) {
+    __shared__ __align__(16) __nv_bfloat16 Vhi[kBNc][kBKc + 8];
+    __shared__ __align__(16) __nv_bfloat16 Vlo[kBNc][kBKc + 8];
+    __shared__ unsigned s_t;
+    __shared__ int s_ok;
+    Ctl* ctl = &A.bc->c;
+    const int lane = threadIdx.x & 31, wv = threadIdx.x >> 5;
+    for (;;) {
+        if (threadIdx.x == 0) s_t = aborted(ctl) ? 0xFFFFFFFFu : atomicAdd(&ctl->ticket, 1u);
+        __syncthreads();
+        const unsigned t = s_t;
+        __syncthreads();
+        if (t >= nitems) break;
+        const int2 it = items[t];
+        const BChunk C = chunks[it.x];
+        if (A.st[C.sys].done) continue;
+        const BSys S = A.sys[C.sys];
+        const int a = C.a, w = C.w, K = C.w + C.m, L = C.ld, rhs = S.rhs;
+        const float* b = A.r32 + S.xb0;
+        float* x = A.d0 + S.xb0;
+        const int row0 = it.y * kBPanel + 16 * wv;  // this warp's 16-row tile
+        bool ok = true;
+        for (int c0 = 0; c0 < rhs; c0 += kBNc) {
+            const int nc = min(kBNc, rhs - c0);
+            const int nc8 = (nc + 7) & ~7;
+            float acc[kBNc / 8][4];
+#pragma unroll
+            for (int q = 0; q < kBNc / 8; ++q) acc[q][0] = acc[q][1] = acc[q][2] = acc[q][3] = 0.f;
+            const int nk = (K + kBKc - 1) / kBKc;
+            for (int kb = nk - 1; kb >= 0; --kb) {
+                const int k0 = kb * kBKc, kc = min(kBKc, K - k0);
+                if (threadIdx.x == 0) s_ok = 1;
+                __syncthreads();
+                for (int e = threadIdx.x; e < kBKc * nc8; e += blockDim.x) {
+                    const int j = e / kBKc, kk = e - j * kBKc, k = k0 + kk;
+                    float v = 0.f;
+                    if (kk < kc && j < nc) {
+                        if (k < w) {
+                            v = b[(size_t)(a + k) * rhs + c0 + j];
+                        } else if (!wait_ready<float>(x + (size_t)C.rect[k - w] * rhs + c0 + j, v, ctl, A.budget)) {
+                            s_ok = 0;
+                            v = 0.f;
+                        }
+                    }
+                    const __nv_bfloat16 h = __float2bfloat16_rn(v);
+                    Vhi[j][kk] = h;
+                    Vlo[j][kk] = __float2bfloat16_rn(v - __bfloat162float(h));
+                }
+                __syncthreads();
+                if (!s_ok) { ok = false; break; }
+                if (row0 < w) {
+                    for (int ks = 0; ks < kc; ks += 16) {
+                        uint32_t ah[4], al[4];
+                        load_a(C.ghi, L, row0, w, k0 + ks, ah);
+                        load_a(C.glo, L, row0, w, k0 + ks, al);
+                        const int kb2 = ks + (lane & 3) * 2;
+#pragma unroll
+                        for (int q = 0; q < kBNc / 8; ++q) {
+                            if (q * 8 >= nc) break;
+                            const int nn = q * 8 + (lane >> 2);
+                            const uint32_t bh0 = *reinterpret_cast<const uint32_t*>(&Vhi[nn][kb2]);
+                            const uint32_t bh1 = *reinterpret_cast<const uint32_t*>(&Vhi[nn][kb2 + 8]);
+                            const uint32_t bl0 = *reinterpret_cast<const uint32_t*>(&Vlo[nn][kb2]);
+                            const uint32_t bl1 = *reinterpret_cast<const uint32_t*>(&Vlo[nn][kb2 + 8]);
+                            mma_bf16(acc[q], ah, bh0, bh1);
+                            mma_bf16(acc[q], ah, bl0, bl1);
+                            mma_bf16(acc[q], al, bh0, bh1);
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+            if (!ok) break;
+            if (row0 < w) {
+                const int ra = row0 + (lane >> 2), rb = ra + 8;
+#pragma unroll
+                for (int q = 0; q < kBNc / 8; ++q) {
+                    const int cj = q * 8 + (lane & 3) * 2;
+                    if (ra < w && cj < nc) st_relaxed(x + (size_t)(a + ra) * rhs + c0 + cj, Pend<float>::fix(acc[q][0]));
+                    if (ra < w && cj + 1 < nc)
+                        st_relaxed(x + (size_t)(a + ra) * rhs + c0 + cj + 1, Pend<float>::fix(acc[q][1]));
+                    if (rb < w && cj < nc) st_relaxed(x + (size_t)(a + rb) * rhs + c0 + cj, Pend<float>::fix(acc[q][2]));
+                    if (rb < w && cj + 1 < nc)
+                        st_relaxed(x + (size_t)(a + rb) * rhs + c0 + cj + 1, Pend<float>::fix(acc[q][3]));
+                }
+            }
+        }
+        if (__syncthreads_or(!ok)) break;
+    }
+}
+
+// --- FP32 Jacobi sweep ------------------------------------------------------------------------
+
+// d_new = (r - N d_old) * invd for the Jacobi systems still sweeping (sweep k reads d[k & 1] and
+// writes d[(k + 1) & 1]; sweep 0 starts from d = 0), with per-system max |d_new| and
+// max |d_new - d_old|.
+__global__ void __launch_bounds__(256) k_b_jacobi(BArgs A, SegList rows) {
+    const int k = *(volatile const int*)&A.bc->sweep_k;
+    const float* src = (k & 1) ? A.d1 : A.d0;
+    float* dst = (k & 1) ? A.d0 : A.d1;
+    const int lane = threadIdx.x & 31;
+    float mx = 0.f, ch = 0.f;
+    for_rows(
+        rows,
+        [&](int s, int i) {
+            const BState& T = A.st[s];
+            if (T.done || T.inner_done) return;
+            const BSys S = A.sys[s];
+            const int r = S.rhs;
+            const int* rp = A.rp + S.rp0;
+            const int beg = rp[i], end = rp[i + 1];
+            const int* cl = A.col + S.nz0;
+            const float* vl = A.val32 + S.nz0;
+            const float dinv = A.invd32[S.row0 + i];
+            const float* rr = A.r32 + S.xb0;
+            const float* so = src + S.xb0;
+            float* dd = dst + S.xb0;
+            for (int c0 = 0; c0 < r; c0 += 32) {
+                const int nc = min(32, r - c0);
+                int groups, g, c;
+                lane_split(nc, groups, g, c);
+                float sum = 0.f;
+                if (k > 0 && g < groups)
+                    for (int q = beg + 1 + g; q < end; q += groups) sum = fmaf(vl[q], so[(size_t)cl[q] * r + c0 + c], sum);
+                sum = group_sum(sum, groups, nc);
+                if (lane < nc) {
+                    const size_t o = (size_t)i * r + c0 + lane;
+                    const float dn = (rr[o] - sum) * dinv;
+                    const float old = k > 0 ? so[o] : 0.f;
+                    dd[o] = dn;
+                    mx = fmaxf(mx, fabsf(dn));
+                    ch = fmaxf(ch, fabsf(dn - old));
+                }
+            }
+        },
+        [&](int s) {
+            const float m1 = warp_max(mx), m2 = warp_max(ch);
+            if (lane == 0 && (m1 > 0.f || m2 > 0.f)) {
+                atomicMax(&A.st[s].dmax_bits, __float_as_uint(m1));
+                atomicMax(&A.st[s].dchg_bits, __float_as_uint(m2));
+            }
+            mx = ch = 0.f;
+        });
+}
+
+// --- FP64 residual ----------------------------------------------------------------------------
+
+// r = b - U x in FP64 for the systems still refining; r32 = (float) r; ||r||^2 per system.
+__global__ void __launch_bounds__(256) k_b_residual(BArgs A, SegList rows) {
+    const int lane = threadIdx.x & 31;
+    double acc = 0.0;
+    for_rows(
+        rows,
+        [&](int s, int i) {
+            if (A.st[s].done) return;
+            const BSys S = A.sys[s];
+            const int r = S.rhs;
+            const int* rp = A.rp + S.rp0;
+            const int beg = rp[i], end = rp[i + 1];
+            const int* cl = A.col + S.nz0;
+            const double* vl = A.val + S.nz0;
+            const double* xx = A.x + S.xb0;
+            const double* bb = A.b + S.xb0;
+            for (int c0 = 0; c0 < r; c0 += 32) {
+                const int nc = min(32, r - c0);
+                int groups, g, c;
+                lane_split(nc, groups, g, c);
+                double sum = 0.0;
+                if (g < groups)
+                    for (int q = beg + g; q < end; q += groups) sum = fma(__ldg(vl + q), xx[(size_t)__ldg(cl + q) * r + c0 + c], sum);
+                sum = group_sum(sum, groups, nc);
+                if (lane < nc) {
+                    const size_t o = (size_t)i * r + c0 + lane;
+                    const double rv = bb[o] - sum;
+                    A.r32[S.xb0 + o] = (float)rv;
+                    acc = fma(rv, rv, acc);
+                }
+            }
+        },
+        [&](int s) {
+            const double v = warp_sum(acc);
+            if (lane == 0 && v != 0.0) atomicAdd(&A.st[s].rnorm2, v);
+            acc = 0.0;
+        });
+}
+
+// --- control (one block) ------------------------------------------------------------------------
+
+__device__ __forceinline__ int block_count(int v) {
+    __shared__ int s_cnt;
+    if (threadIdx.x == 0) s_cnt = 0;
+    __syncthreads();
+    const int w = __reduce_add_sync(0xffffffffu, v);
+    if ((threadIdx.x & 31) == 0 && w) atomicAdd(&s_cnt, w);
+    __syncthreads();
+    const int r = s_cnt;
+    __syncthreads();
+    return r;
+}
+
+// Start of the chosen solve: the mixed systems begin refining.
+__global__ void k_b_state_init(BArgs A, int count, cudaGraphConditionalHandle outer, bool set_cond) {
+    int mine = 0;
+    for (int s0 = 0; s0 < count; s0 += blockDim.x) {
+        const int s = s0 + threadIdx.x;
+        int m = 0;
+        if (s < count) {
+            BState& T = A.st[s];
+            T.done = A.sys[s].sched == BS_PLAIN ? 1 : 0;
+            m = !T.done;
+        }
+        mine += block_count(m);
+    }
+    if (threadIdx.x == 0) {
+        A.bc->active = mine;
+        A.bc->nmixed = mine;
+        if (set_cond) cudaGraphSetConditional(outer, mine > 0 ? 1u : 0u);
+    }
+}
+
+// Start of a refinement step: reset the inner solves of the systems still refining.
+__global__ void k_b_inner_begin(BArgs A, int count, cudaGraphConditionalHandle inner, bool set_cond) {
+    int jac = 0;
+    for (int s0 = 0; s0 < count; s0 += blockDim.x) {
+        const int s = s0 + threadIdx.x;
+        int j = 0;
+        if (s < count) {
+            BState& T = A.st[s];
+            T.final_idx = 0;
+            if (!T.done && A.sys[s].sched == BS_JACOBI) {
+                T.inner_done = 0;
+                T.inner_count = 0;
+                T.dmax_bits = T.dchg_bits = 0u;
+                j = 1;
+            }
+        }
+        jac += block_count(j);
+    }
+    if (threadIdx.x == 0) {
+        A.bc->jac_active = jac;
+        A.bc->sweep_k = 0;
+        A.bc->c.ticket = 0u;
+        A.bc->c.ticket2 = 0u;
+        if (set_cond) cudaGraphSetConditional(inner, jac > 0 && !A.bc->c.status ? 1u : 0u);
+    }
+}
+
+// After a Jacobi sweep: per-system change test |d_new - d_old| <= eps |d_new| (max norms) or the
+// sweep cap.
+__global__ void k_b_jcheck(BArgs A, int count, cudaGraphConditionalHandle inner) {
+    const int k = A.bc->sweep_k;
+    int still = 0, swept = 0;
+    for (int s0 = 0; s0 < count; s0 += blockDim.x) {
+        const int s = s0 + threadIdx.x;
+        int st = 0, sw = 0;
+        if (s < count) {
+            BState& T = A.st[s];
+            if (!T.done && A.sys[s].sched == BS_JACOBI && !T.inner_done) {
+                sw = 1;
+                ++T.inner_count;
+                ++T.sweeps;
+                const float mx = __uint_as_float(T.dmax_bits), ch = __uint_as_float(T.dchg_bits);
+                const bool conv = k > 0 ? ch <= A.inner_eps * mx : mx == 0.f;
+                if (conv || T.inner_count >= A.max_sweeps || !(ch == ch)) {
+                    T.inner_done = 1;
+                    T.final_idx = (k + 1) & 1;
+                } else {
+                    st = 1;
+                }
+                T.dmax_bits = T.dchg_bits = 0u;
+            }
+        }
+        still += block_count(st);
+        swept += block_count(sw);
+    }
+    if (threadIdx.x == 0) {
+        A.bc->jac_active = still;
+        A.bc->sweep_k = k + 1;
+        A.bc->total_sweeps += swept > 0 ? 1 : 0;
+        cudaGraphSetConditional(inner, still > 0 && !A.bc->c.status ? 1u : 0u);
+    }
+}
+
+// After the residual: per-system convergence; the step loop runs while any system refines.
+__global__ void k_b_check(BArgs A, int count, cudaGraphConditionalHandle outer) {
+    int act = 0;
+    for (int s0 = 0; s0 < count; s0 += blockDim.x) {
+        const int s = s0 + threadIdx.x;
+        int a = 0;
+        if (s < count) {
+            BState& T = A.st[s];
+            if (!T.done) {
+                ++T.steps;
+                const double rel = T.bnorm2 > 0.0 ? sqrt(T.rnorm2 / T.bnorm2) : sqrt(T.rnorm2);
+                T.rel = rel;
+                T.rnorm2 = 0.0;
+                if (rel <= A.tol) {
+                    T.done = 1;
+                } else if (T.steps >= A.max_refine || !(rel == rel)) {
+                    T.done = 2;
+                    T.status = SPTRSV_ERR_NOT_CONVERGED;
+                } else {
+                    a = 1;
+                }
+            }
+        }
+        act += block_count(a);
+    }
+    if (threadIdx.x == 0) {
+        A.bc->active = act;
+        A.bc->outer += 1;
+        cudaGraphSetConditional(outer, act > 0 && !A.bc->c.status ? 1u : 0u);
+    }
+}
+
+// --- host side --------------------------------------------------------------------------------
+
+struct HostSeg {
+    std::vector<int> sys;
+    std::vector<long long> off{0};
+    void add(int s, long long cnt) {
+        sys.push_back(s);
+        off.push_back(off.back() + cnt);
+    }
+    long long total() const { return off.back(); }
+};
+
+struct DevSeg {
+    DevBuf sys, off;
+    int nseg = 0;
+    long long total = 0;
+    int upload(const HostSeg& h, cudaStream_t st) {
+        nseg = (int)h.sys.size();
+        total = h.total();
+        if (!nseg) return 0;
+        int rc;
+        if ((rc = sys.ensure(sizeof(int) * nseg)) || (rc = off.ensure(sizeof(long long) * (nseg + 1)))) return rc;
+        CUDA_TRY(cudaMemcpyAsync(sys.p, h.sys.data(), sizeof(int) * nseg, cudaMemcpyHostToDevice, st));
+        CUDA_TRY(cudaMemcpyAsync(off.p, h.off.data(), sizeof(long long) * (nseg + 1), cudaMemcpyHostToDevice, st));
+        CUDA_TRY(cudaStreamSynchronize(st));
+        return 0;
+    }
+    SegList list() const { return SegList{sys.as<int>(), off.as<long long>(), nseg, total}; }
+    void release() { sys.release(); off.release(); nseg = 0; total = 0; }
+};
+
+struct Batch {
+    int device = 0;
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    int sm_count = 0;
+    int count = 0;
+    std::vector<BSys> sys;
+    std::vector<float> ratio;
+    std::vector<int> sched;
+    std::vector<int> panel_ok;  // -1 unknown, 0 no, 1 yes
+    long long tot_rows = 0, tot_nnz = 0, tot_x = 0, tot_rp = 0;
+    DevBuf rp, col, val, val32, invd, invd32, dsys, dstate, dctl;
+    DevBuf r32, d0, d1, bw, xw;
+    // schedule-dependent work lists
+    DevBuf order_all, order_plain, order_sf32, items, chunks;
+    unsigned n_order_all = 0, n_order_plain = 0, n_order_sf32 = 0, n_items = 0;
+    DevSeg all_rows, all_el, mixed_rows, mixed_el, jac_rows, pend_el, plain_el;
+    std::vector<DevBuf> gbufs;            // per panel system: hi, lo, rect
+    std::vector<std::vector<BChunk>> pchunks;  // per system (host copies, pointers into gbufs)
+    std::vector<int> gidx;                // per system: first of its 3 gbufs, or -1
+    bool lists_ready = false;
+    // options
+    double tol = 1e-12;
+    int max_refine = 20, max_sweeps = 200, inner_tol_exp = 6;
+    int64_t budget = kDefaultBudgetNs;
+    // graphs
+    struct G {
+        int mode = -1;
+        const double* b = nullptr;
+        double* x = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        int64_t fixed = 0;
+    };
+    std::vector<G> graphs;
+    int64_t launches = 0;
+    int last_mode = -1;
+    int64_t last_fixed = 0;
+    Handle* scratch = nullptr;
+
+    ~Batch();
+    BArgs args(const double* b, double* x) const;
+    int build_lists();
+    int build_panels(int s);
+    int build_graph(int mode, const double* b, double* x, cudaGraphExec_t* out, int64_t* fixed);
+    int solve(int mode, const double* b, double* x);
+    int sync(int64_t* kernels);
+    void drop_graphs() {
+        for (auto& g : graphs) if (g.exec) cudaGraphExecDestroy(g.exec);
+        graphs.clear();
+    }
+};
+
+Batch::~Batch() {
+    if (device >= 0) cudaSetDevice(device);
+    drop_graphs();
+    DevBuf* bufs[] = {&rp, &col, &val, &val32, &invd, &invd32, &dsys, &dstate, &dctl, &r32, &d0, &d1, &bw, &xw,
+                      &order_all, &order_plain, &order_sf32, &items, &chunks};
+    for (DevBuf* b : bufs) b->release();
+    DevSeg* segs[] = {&all_rows, &all_el, &mixed_rows, &mixed_el, &jac_rows, &pend_el, &plain_el};
+    for (DevSeg* s : segs) s->release();
+    for (auto& b : gbufs) b.release();
+    if (scratch) sptrsv_destroy(reinterpret_cast<sptrsv_handle>(scratch));
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+    if (st) cudaStreamDestroy(st);
+}
+
+BArgs Batch::args(const double* b, double* x) const {
+    BArgs A{};
+    A.sys = dsys.as<BSys>();
+    A.st = dstate.as<BState>();
+    A.bc = dctl.as<BCtl>();
+    A.rp = rp.as<int>();
+    A.col = col.as<int>();
+    A.val = val.as<double>();
+    A.val32 = val32.as<float>();
+    A.invd = invd.as<double>();
+    A.invd32 = invd32.as<float>();
+    A.b = b;
+    A.x = x;
+    A.r32 = r32.as<float>();
+    A.d0 = d0.as<float>();
+    A.d1 = d1.as<float>();
+    A.budget = budget;
+    A.tol = tol;
+    A.inner_eps = powf(10.f, -(float)inner_tol_exp);
+    A.max_refine = max_refine;
+    A.max_sweeps = max_sweeps;
+    return A;
+}
+
+// Queue order interleaving the systems from their last rows: position t holds row n_s - 1 - t of
+// every listed system with n_s > t (systems by decreasing n, then index).
+static std::vector<int2> interleave_rows(const std::vector<BSys>& sys, const std::vector<int>& pick) {
+    std::vector<int> ord = pick;
+    std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return sys[a].n > sys[b].n; });
+    long long tot = 0;
+    for (int s : ord) tot += sys[s].n;
+    std::vector<int2> out;
+    out.reserve(tot);
+    const int nmax = ord.empty() ? 0 : sys[ord[0]].n;
+    size_t live = ord.size();
+    for (int t = 0; t < nmax; ++t) {
+        while (live > 0 && sys[ord[live - 1]].n <= t) --live;
+        for (size_t k = 0; k < live; ++k) out.push_back(make_int2(ord[k], sys[ord[k]].n - 1 - t));
+    }
+    return out;
+}
+
+template <typename T>
+static int upload_vec(DevBuf& d, const std::vector<T>& h, cudaStream_t st) {
+    if (h.empty()) return 0;
+    int rc = d.ensure(sizeof(T) * h.size());
+    if (rc) return rc;
+    CUDA_TRY(cudaMemcpyAsync(d.p, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    return 0;
+}
+
+// Dense panels of system s: uniform 64-row chunks (each one a skyline or exact supernode chunk),
+// G = [T^-1 | -T^-1 Rect] formed in FP64 by the single-system supernodal analysis and kept as
+// its BF16 hi/lo split.
+int Batch::build_panels(int s) {
+    if (panel_ok[s] >= 0) return panel_ok[s] ? 0 : SPTRSV_ERR_SUPERNODES;
+    int rc;
+    if (!scratch) {
+        sptrsv_handle h = nullptr;
+        if ((rc = sptrsv_create(&h, device))) return rc;
+        scratch = reinterpret_cast<Handle*>(h);
+    }
+    Handle& H = *scratch;
+    const BSys& S = sys[s];
+    H.drop_matrix();
+    H.n = S.n;
+    H.nnz = (int)(s + 1 < count ? sys[s + 1].nz0 - S.nz0 : tot_nnz - S.nz0);
+    H.rp = rp.as<int>() + S.rp0;
+    H.col = col.as<int>() + S.nz0;
+    H.val = val.as<double>() + S.nz0;
+    if ((rc = H.analyse())) return rc;
+    std::vector<int> sn;
+    for (int a = 0; a < S.n; a += kBPanel) sn.push_back(a);
+    sn.push_back(S.n);
+    rc = H.set_supernodes((int)sn.size() - 1, sn.data());
+    if (rc == SPTRSV_ERR_SUPERNODES) {
+        panel_ok[s] = 0;
+        return rc;
+    }
+    if (rc) return rc;
+    const int C = H.sn_count;
+    std::vector<int> ss(C + 1), mm(C), roff(C + 1), ld(C);
+    std::vector<long long> goff(C + 1);
+    CUDA_TRY(cudaMemcpy(ss.data(), H.sn_start.p, sizeof(int) * (C + 1), cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(mm.data(), H.sn_m.p, sizeof(int) * C, cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(roff.data(), H.sn_roff.p, sizeof(int) * (C + 1), cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(ld.data(), H.sn_ld.p, sizeof(int) * C, cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(goff.data(), H.sn_goff.p, sizeof(long long) * (C + 1), cudaMemcpyDeviceToHost));
+    const long long gtot = goff[C];
+    const int k0 = (int)gbufs.size();
+    gbufs.resize(k0 + 3);
+    if ((rc = gbufs[k0].ensure(2 * (size_t)gtot)) || (rc = gbufs[k0 + 1].ensure(2 * (size_t)gtot)) ||
+        (rc = gbufs[k0 + 2].ensure(sizeof(int) * ((size_t)roff[C] + 1))))
+        return rc;
+    CUDA_TRY(cudaMemcpyAsync(gbufs[k0].p, H.sn_Ghi.p, 2 * (size_t)gtot, cudaMemcpyDeviceToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(gbufs[k0 + 1].p, H.sn_Glo.p, 2 * (size_t)gtot, cudaMemcpyDeviceToDevice, st));
+    if (roff[C] > 0)
+        CUDA_TRY(cudaMemcpyAsync(gbufs[k0 + 2].p, H.sn_rect.p, sizeof(int) * roff[C], cudaMemcpyDeviceToDevice, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    gidx[s] = k0;
+    pchunks[s].clear();
+    for (int c = 0; c < C; ++c) {
+        BChunk ch{};
+        ch.sys = s;
+        ch.a = ss[c];
+        ch.w = ss[c + 1] - ss[c];
+        ch.m = mm[c];
+        ch.ld = ld[c];
+        ch.ghi = gbufs[k0].as<__nv_bfloat16>() + goff[c];
+        ch.glo = gbufs[k0 + 1].as<__nv_bfloat16>() + goff[c];
+        ch.rect = gbufs[k0 + 2].as<int>() + roff[c];
+        pchunks[s].push_back(ch);
+    }
+    H.drop_matrix();
+    panel_ok[s] = 1;
+    return 0;
+}
+
+int Batch::build_lists() {
+    if (lists_ready) return 0;
+    int rc;
+    for (int s = 0; s < count; ++s)
+        if (sched[s] == BS_PANEL && (rc = build_panels(s))) return rc;
+    std::vector<int> plain, sf32;
+    HostSeg mr, me, jr, pe, pl;
+    for (int s = 0; s < count; ++s) {
+        const long long n = sys[s].n, ne = n * sys[s].rhs;
+        sys[s].sched = sched[s];
+        if (sched[s] == BS_PLAIN) {
+            plain.push_back(s);
+            pl.add(s, ne);
+            continue;
+        }
+        mr.add(s, n);
+        me.add(s, ne);
+        if (sched[s] == BS_JACOBI) jr.add(s, n);
+        if (sched[s] == BS_PANEL || sched[s] == BS_SF32) pe.add(s, ne);
+        if (sched[s] == BS_SF32) sf32.push_back(s);
+    }
+    if ((rc = upload_vec(dsys, sys, st))) return rc;
+    if ((rc = mixed_rows.upload(mr, st)) || (rc = mixed_el.upload(me, st)) || (rc = jac_rows.upload(jr, st)) ||
+        (rc = pend_el.upload(pe, st)) || (rc = plain_el.upload(pl, st)))
+        return rc;
+    std::vector<int2> op = interleave_rows(sys, plain), os = interleave_rows(sys, sf32);
+    n_order_plain = (unsigned)op.size();
+    n_order_sf32 = (unsigned)os.size();
+    if ((rc = upload_vec(order_plain, op, st)) || (rc = upload_vec(order_sf32, os, st))) return rc;
+    // panel work items: per system its chunks' panels from the last, interleaved across systems
+    std::vector<BChunk> ch;
+    std::vector<std::vector<int2>> per;
+    for (int s = 0; s < count; ++s) {
+        if (sched[s] != BS_PANEL) continue;
+        const int base = (int)ch.size();
+        std::vector<int2> its;
+        for (int c = (int)pchunks[s].size() - 1; c >= 0; --c)
+            for (int p = (pchunks[s][c].w + kBPanel - 1) / kBPanel - 1; p >= 0; --p) its.push_back(make_int2(base + c, p));
+        for (const BChunk& b : pchunks[s]) ch.push_back(b);
+        per.push_back(std::move(its));
+    }
+    std::vector<int2> it;
+    size_t longest = 0;
+    for (auto& v : per) longest = std::max(longest, v.size());
+    for (size_t t = 0; t < longest; ++t)
+        for (auto& v : per)
+            if (t < v.size()) it.push_back(v[t]);
+    n_items = (unsigned)it.size();
+    if ((rc = upload_vec(chunks, ch, st)) || (rc = upload_vec(items, it, st))) return rc;
+    lists_ready = true;
+    drop_graphs();
+    return 0;
+}
+
+static int resident(const void* kernel, int threads, int sm_count, long long want) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0) != cudaSuccess) per_sm = 1;
+    const long long g = (long long)std::max(1, per_sm) * sm_count;
+    return (int)std::max(1LL, std::min(g, want));
+}
+
+static int elem_grid(int sm_count, long long total) {
+    return (int)std::max(1LL, std::min((long long)sm_count * 16, (total + 255) / 256));
+}
+
+static int row_grid(int sm_count, long long rows) {
+    const long long tasks = (rows + kBRowChunk - 1) / kBRowChunk;
+    return (int)std::max(1LL, std::min((long long)sm_count * 8, (tasks + 7) / 8));
+}
+
+int Batch::build_graph(int mode, const double* b, double* x, cudaGraphExec_t* out, int64_t* fixed) {
+    *out = nullptr;
+    int rc = mode == 1 ? build_lists() : 0;
+    if (rc) return rc;
+    const BArgs A = args(b, x);
+    int64_t nk = 0;
+    cudaGraph_t g = nullptr;
+    CUDA_TRY(cudaGraphCreate(&g, 0));
+    cudaGraphConditionalHandle ho = 0, hi = 0;
+    cudaError_t e = cudaSuccess;
+    if (mode == 1) {
+        e = cudaGraphConditionalHandleCreate(&ho, g, 1, cudaGraphCondAssignDefault);
+        if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&hi, g, 0, cudaGraphCondAssignDefault);
+    }
+    if (e != cudaSuccess) { cudaGraphDestroy(g); return set_cuda_error(e, "batch conditional handle"); }
+    auto add_while = [&](cudaGraph_t parent, cudaGraphConditionalHandle h, cudaGraph_t* body) -> cudaError_t {
+        cudaStreamCaptureStatus cs;
+        const cudaGraphNode_t* deps = nullptr;
+        size_t nd = 0;
+        cudaError_t er = cudaStreamGetCaptureInfo(st, &cs, nullptr, nullptr, &deps, nullptr, &nd);
+        if (er != cudaSuccess) return er;
+        alignas(cudaGraphNodeParams) unsigned char raw[sizeof(cudaGraphNodeParams)];
+        memset(raw, 0, sizeof(raw));
+        cudaGraphNodeParams* p = reinterpret_cast<cudaGraphNodeParams*>(raw);
+        p->type = cudaGraphNodeTypeConditional;
+        p->conditional.handle = h;
+        p->conditional.type = cudaGraphCondTypeWhile;
+        p->conditional.size = 1;
+        cudaGraphNode_t node;
+        er = cudaGraphAddNode(&node, parent, deps, nullptr, nd, p);
+        if (er != cudaSuccess) return er;
+        *body = p->conditional.phGraph_out[0];
+        return cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+    };
+    auto launch_pull64 = [&](const DevBuf& order, unsigned n) {
+        const int grid = resident((const void*)k_b_pull<double>, 256, sm_count, ((long long)n + 7) / 8);
+        k_b_pull<double><<<grid, 256, 0, st>>>(A, order.as<int2>(), n, b, x, A.val, A.invd, 0, false);
+        ++nk;
+    };
+    cudaGraph_t obody = nullptr, ibody = nullptr;
+    e = cudaStreamBeginCaptureToGraph(st, g, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
+    if (e != cudaSuccess) { cudaGraphDestroy(g); return set_cuda_error(e, "batch capture"); }
+    cudaMemsetAsync(A.bc, 0, sizeof(BCtl), st);
+    cudaMemsetAsync(A.st, 0, sizeof(BState) * count, st);
+    if (mode == 0) {
+        // plain: every system by the FP64 pull, one persistent launch
+        k_b_fill_pending<double><<<elem_grid(sm_count, all_el.total), 256, 0, st>>>(A, all_el.list(), x, false);
+        ++nk;
+        launch_pull64(order_all, n_order_all);
+    } else {
+        k_b_state_init<<<1, 512, 0, st>>>(A, count, ho, mixed_el.nseg > 0);
+        ++nk;
+        if (n_order_plain) {
+            k_b_fill_pending<double><<<elem_grid(sm_count, plain_el.total), 256, 0, st>>>(A, plain_el.list(), x, false);
+            ++nk;
+            launch_pull64(order_plain, n_order_plain);
+        }
+        if (mixed_el.nseg) {
+            k_b_init_mixed<<<elem_grid(sm_count, mixed_el.total), 256, 0, st>>>(A, mixed_el.list());
+            ++nk;
+            if (add_while(g, ho, &obody) != cudaSuccess) rc = SPTRSV_ERR_CUDA;
+        }
+    }
+    cudaGraph_t g2 = nullptr;
+    e = cudaStreamEndCapture(st, &g2);
+    if (!rc && e != cudaSuccess) rc = set_cuda_error(e, "batch capture end");
+    *fixed = nk;
+    int64_t per_outer = 0;
+    if (!rc && obody) {
+        e = cudaStreamBeginCaptureToGraph(st, obody, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
+        if (e == cudaSuccess) {
+            int64_t k0 = nk;
+            k_b_inner_begin<<<1, 512, 0, st>>>(A, count, hi, jac_rows.nseg > 0);
+            ++nk;
+            if (pend_el.nseg) {
+                k_b_fill_pending<float><<<elem_grid(sm_count, pend_el.total), 256, 0, st>>>(A, pend_el.list(), A.d0, true);
+                ++nk;
+            }
+            if (n_items) {
+                const int grid = resident((const void*)k_b_panels, 128, sm_count, n_items);
+                k_b_panels<<<grid, 128, 0, st>>>(A, items.as<int2>(), n_items, chunks.as<BChunk>());
+                ++nk;
+            }
+            if (n_order_sf32) {
+                const int grid = resident((const void*)k_b_pull<float>, 256, sm_count, ((long long)n_order_sf32 + 7) / 8);
+                k_b_pull<float><<<grid, 256, 0, st>>>(A, order_sf32.as<int2>(), n_order_sf32, A.r32, A.d0, A.val32,
+                                                      A.invd32, 1, true);
+                ++nk;
+            }
+            if (jac_rows.nseg && add_while(obody, hi, &ibody) != cudaSuccess) rc = SPTRSV_ERR_CUDA;
+            k_b_axpy<<<elem_grid(sm_count, mixed_el.total), 256, 0, st>>>(A, mixed_el.list());
+            k_b_residual<<<row_grid(sm_count, mixed_rows.total), 256, 0, st>>>(A, mixed_rows.list());
+            k_b_check<<<1, 512, 0, st>>>(A, count, ho);
+            nk += 3;
+            per_outer = nk - k0;
+            e = cudaStreamEndCapture(st, &g2);
+            if (!rc && e != cudaSuccess) rc = set_cuda_error(e, "batch capture outer");
+        } else {
+            rc = set_cuda_error(e, "batch capture outer begin");
+        }
+    }
+    if (!rc && ibody) {
+        e = cudaStreamBeginCaptureToGraph(st, ibody, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
+        if (e == cudaSuccess) {
+            k_b_jacobi<<<row_grid(sm_count, jac_rows.total), 256, 0, st>>>(A, jac_rows.list());
+            k_b_jcheck<<<1, 512, 0, st>>>(A, count, hi);
+            e = cudaStreamEndCapture(st, &g2);
+            if (!rc && e != cudaSuccess) rc = set_cuda_error(e, "batch capture inner");
+        } else {
+            rc = set_cuda_error(e, "batch capture inner begin");
+        }
+    }
+    if (!rc) {
+        e = cudaGraphInstantiate(out, g, 0);
+        if (e != cudaSuccess) rc = set_cuda_error(e, "batch instantiate");
+    }
+    cudaGraphDestroy(g);
+    (void)cudaGetLastError();
+    // launches per refinement step in the upper 32 bits, fixed ones in the lower
+    *fixed = (per_outer << 32) | *fixed;
+    return rc;
+}
+
+int Batch::solve(int mode, const double* b, double* x) {
+    if (mode != 0 && mode != 1) return SPTRSV_ERR_INVALID_ARG;
+    if (!b || !x) return SPTRSV_ERR_INVALID_ARG;
+    int rc = mode == 1 ? build_lists() : 0;
+    if (rc) return rc;
+    G* hit = nullptr;
+    for (auto& gg : graphs)
+        if (gg.mode == mode && gg.b == b && gg.x == x) { hit = &gg; break; }
+    if (!hit) {
+        if (graphs.size() >= 8) drop_graphs();
+        G gg;
+        gg.mode = mode;
+        gg.b = b;
+        gg.x = x;
+        if ((rc = build_graph(mode, b, x, &gg.exec, &gg.fixed))) return rc;
+        graphs.push_back(gg);
+        hit = &graphs.back();
+    }
+    CUDA_TRY(cudaGraphLaunch(hit->exec, st));
+    last_mode = mode;
+    last_fixed = hit->fixed;
+    return 0;
+}
+
+int Batch::sync(int64_t* kernels) {
+    CUDA_TRY(cudaStreamSynchronize(st));
+    BCtl c{};
+    CUDA_TRY(cudaMemcpy(&c, dctl.p, sizeof(c), cudaMemcpyDeviceToHost));
+    const int64_t fixed = last_fixed & 0xffffffffLL, per_outer = last_fixed >> 32;
+    const int64_t k = fixed + per_outer * c.outer + 2 * (int64_t)c.total_sweeps;
+    launches += k;
+    if (kernels) *kernels = k;
+    if (c.c.status) return c.c.status;
+    if (last_mode == 1) {
+        std::vector<BState> h(count);
+        CUDA_TRY(cudaMemcpy(h.data(), dstate.p, sizeof(BState) * count, cudaMemcpyDeviceToHost));
+        for (const BState& t : h)
+            if (t.status) return t.status;
+    }
+    return 0;
+}
+
+// Default schedule from the analysis: dense row ranges (banded / skyline) -> panels; rows
+// dominated by their diagonal -> Jacobi; otherwise the FP32 sync-free pull.
+static int default_schedule(const BSys& S, long long nnz, float ratio, int gapped) {
+    if (!gapped && nnz >= 8LL * S.n) return BS_PANEL;
+    if (ratio < 1.f) return BS_JACOBI;
+    return BS_SF32;
+}
+
+}  // namespace sptrsv
+
+using sptrsv::Batch;
+
+extern "C" {
+
+int sptrsv_batch_create(sptrsv_batch* out, int device, int count, const int* n, const int* rhs,
+                        const int64_t* row_ptr, const int* col, const double* val) {
+    using namespace sptrsv;
+    if (!out) return SPTRSV_ERR_INVALID_ARG;
+    *out = nullptr;
+    if (count < 1 || !n || !rhs || !row_ptr || !col || !val) return SPTRSV_ERR_INVALID_ARG;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        (void)cudaGetLastError();
+        return SPTRSV_ERR_NO_DEVICE;
+    }
+    if (device < 0) CUDA_TRY(cudaGetDevice(&device));
+    if (device >= ndev) return SPTRSV_ERR_INVALID_ARG;
+    // host-side layout and row-pointer checks
+    std::vector<BSys> sys(count);
+    std::vector<long long> nnz(count);
+    long long rp0 = 0, nz0 = 0, row0 = 0, xb0 = 0;
+    for (int s = 0; s < count; ++s) {
+        if (n[s] < 1 || rhs[s] < 1) return SPTRSV_ERR_INVALID_ARG;
+        const int64_t* r = row_ptr + rp0;
+        if (r[0] != 0) return SPTRSV_ERR_ROW_PTR;
+        for (int i = 0; i < n[s]; ++i)
+            if (r[i + 1] < r[i]) return SPTRSV_ERR_ROW_PTR;
+        if (r[n[s]] > 0x7fffffffLL) return SPTRSV_ERR_TOO_LARGE;
+        if ((long long)n[s] * rhs[s] > 0x7fffffffLL) return SPTRSV_ERR_TOO_LARGE;
+        nnz[s] = r[n[s]];
+        sys[s] = BSys{n[s], rhs[s], BS_PLAIN, 0, rp0, nz0, row0, xb0};
+        rp0 += n[s] + 1;
+        nz0 += nnz[s];
+        row0 += n[s];
+        xb0 += (long long)n[s] * rhs[s];
+    }
+    if (row0 > 0x7fffffffLL) return SPTRSV_ERR_TOO_LARGE;
+    CUDA_TRY(cudaSetDevice(device));
+    Batch* B = new Batch;
+    B->device = device;
+    B->count = count;
+    B->sys = sys;
+    B->tot_rp = rp0;
+    B->tot_nnz = nz0;
+    B->tot_rows = row0;
+    B->tot_x = xb0;
+    B->sched.assign(count, BS_PLAIN);
+    B->panel_ok.assign(count, -1);
+    B->gidx.assign(count, -1);
+    B->pchunks.resize(count);
+    int rc = 0;
+    auto fail = [&](int code) {
+        delete B;
+        return code;
+    };
+    cudaError_t er;
+    if ((er = cudaStreamCreateWithFlags(&B->st, cudaStreamNonBlocking)) != cudaSuccess ||
+        (er = cudaEventCreate(&B->ev0)) != cudaSuccess || (er = cudaEventCreate(&B->ev1)) != cudaSuccess ||
+        (er = cudaDeviceGetAttribute(&B->sm_count, cudaDevAttrMultiProcessorCount, device)) != cudaSuccess)
+        return fail(set_cuda_error(er, "batch setup"));
+    {
+        std::vector<int> rp32(rp0);
+        for (long long k = 0; k < rp0; ++k) rp32[k] = (int)row_ptr[k];
+        if ((rc = B->rp.ensure(sizeof(int) * rp0)) || (rc = B->col.ensure(sizeof(int) * std::max(1LL, nz0))) ||
+            (rc = B->val.ensure(sizeof(double) * std::max(1LL, nz0))) ||
+            (rc = B->val32.ensure(sizeof(float) * std::max(1LL, nz0))) || (rc = B->invd.ensure(sizeof(double) * row0)) ||
+            (rc = B->invd32.ensure(sizeof(float) * row0)) || (rc = B->dstate.ensure(sizeof(BState) * count)) ||
+            (rc = B->dctl.ensure(sizeof(BCtl))) || (rc = B->r32.ensure(sizeof(float) * xb0)) ||
+            (rc = B->d0.ensure(sizeof(float) * xb0)) || (rc = B->d1.ensure(sizeof(float) * xb0)))
+            return fail(rc);
+        // stream-ordered copies: the kernels below run on the batch's non-blocking stream
+        if ((er = cudaMemcpyAsync(B->rp.p, rp32.data(), sizeof(int) * rp0, cudaMemcpyHostToDevice, B->st)) !=
+                cudaSuccess ||
+            (er = cudaStreamSynchronize(B->st)) != cudaSuccess)
+            return fail(set_cuda_error(er, "batch upload"));
+    }
+    if (nz0 > 0) {
+        if ((er = cudaMemcpyAsync(B->col.p, col, sizeof(int) * nz0, cudaMemcpyHostToDevice, B->st)) != cudaSuccess ||
+            (er = cudaMemcpyAsync(B->val.p, val, sizeof(double) * nz0, cudaMemcpyHostToDevice, B->st)) !=
+                cudaSuccess)
+            return fail(set_cuda_error(er, "batch upload"));
+        k_to_f32<<<B->sm_count * 16, 256, 0, B->st>>>((size_t)nz0, B->val.as<double>(), B->val32.as<float>());
+        ++B->launches;
+    }
+    if ((rc = upload_vec(B->dsys, sys, B->st))) return fail(rc);
+    HostSeg ar, ae;
+    std::vector<int> all(count);
+    for (int s = 0; s < count; ++s) {
+        ar.add(s, sys[s].n);
+        ae.add(s, (long long)sys[s].n * sys[s].rhs);
+        all[s] = s;
+    }
+    if ((rc = B->all_rows.upload(ar, B->st)) || (rc = B->all_el.upload(ae, B->st))) return fail(rc);
+    {
+        std::vector<int2> oa = interleave_rows(sys, all);
+        B->n_order_all = (unsigned)oa.size();
+        if ((rc = upload_vec(B->order_all, oa, B->st))) return fail(rc);
+    }
+    if ((er = cudaMemsetAsync(B->dstate.p, 0, sizeof(BState) * count, B->st)) != cudaSuccess ||
+        (er = cudaMemsetAsync(B->dctl.p, 0, sizeof(BCtl), B->st)) != cudaSuccess)
+        return fail(set_cuda_error(er, "batch memset"));
+    const BArgs A = B->args(nullptr, nullptr);
+    k_b_setup<<<row_grid(B->sm_count, row0), 256, 0, B->st>>>(A, B->all_rows.list());
+    ++B->launches;
+    if ((er = cudaGetLastError()) != cudaSuccess || (er = cudaStreamSynchronize(B->st)) != cudaSuccess)
+        return fail(set_cuda_error(er, "batch setup kernels"));
+    BCtl c{};
+    std::vector<BState> hs(count);
+    if ((er = cudaMemcpy(&c, B->dctl.p, sizeof(c), cudaMemcpyDeviceToHost)) != cudaSuccess ||
+        (er = cudaMemcpy(hs.data(), B->dstate.p, sizeof(BState) * count, cudaMemcpyDeviceToHost)) != cudaSuccess)
+        return fail(set_cuda_error(er, "batch setup read"));
+    if (c.c.status) return fail(c.c.status);
+    B->ratio.resize(count);
+    for (int s = 0; s < count; ++s) {
+        float r;
+        memcpy(&r, &hs[s].ratio_bits, sizeof(float));
+        B->ratio[s] = r;
+        B->sched[s] = default_schedule(sys[s], nnz[s], r, hs[s].gapped);
+        if (hs[s].gapped) B->panel_ok[s] = 0;
+    }
+    *out = reinterpret_cast<sptrsv_batch>(B);
+    return 0;
+}
+
+int sptrsv_batch_destroy(sptrsv_batch bh) {
+    Batch* B = reinterpret_cast<Batch*>(bh);
+    if (!B) return SPTRSV_ERR_INVALID_ARG;
+    delete B;
+    return 0;
+}
+
+#define BH()                                                        \
+    Batch* B = reinterpret_cast<Batch*>(bh);                        \
+    if (!B) return SPTRSV_ERR_INVALID_ARG;                          \
+    if (cudaSetDevice(B->device) != cudaSuccess) return SPTRSV_ERR_CUDA
+
+int sptrsv_batch_get_schedule(sptrsv_batch bh, int* sched) {
+    BH();
+    if (!sched) return SPTRSV_ERR_INVALID_ARG;
+    for (int s = 0; s < B->count; ++s) sched[s] = B->sched[s];
+    return 0;
+}
+
+int sptrsv_batch_set_schedule(sptrsv_batch bh, const int* sched) {
+    using namespace sptrsv;
+    BH();
+    if (!sched) return SPTRSV_ERR_INVALID_ARG;
+    for (int s = 0; s < B->count; ++s)
+        if (sched[s] < -1 || sched[s] >= BS_COUNT) return SPTRSV_ERR_INVALID_ARG;
+    for (int s = 0; s < B->count; ++s) {
+        if (sched[s] == BS_PANEL) {
+            const int rc = B->build_panels(s);
+            if (rc) return rc;
+        }
+        if (sched[s] == BS_JACOBI && !(B->ratio[s] < 1.f)) return SPTRSV_ERR_UNSUPPORTED;
+    }
+    for (int s = 0; s < B->count; ++s)
+        if (sched[s] >= 0) B->sched[s] = sched[s];
+    B->lists_ready = false;
+    B->drop_graphs();
+    return 0;
+}
+
+int sptrsv_batch_set_options(sptrsv_batch bh, double tol, int max_refine, int inner_tol_exp, int64_t budget_ns) {
+    BH();
+    if (tol > 0) B->tol = tol;
+    if (max_refine > 0) B->max_refine = max_refine;
+    if (inner_tol_exp > 0) B->inner_tol_exp = inner_tol_exp;
+    if (budget_ns > 0) B->budget = budget_ns;
+    B->drop_graphs();
+    return 0;
+}
+
+int sptrsv_batch_solve(sptrsv_batch bh, int mode, const double* d_b, double* d_x) {
+    BH();
+    const int rc = B->solve(mode, d_b, d_x);
+    sptrsv::set_last_status(rc);
+    return rc;
+}
+
+int sptrsv_batch_sync(sptrsv_batch bh, int64_t* kernels) {
+    BH();
+    const int rc = B->sync(kernels);
+    sptrsv::set_last_status(rc);
+    return rc;
+}
+
+int sptrsv_batch_solve_host(sptrsv_batch bh, int mode, const double* h_b, double* h_x) {
+    BH();
+    if (!h_b || !h_x) return SPTRSV_ERR_INVALID_ARG;
+    int rc;
+    const size_t bytes = sizeof(double) * (size_t)B->tot_x;
+    if ((rc = B->bw.ensure(bytes)) || (rc = B->xw.ensure(bytes))) return rc;
+    CUDA_TRY(cudaMemcpyAsync(B->bw.p, h_b, bytes, cudaMemcpyHostToDevice, B->st));
+    if ((rc = B->solve(mode, B->bw.as<double>(), B->xw.as<double>()))) return rc;
+    CUDA_TRY(cudaMemcpyAsync(h_x, B->xw.p, bytes, cudaMemcpyDeviceToHost, B->st));
+    return 0;
+}
+
+int sptrsv_batch_stats(sptrsv_batch bh, int* status, int* steps, double* rel, int* sweeps) {
+    BH();
+    std::vector<sptrsv::BState> hs(B->count);
+    CUDA_TRY(cudaStreamSynchronize(B->st));
+    CUDA_TRY(cudaMemcpy(hs.data(), B->dstate.p, sizeof(sptrsv::BState) * B->count, cudaMemcpyDeviceToHost));
+    for (int s = 0; s < B->count; ++s) {
+        if (status) status[s] = hs[s].status;
+        if (steps) steps[s] = hs[s].steps;
+        if (rel) rel[s] = hs[s].rel;
+        if (sweeps) sweeps[s] = hs[s].sweeps;
+    }
+    return 0;
+}
+
+int sptrsv_batch_info(sptrsv_batch bh, int64_t* totals, float* ratio) {
+    BH();
+    if (totals) {
+        totals[0] = B->tot_rows;
+        totals[1] = B->tot_nnz;
+        totals[2] = B->tot_x;
+        totals[3] = B->count;
+    }
+    if (ratio)
+        for (int s = 0; s < B->count; ++s) ratio[s] = B->ratio[s];
+    return 0;
+}
+
+int sptrsv_batch_features(sptrsv_batch bh, int s, float* f) {
+    BH();
+    if (s < 0 || s >= B->count || !f) return SPTRSV_ERR_INVALID_ARG;
+    int rc;
+    if (!B->scratch) {
+        sptrsv_handle h = nullptr;
+        if ((rc = sptrsv_create(&h, B->device))) return rc;
+        B->scratch = reinterpret_cast<sptrsv::Handle*>(h);
+    }
+    sptrsv::Handle& H = *B->scratch;
+    const sptrsv::BSys& S = B->sys[s];
+    H.drop_matrix();
+    H.n = S.n;
+    H.nnz = (int)((s + 1 < B->count ? B->sys[s + 1].nz0 : B->tot_nnz) - S.nz0);
+    H.rp = B->rp.as<int>() + S.rp0;
+    H.col = B->col.as<int>() + S.nz0;
+    H.val = B->val.as<double>() + S.nz0;
+    if ((rc = H.analyse())) return rc;
+    rc = H.features(f, S.rhs);
+    H.drop_matrix();
+    return rc;
+}
+
+int sptrsv_batch_timer_begin(sptrsv_batch bh) {
+    BH();
+    CUDA_TRY(cudaEventRecord(B->ev0, B->st));
+    return 0;
+}
+
+int sptrsv_batch_timer_end(sptrsv_batch bh, float* ms) {
+    BH();
+    CUDA_TRY(cudaEventRecord(B->ev1, B->st));
+    CUDA_TRY(cudaEventSynchronize(B->ev1));
+    float t = 0.f;
+    CUDA_TRY(cudaEventElapsedTime(&t, B->ev0, B->ev1));
+    if (ms) *ms = t;
+    return 0;
+}
+
+int64_t sptrsv_batch_launches(sptrsv_batch bh) {
+    Batch* B = reinterpret_cast<Batch*>(bh);
+    return B ? B->launches : -1;
+}
+
+}  // extern "C"

@@ -116,11 +116,20 @@ struct Handle {
     int resident_warps(const sptrsv_opts& o) const;
     int set_supernodes(int sn, const int* snodes_host);
     SnArgs sn_args() const;
+    // autotuner state (tune.cu)
+    DevBuf tune_b, tune_x;
+    sptrsv_opts tuned[4];
+    bool tuned_valid[4] = {false, false, false, false};
+    bool applicable(const sptrsv_opts& o, int rhs) const;
+    int autotune(int rhs, float cap_ms, int reps, float* ms_out, int* best_id);
+    int features(float* f, int rhs);
     int solve(const sptrsv_opts* o, const double* b, double* x, int rhs, int layout);
     int sync();
 };
 
 void set_last_status(int s);
+int rhs_class(int rhs);
+const sptrsv_opts* tune_candidates(int* count);
 int launch_sn_solve(const Handle& h, bool mixed, const void* b, void* x, int rhs, int64_t budget, int64_t* launches);
 
 }  // namespace sptrsv

@@ -20,6 +20,7 @@
 #include "common.cuh"
 #include "kernels.cuh"
 #include "handle.cuh"
+#include "mma.cuh"
 
 namespace sptrsv {
 
@@ -30,34 +31,63 @@ constexpr int kNc = 32;        // right-hand-side columns per pass
 
 // --- analysis ---------------------------------------------------------------------------
 
-// One block per supernode chunk: checks the layout (row a+t: the w-t triangle columns a+t..b-1
-// first, then exactly row a's rectangle columns) and records the rectangle width.
+// One block per supernode chunk [a, b), w = b - a.  Two layouts are accepted:
+//   * exact (the layout supernodal_upper and ccs2ccs_pad rely on, core.cpp:53-78,136-161): row
+//     a+t holds the w-t triangle columns a+t..b-1 first, then exactly row a's rectangle columns;
+//   * skyline: every row a+t is one contiguous column range starting at its diagonal (a banded
+//     factor stored with its explicit zeros); a row that ends inside the triangle leaves zeros
+//     there, the rectangle is the contiguous range b..b+m-1 with m the longest row's reach past b,
+//     and shorter rows read zero in it.
+// Records the rectangle width and the layout (0 exact, 1 skyline).
 __global__ void k_sn_check(int S, const int* __restrict__ sstart, const int* __restrict__ rp,
-                           const int* __restrict__ col, int* __restrict__ m_out, Ctl* ctl) {
+                           const int* __restrict__ col, int* __restrict__ m_out, int* __restrict__ kind_out,
+                           Ctl* ctl) {
     for (int s = blockIdx.x; s < S; s += gridDim.x) {
         const int a = sstart[s], b = sstart[s + 1], w = b - a;
         const int m = rp[a + 1] - rp[a] - w;
-        if (threadIdx.x == 0) m_out[s] = m < 0 ? 0 : m;
-        if (m < 0) { if (threadIdx.x == 0) record_error(ctl, SPTRSV_ERR_SUPERNODES); continue; }
+        bool exact = m >= 0;
         const int* rect0 = col + rp[a] + w;
-        for (int t = 0; t < w; ++t) {
+        for (int t = 0; t < w && exact; ++t) {
             const int i = a + t, base = rp[i];
-            if (rp[i + 1] - base != (w - t) + m) { if (threadIdx.x == 0) record_error(ctl, SPTRSV_ERR_SUPERNODES); break; }
+            if (rp[i + 1] - base != (w - t) + m) { exact = false; break; }
             bool bad = false;
             for (int q = threadIdx.x; q < w - t; q += blockDim.x) bad |= col[base + q] != i + q;
             for (int q = threadIdx.x; q < m; q += blockDim.x) bad |= col[base + (w - t) + q] != rect0[q];
-            if (__syncthreads_or(bad)) { if (threadIdx.x == 0) record_error(ctl, SPTRSV_ERR_SUPERNODES); break; }
+            if (__syncthreads_or(bad)) exact = false;
+        }
+        if (exact) {
+            if (threadIdx.x == 0) { m_out[s] = m; kind_out[s] = 0; }
+            continue;
+        }
+        bool sky = true;
+        int msky = 0;
+        for (int t = 0; t < w && sky; ++t) {
+            const int i = a + t, base = rp[i], len = rp[i + 1] - base;
+            if (len < 1) { sky = false; break; }
+            msky = max(msky, len - (w - t));
+            bool bad = false;
+            for (int q = threadIdx.x; q < len; q += blockDim.x) bad |= col[base + q] != i + q;
+            if (__syncthreads_or(bad)) sky = false;
+        }
+        if (threadIdx.x == 0) {
+            m_out[s] = sky ? msky : 0;
+            kind_out[s] = 1;
+            if (!sky) record_error(ctl, SPTRSV_ERR_SUPERNODES);
         }
     }
 }
 
 __global__ void k_sn_rectcols(int S, const int* __restrict__ sstart, const int* __restrict__ rp,
                               const int* __restrict__ col, const int* __restrict__ roff,
-                              int* __restrict__ rect_cols) {
+                              const int* __restrict__ kind, int* __restrict__ rect_cols) {
     for (int s = blockIdx.x; s < S; s += gridDim.x) {
         const int a = sstart[s], w = sstart[s + 1] - a;
         const int m = roff[s + 1] - roff[s];
-        for (int q = threadIdx.x; q < m; q += blockDim.x) rect_cols[roff[s] + q] = col[rp[a] + w + q];
+        if (kind[s] == 0) {
+            for (int q = threadIdx.x; q < m; q += blockDim.x) rect_cols[roff[s] + q] = col[rp[a] + w + q];
+        } else {
+            for (int q = threadIdx.x; q < m; q += blockDim.x) rect_cols[roff[s] + q] = a + w + q;
+        }
     }
 }
 
@@ -84,8 +114,9 @@ __global__ void __launch_bounds__(256) k_sn_tinv(int S, const int* __restrict__ 
         __syncwarp();
         for (int r = j - 1; r >= 0; --r) {
             const int base = rp[a + r] - r;
+            const int lim = min(j, rp[a + r + 1] - base - 1);  // a skyline row may end inside the triangle
             double sum = 0.0;
-            for (int c = r + 1 + lane; c <= j; c += 32) sum = fma(val[base + c], x[c], sum);
+            for (int c = r + 1 + lane; c <= lim; c += 32) sum = fma(val[base + c], x[c], sum);
             sum = warp_sum(sum);
             if (lane == 0) x[r] = -sum / val[rp[a + r]];
             __syncwarp();
@@ -116,15 +147,20 @@ __global__ void k_sn_w(int S, const int* __restrict__ sstart, const int* __restr
         const double* g = G + goff[s];
         const int L = ld[s];
         double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+        // Rect[c][k] = val[rp[a+c] + (w - c) + k] while that position is inside row a+c (in the
+        // exact layout always; a skyline row shorter than the rectangle reads zero past its end)
+        auto rect = [&](int c) -> double {
+            const int base = rp[a + c], off = (w - c) + k;
+            return off < rp[a + c + 1] - base ? val[base + off] : 0.0;
+        };
         int c = r;
-        // Rect[c][k] = val[rp[a+c] + (w - c) + k]
         for (; c + 3 < w; c += 4) {
-            s0 = fma(g[(size_t)r * L + c], val[rp[a + c] + (w - c) + k], s0);
-            s1 = fma(g[(size_t)r * L + c + 1], val[rp[a + c + 1] + (w - c - 1) + k], s1);
-            s2 = fma(g[(size_t)r * L + c + 2], val[rp[a + c + 2] + (w - c - 2) + k], s2);
-            s3 = fma(g[(size_t)r * L + c + 3], val[rp[a + c + 3] + (w - c - 3) + k], s3);
+            s0 = fma(g[(size_t)r * L + c], rect(c), s0);
+            s1 = fma(g[(size_t)r * L + c + 1], rect(c + 1), s1);
+            s2 = fma(g[(size_t)r * L + c + 2], rect(c + 2), s2);
+            s3 = fma(g[(size_t)r * L + c + 3], rect(c + 3), s3);
         }
-        for (; c < w; ++c) s0 = fma(g[(size_t)r * L + c], val[rp[a + c] + (w - c) + k], s0);
+        for (; c < w; ++c) s0 = fma(g[(size_t)r * L + c], rect(c), s0);
         G[goff[s] + (size_t)r * L + w + k] = -((s0 + s1) + (s2 + s3));
     }
 }
@@ -212,32 +248,6 @@ __global__ void __launch_bounds__(128) k_sn_solve_f64(SnArgs A, const double* __
 }
 
 // BF16x3 tensor-core panel product, FP32 output (the mixed path's inner solve).
-__device__ __forceinline__ void mma_bf16(float* c, const uint32_t* a, uint32_t b0, uint32_t b1) {
-    asm volatile(
-        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-        "{%0,%1,%2,%3};\n"
-        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
-}
-
-__device__ __forceinline__ uint32_t pack_bf16(__nv_bfloat16 lo_k, __nv_bfloat16 hi_k) {
-    return (uint32_t)__bfloat16_as_ushort(lo_k) | ((uint32_t)__bfloat16_as_ushort(hi_k) << 16);
-}
-
-// A fragment (16 x 16, row-major) of G rows [row0, row0+16), columns [k0, k0+16); rows past
-// `nrows` and columns past `K` read as zero (G is padded to a multiple of 16 columns).
-__device__ __forceinline__ void load_a(const __nv_bfloat16* g, int L, int row0, int nrows, int k0, uint32_t* a) {
-    const int lane = threadIdx.x & 31;
-    const int r = lane >> 2, c = (lane & 3) * 2;
-    const int ra = row0 + r, rb = row0 + r + 8;
-    const uint32_t* pa = reinterpret_cast<const uint32_t*>(g + (size_t)ra * L + k0 + c);
-    const uint32_t* pb = reinterpret_cast<const uint32_t*>(g + (size_t)rb * L + k0 + c);
-    a[0] = ra < nrows ? __ldg(pa) : 0u;
-    a[1] = rb < nrows ? __ldg(pb) : 0u;
-    a[2] = ra < nrows ? __ldg(pa + 4) : 0u;
-    a[3] = rb < nrows ? __ldg(pb + 4) : 0u;
-}
-
 __global__ void __launch_bounds__(128) k_sn_solve_bf16x3(SnArgs A, const __nv_bfloat16* __restrict__ Ghi,
                                                          const __nv_bfloat16* __restrict__ Glo, int rhs,
                                                          const float* __restrict__ b, float* x, Ctl* ctl,
@@ -350,10 +360,11 @@ int Handle::set_supernodes(int sn, const int* snodes_host) {
     }
     const int S = (int)ss.size() - 1;
     int rc;
-    if ((rc = sn_start.ensure(sizeof(int) * (S + 1))) || (rc = sn_m.ensure(sizeof(int) * S))) return rc;
+    if ((rc = sn_start.ensure(sizeof(int) * (S + 1))) || (rc = sn_m.ensure(sizeof(int) * 2 * S))) return rc;
     CUDA_TRY(cudaMemcpyAsync(sn_start.p, ss.data(), sizeof(int) * (S + 1), cudaMemcpyHostToDevice, st));
     if ((rc = reset_ctl())) return rc;
-    k_sn_check<<<std::min(S, sm_count * 8), 128, 0, st>>>(S, sn_start.as<int>(), rp, col, sn_m.as<int>(), ctl);
+    k_sn_check<<<std::min(S, sm_count * 8), 128, 0, st>>>(S, sn_start.as<int>(), rp, col, sn_m.as<int>(),
+                                                         sn_m.as<int>() + S, ctl);
     ++launches;
     CUDA_TRY(cudaGetLastError());
     Ctl c{};
@@ -395,7 +406,7 @@ int Handle::set_supernodes(int sn, const int* snodes_host) {
                              cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaMemsetAsync(sn_G.p, 0, sizeof(double) * (size_t)gtot, st));
     k_sn_rectcols<<<std::min(S, sm_count * 8), 128, 0, st>>>(S, sn_start.as<int>(), rp, col, sn_roff.as<int>(),
-                                                            sn_rect.as<int>());
+                                                            sn_m.as<int>() + S, sn_rect.as<int>());
     k_sn_tinv<<<sm_count * 8, 256, 0, st>>>(S, sn_start.as<int>(), rp, val, sn_goff.as<long long>(), sn_ld.as<int>(),
                                             sn_colbase.as<int>(), colbase[S], sn_G.as<double>());
     launches += 2;

@@ -244,3 +244,71 @@ def supernodal_case(g=40, rhs=1, seed=3):
     m = laplace3d_nd_cholesky(g)
     xs = uniform((int(seed) + XSTAR_SALT) % (1 << 64), m.n * rhs)
     return m, xs, spmv(m, xs, rhs)
+
+
+# --------------------------------------------------------------------------------------------
+# The batched uneven mix
+
+class Mix:
+    """A packed host arena of independent systems (see csrc/gen.cpp, sptrsv_gen_mix): per-system
+    n, rhs, kind (0 Laplacian factor, 1 random), nnz and offsets; the concatenated local row
+    pointers (int64), columns, values; x* and b = U x* (row-major n x rhs per system).  The arrays
+    are views of generator-owned memory, released by close()."""
+
+    _FIELDS = [("n", np.int32), ("rhs", np.int32), ("kind", np.int32), ("nnz", np.int64), ("rp_off", np.int64),
+               ("nz_off", np.int64), ("xb_off", np.int64), ("row_ptr", np.int64), ("col", np.int32),
+               ("val", np.float64), ("xstar", np.float64), ("b", np.float64), ("mean", np.float64)]
+
+    def __init__(self, h):
+        self._h = h
+        G = _lib.gen()
+        for k, (name, dt) in enumerate(self._FIELDS):
+            p = ctypes.c_void_p()
+            ln = ctypes.c_int64()
+            if G.sptrsv_gen_mix_array(h, k, ctypes.byref(p), ctypes.byref(ln)):
+                raise RuntimeError("mix array %s" % name)
+            if ln.value == 0:
+                arr = np.empty(0, dtype=dt)
+            else:
+                buf = (ctypes.c_char * (ln.value * np.dtype(dt).itemsize)).from_address(p.value)
+                arr = np.frombuffer(buf, dtype=dt)
+            setattr(self, name, arr)
+        self.count = len(self.n)
+
+    def system(self, s):
+        """System s as a Csr with its x* and b (row-major n x rhs): views of the mix's memory,
+        valid until close()."""
+        rp = self.row_ptr[self.rp_off[s]:self.rp_off[s + 1]]
+        col = self.col[self.nz_off[s]:self.nz_off[s + 1]]
+        val = self.val[self.nz_off[s]:self.nz_off[s + 1]]
+        xs = self.xstar[self.xb_off[s]:self.xb_off[s + 1]]
+        b = self.b[self.xb_off[s]:self.xb_off[s + 1]]
+        return Csr(rp, col, val), xs, b
+
+    def close(self):
+        if self._h:
+            for name, _ in self._FIELDS:
+                setattr(self, name, None)
+            _lib.gen().sptrsv_gen_mix_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def mix(count=512, seed=2, nmin=1000, nmax=200_000, mean_lo=4.0, mean_hi=16.0, rhs_max=16, threads=0):
+    """The batched uneven mix: `count` systems, n log-uniform in [nmin, nmax], even-indexed ones
+    2D-Laplacian Cholesky factors (grid side round(sqrt n)), odd-indexed ones random diagonally
+    dominant (Poisson mean U[mean_lo, mean_hi], p_near 0.9, band 64), RHS U{1..rhs_max}.
+    count 512, seed 2, n in [1k, 200k], mean in [4, 16], rhs_max 16 is the batched workload."""
+    import os
+    if threads <= 0:
+        threads = os.cpu_count() or 1
+    h = _lib.gen().sptrsv_gen_mix(int(count), int(seed), int(nmin), int(nmax), float(mean_lo), float(mean_hi),
+                                  int(rhs_max), int(threads))
+    if not h:
+        raise ValueError("mix generator rejected its arguments")
+    return Mix(h)

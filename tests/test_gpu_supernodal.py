@@ -86,3 +86,21 @@ def test_partition_without_shared_rectangle_is_rejected(solver):
     with pytest.raises(sp.SptrsvError) as e:
         solver.set_supernodes(np.array([0, 10, 3999], dtype=np.int32))
     assert e.value.status == -14
+
+
+@pytest.mark.parametrize("width", [16, 64, 300])
+@pytest.mark.parametrize("rhs", [1, 8])
+def test_band_factor_skyline_panels(orc, solver, width, rhs):
+    """A banded factor stored with its explicit zeros, cut into uniform row chunks: every row is a
+    contiguous range from its diagonal (skyline), so each chunk is a dense panel whose rectangle
+    is the longest row's reach; shorter rows read zero there."""
+    m = gen.laplace2d_cholesky(30)
+    sn = np.unique(np.append(np.arange(0, m.n, width), m.n)).astype(np.int32)
+    solver.analyse(m.row_ptr, m.col, m.val).set_supernodes(sn)
+    b = gen.uniform(17 + rhs, m.n * rhs)
+    ref = orc.base_gauss_upper(m.row_ptr.astype(np.uint64), m.col, m.val, b, rhs)
+    x = solver.solve(b, rhs=rhs, schedule="supernodal")
+    assert elem_err(x, ref) <= ELEM_TOL
+    x = solver.solve(b, rhs=rhs, schedule="supernodal", precision="mixed", max_refine=20)
+    assert solver.last_refine()[1] <= RES_TOL
+    assert elem_err(x, ref) <= MIXED_ELEM_TOL
