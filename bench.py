@@ -53,8 +53,9 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=2_000_000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="irregular2m", choices=["irregular2m", "batch"],
-                    help="irregular2m: the 2M-row single solve (default); batch: the 512-system uneven mix")
+    ap.add_argument("--workload", default="irregular2m", choices=["irregular2m", "batch", "supernodal"],
+                    help="irregular2m: the 2M-row single solve (default); batch: the 512-system uneven mix; "
+                         "supernodal: the 40^3 nested-dissection factor at 1/8/32/128 right-hand sides")
     ap.add_argument("--count", type=int, default=512, help="batch: number of systems")
     ap.add_argument("--nmax", type=int, default=200_000, help="batch: largest n")
     return ap.parse_args()
@@ -428,6 +429,8 @@ def run_ours(args, dist):
                    "parallelism": f"replicas x{dist.ws}"},
         "hbm_gbs": fb * value / dist.ws / 1e9,
         "hbm_frac": fb * value / dist.ws / 1e9 / peak,
+        "us_per_solve": 1e6 / (value / dist.ws),
+        "gflops": (2 * (nnz - n) + n) * value / 1e9,
         "rel_residual": rel_res, "refine_steps": steps_ref, "inner_sweeps": sweeps_ref,
         "max_abs_err_vs_xstar": err_xstar,
         "plain_fp64_syncfree": {"solves_per_s": plain_sps, "ms_per_solve": 1e3 / plain_sps,
@@ -595,6 +598,8 @@ def run_batch(args, dist):
                    "parallelism": f"replicas x{dist.ws}"},
         "solve_unit": "one system with all its right-hand sides",
         "hbm_gbs": fb / (ms_step * 1e-3) / 1e9,
+        "us_per_solve": 1e3 * ms_step / args.count,
+        "gflops": float(np.sum((2 * (M.nnz - M.n) + M.n) * M.rhs)) / (ms_step * 1e-3) / 1e9,
         "plain_fp64_syncfree": {"solves_per_s": plain_sps, "ms_per_batch": 1e3 * args.count / plain_sps,
                                 "hbm_gbs": fb * plain_sps / args.count / 1e9},
         "speedup_vs_plain": value / dist.ws / plain_sps,
@@ -611,6 +616,70 @@ def run_batch(args, dist):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------------------------------
+def run_supernodal(args, dist):
+    """The 3D-Laplacian nested-dissection factor (40^3, supernodes 8-400): device time per solve
+    (CUDA events, L2 flushed, best of `steps`) of the FP64 supernodal schedule, the mixed one
+    (BF16x3 tensor-core panels + FP64 refinement) and the plain FP64 sync-free schedule, at
+    1, 8, 32 and 128 right-hand sides, beside the serial CPU solve."""
+    import ctypes
+    import sptrsv_gb300 as sp
+    from sptrsv_gb300 import gen
+    from oracle import oracle
+    if dist.rank != 0:
+        return
+    L = sp._lib.lib()
+    t_gen = time.time()
+    m = gen.laplace3d_nd_cholesky(40)
+    t_gen = time.time() - t_gen
+    s = sp.Solver(dist.local)
+    s.analyse(m.row_ptr, m.col, m.val).set_supernodes(m.snodes)
+    h = s.handle
+    rows = []
+    rpu = m.row_ptr.astype(np.uint64)
+    for rhs in (1, 8, 32, 128):
+        b = gen.uniform(3 + rhs, m.n * rhs)
+        ref = oracle.base_gauss_upper(rpu, m.col, m.val, b, rhs)
+        nb = 8 * m.n * rhs
+        d_b, d_x = ctypes.c_void_p(), ctypes.c_void_p()
+        assert L.sptrsv_device_alloc(h, nb, ctypes.byref(d_b)) == 0
+        assert L.sptrsv_device_alloc(h, nb, ctypes.byref(d_x)) == 0
+        L.sptrsv_copy_h2d(h, d_b, b.ctypes.data, nb)
+        row = {"rhs": rhs}
+        for name, o, reps in (("fp64_supernodal", sp.make_opts(schedule="supernodal"), args.steps),
+                              ("mixed_supernodal_bf16x3", sp.make_opts(schedule="supernodal", precision="mixed"),
+                               args.steps),
+                              ("plain_fp64_syncfree", sp.make_opts(schedule="syncfree_block" if rhs == 1 else
+                                                                   "syncfree_warp"), 1 if rhs > 1 else 3)):
+            x = np.empty(m.n * rhs)
+            best = None
+            for k in range(1 + reps):
+                L.sptrsv_flush_l2(h)
+                L.sptrsv_timer_begin(h)
+                rc = L.sptrsv_solve(h, ctypes.byref(o), d_b, d_x, rhs, sp.COL_MAJOR)
+                fms = ctypes.c_float()
+                L.sptrsv_timer_end(h, ctypes.byref(fms))
+                if rc or s.sync():
+                    raise SystemExit(f"{name} failed")
+                if k > 0:
+                    best = fms.value if best is None else min(best, fms.value)
+            L.sptrsv_copy_d2h(h, x.ctypes.data, d_x, nb)
+            s.sync()
+            row[name] = {"ms": best, "elem_err": oracle.max_elem_rel_error(ref, x, 1e-12),
+                         "rel_residual": oracle.rel_residual(rpu, m.col, m.val, x, b, rhs)}
+        t0 = time.perf_counter()
+        oracle.base_gauss_upper(rpu, m.col, m.val, b, rhs)
+        row["cpu_serial_ms"] = 1e3 * (time.perf_counter() - t0)
+        rows.append(row)
+        L.sptrsv_device_free(h, d_b)
+        L.sptrsv_device_free(h, d_x)
+    info = s.info()
+    print(json.dumps({"workload": "supernodal: 7-point 3D Laplacian Cholesky factor, 40^3 grid, nested dissection "
+                                  "(8^3 leaves), supernodes <= 400 rows",
+                      "n": m.n, "nnz": m.nnz, "supernodes": int(len(m.snodes) - 1), "max_level": info["max_level"],
+                      "generation_s": t_gen, "rows": rows}), flush=True)
+
+
 def main():
     args = parse()
     dist = Dist()
@@ -619,6 +688,8 @@ def main():
             run_reference(args, dist)
         elif args.workload == "batch":
             run_batch(args, dist)
+        elif args.workload == "supernodal":
+            run_supernodal(args, dist)
         else:
             run_ours(args, dist)
     finally:

@@ -140,6 +140,11 @@ SPTRSV_API int sptrsv_set_supernodes(sptrsv_handle h, int sn, const int* superno
 #define SPTRSV_FEATURES 24
 SPTRSV_API int sptrsv_autotune(sptrsv_handle h, int rhs, float cap_ms, int reps, float* cand_ms, int* best_id,
                                sptrsv_opts* best);
+/* As sptrsv_autotune, and a candidate still running after max(abort_ms, 20 x the best time so far)
+ * is cancelled (its spins see the abort flag and return): its time is then a lower bound and
+ * censored[id] = 1.  abort_ms = 0 never cancels. */
+SPTRSV_API int sptrsv_autotune_bounded(sptrsv_handle h, int rhs, float cap_ms, int reps, float abort_ms,
+                                       float* cand_ms, int* censored, int* best_id, sptrsv_opts* best);
 /* Options of candidate `id` of the autotuner's table. */
 SPTRSV_API int sptrsv_candidate(int id, sptrsv_opts* o);
 /* 1 when candidate `id` can run on the resident matrix with `rhs` columns. */

@@ -195,13 +195,16 @@ class Solver:
         _check(_lib.lib().sptrsv_set_supernodes(self._h, len(sn) - 1, sn), "set_supernodes")
         return self
 
-    def autotune(self, rhs=1, cap_ms=50.0, reps=2):
-        """Exhaustive tuning over the candidate table; returns (best id, times in ms per candidate).
-        The winner is cached for this RHS class and used by schedule="auto"."""
+    def autotune(self, rhs=1, cap_ms=50.0, reps=2, abort_ms=0.0, with_censored=False):
+        """Exhaustive tuning over the candidate table; returns (best id, times in ms per candidate)
+        and, with_censored, the flags of candidates cancelled after abort_ms (their times are lower
+        bounds).  The winner is cached for this RHS class and used by schedule="auto"."""
         ms = np.zeros(N_CANDIDATES, dtype=np.float32)
+        cens = np.zeros(N_CANDIDATES, dtype=np.int32)
         best = ctypes.c_int(-1)
-        _check(_lib.lib().sptrsv_autotune(self._h, rhs, cap_ms, reps, ms, ctypes.byref(best), None), "autotune")
-        return best.value, ms
+        _check(_lib.lib().sptrsv_autotune_bounded(self._h, rhs, cap_ms, reps, float(abort_ms), ms, cens,
+                                                  ctypes.byref(best), None), "autotune")
+        return (best.value, ms, cens) if with_censored else (best.value, ms)
 
     def features(self, rhs=1):
         f = np.zeros(N_FEATURES, dtype=np.float32)

@@ -77,6 +77,9 @@ C_API = {
     "sptrsv_set_supernodes": ([c_vp, c_int, i32], c_int),
     "sptrsv_autotune": ([c_vp, c_int, ctypes.c_float, c_int, _P(dtype=np.float32, flags="C_CONTIGUOUS"), _c_int_p,
                          ctypes.POINTER(Opts)], c_int),
+    "sptrsv_autotune_bounded": ([c_vp, c_int, ctypes.c_float, c_int, ctypes.c_float,
+                                 _P(dtype=np.float32, flags="C_CONTIGUOUS"), i32, _c_int_p, ctypes.POINTER(Opts)],
+                                c_int),
     "sptrsv_candidate": ([c_int, ctypes.POINTER(Opts)], c_int),
     "sptrsv_candidate_applicable": ([c_vp, c_int, c_int], c_int),
     "sptrsv_features": ([c_vp, c_int, _P(dtype=np.float32, flags="C_CONTIGUOUS")], c_int),

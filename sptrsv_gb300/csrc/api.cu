@@ -711,6 +711,8 @@ int Handle::set_matrix_host(int n_, int64_t nnz_, const int64_t* rp_h, const int
 }
 
 Handle::~Handle() {
+    if (cancel_st) cudaStreamDestroy(cancel_st);
+    if (cancel_flag) cudaFreeHost(cancel_flag);
     drop_graphs();
     for (cudaEvent_t e : prof_ev) cudaEventDestroy(e);
     if (prof0) cudaEventDestroy(prof0);

@@ -300,19 +300,38 @@ __global__ void __launch_bounds__(256) k_b_pull(BArgs A, const int2* __restrict_
             const int nc = min(32, r - c0);
             int groups, g, c;
             lane_split(nc, groups, g, c);
-            T sum = 0;
+            T s0 = 0, s1 = 0, s2 = 0, s3 = 0;
             bool lok = true;
             if (g < groups) {
-                for (int k = beg + 1 + g; k < end; k += groups) {
+                // entries from the farthest column down to the nearest: the far ones were solved
+                // long ago, so when the nearest (the last to be published) arrives only its own
+                // product is left; four loads issue together and only a pending value waits
+                int k = end - 1 - g;
+                for (; lok && k - 3 * groups > beg; k -= 4 * groups) {
+                    const T* p0 = xx + (size_t)__ldg(cl + k) * r + c0 + c;
+                    const T* p1 = xx + (size_t)__ldg(cl + k - groups) * r + c0 + c;
+                    const T* p2 = xx + (size_t)__ldg(cl + k - 2 * groups) * r + c0 + c;
+                    const T* p3 = xx + (size_t)__ldg(cl + k - 3 * groups) * r + c0 + c;
+                    T v0 = ld_relaxed(p0), v1 = ld_relaxed(p1), v2 = ld_relaxed(p2), v3 = ld_relaxed(p3);
+                    if (Pend<T>::is(v0)) lok = wait_ready<T>(p0, v0, ctl, A.budget);
+                    if (lok && Pend<T>::is(v1)) lok = wait_ready<T>(p1, v1, ctl, A.budget);
+                    if (lok && Pend<T>::is(v2)) lok = wait_ready<T>(p2, v2, ctl, A.budget);
+                    if (lok && Pend<T>::is(v3)) lok = wait_ready<T>(p3, v3, ctl, A.budget);
+                    s0 = fma(__ldg(vl + k), v0, s0);
+                    s1 = fma(__ldg(vl + k - groups), v1, s1);
+                    s2 = fma(__ldg(vl + k - 2 * groups), v2, s2);
+                    s3 = fma(__ldg(vl + k - 3 * groups), v3, s3);
+                }
+                for (; lok && k > beg; k -= groups) {
                     T xv;
                     if (!wait_ready<T>(xx + (size_t)__ldg(cl + k) * r + c0 + c, xv, ctl, A.budget)) {
                         lok = false;
                         break;
                     }
-                    sum = fma(__ldg(vl + k), xv, sum);
+                    s0 = fma(__ldg(vl + k), xv, s0);
                 }
             }
-            sum = group_sum(sum, groups, nc);
+            T sum = group_sum((s0 + s1) + (s2 + s3), groups, nc);
             if (__any_sync(0xffffffffu, !lok)) { ok = false; break; }
             if (lane < nc) {
                 const size_t o = (size_t)i * r + c0 + lane;
@@ -451,10 +470,16 @@ __global__ void __launch_bounds__(256) k_b_jacobi(BArgs A, SegList rows) {
                 const int nc = min(32, r - c0);
                 int groups, g, c;
                 lane_split(nc, groups, g, c);
-                float sum = 0.f;
-                if (k > 0 && g < groups)
-                    for (int q = beg + 1 + g; q < end; q += groups) sum = fmaf(vl[q], so[(size_t)cl[q] * r + c0 + c], sum);
-                sum = group_sum(sum, groups, nc);
+                float s0 = 0.f, s1 = 0.f;
+                if (k > 0 && g < groups) {
+                    int q = beg + 1 + g;
+                    for (; q + groups < end; q += 2 * groups) {
+                        s0 = fmaf(vl[q], so[(size_t)cl[q] * r + c0 + c], s0);
+                        s1 = fmaf(vl[q + groups], so[(size_t)cl[q + groups] * r + c0 + c], s1);
+                    }
+                    if (q < end) s0 = fmaf(vl[q], so[(size_t)cl[q] * r + c0 + c], s0);
+                }
+                const float sum = group_sum(s0 + s1, groups, nc);
                 if (lane < nc) {
                     const size_t o = (size_t)i * r + c0 + lane;
                     const float dn = (rr[o] - sum) * dinv;
@@ -497,10 +522,18 @@ __global__ void __launch_bounds__(256) k_b_residual(BArgs A, SegList rows) {
                 const int nc = min(32, r - c0);
                 int groups, g, c;
                 lane_split(nc, groups, g, c);
-                double sum = 0.0;
-                if (g < groups)
-                    for (int q = beg + g; q < end; q += groups) sum = fma(__ldg(vl + q), xx[(size_t)__ldg(cl + q) * r + c0 + c], sum);
-                sum = group_sum(sum, groups, nc);
+                double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+                if (g < groups) {
+                    int q = beg + g;
+                    for (; q + 3 * groups < end; q += 4 * groups) {
+                        s0 = fma(__ldg(vl + q), xx[(size_t)__ldg(cl + q) * r + c0 + c], s0);
+                        s1 = fma(__ldg(vl + q + groups), xx[(size_t)__ldg(cl + q + groups) * r + c0 + c], s1);
+                        s2 = fma(__ldg(vl + q + 2 * groups), xx[(size_t)__ldg(cl + q + 2 * groups) * r + c0 + c], s2);
+                        s3 = fma(__ldg(vl + q + 3 * groups), xx[(size_t)__ldg(cl + q + 3 * groups) * r + c0 + c], s3);
+                    }
+                    for (; q < end; q += groups) s0 = fma(__ldg(vl + q), xx[(size_t)__ldg(cl + q) * r + c0 + c], s0);
+                }
+                const double sum = group_sum((s0 + s1) + (s2 + s3), groups, nc);
                 if (lane < nc) {
                     const size_t o = (size_t)i * r + c0 + lane;
                     const double rv = bb[o] - sum;
@@ -942,9 +975,10 @@ int Batch::build_graph(int mode, const double* b, double* x, cudaGraphExec_t* ou
     CUDA_TRY(cudaGraphCreate(&g, 0));
     cudaGraphConditionalHandle ho = 0, hi = 0;
     cudaError_t e = cudaSuccess;
-    if (mode == 1) {
+    // a conditional handle exists only with the WHILE node that reads it
+    if (mode == 1 && mixed_el.nseg) {
         e = cudaGraphConditionalHandleCreate(&ho, g, 1, cudaGraphCondAssignDefault);
-        if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&hi, g, 0, cudaGraphCondAssignDefault);
+        if (e == cudaSuccess && jac_rows.nseg) e = cudaGraphConditionalHandleCreate(&hi, g, 0, cudaGraphCondAssignDefault);
     }
     if (e != cudaSuccess) { cudaGraphDestroy(g); return set_cuda_error(e, "batch conditional handle"); }
     auto add_while = [&](cudaGraph_t parent, cudaGraphConditionalHandle h, cudaGraph_t* body) -> cudaError_t {
@@ -1351,6 +1385,15 @@ int sptrsv_batch_features(sptrsv_batch bh, int s, float* f) {
     H.col = B->col.as<int>() + S.nz0;
     H.val = B->val.as<double>() + S.nz0;
     if ((rc = H.analyse())) return rc;
+    if (B->panel_ok[s] != 0) {
+        // the panel structure the batched path would use (uniform 64-row chunks), as in the
+        // selector's training data for banded factors
+        std::vector<int> sn;
+        for (int a = 0; a < S.n; a += 64) sn.push_back(a);
+        sn.push_back(S.n);
+        rc = H.set_supernodes((int)sn.size() - 1, sn.data());
+        if (rc && rc != SPTRSV_ERR_SUPERNODES) return rc;
+    }
     rc = H.features(f, S.rhs);
     H.drop_matrix();
     return rc;

@@ -121,7 +121,11 @@ struct Handle {
     sptrsv_opts tuned[4];
     bool tuned_valid[4] = {false, false, false, false};
     bool applicable(const sptrsv_opts& o, int rhs) const;
-    int autotune(int rhs, float cap_ms, int reps, float* ms_out, int* best_id);
+    int autotune(int rhs, float cap_ms, int reps, float abort_ms, float* ms_out, int* censored_out, int* best_id);
+    int timed_candidate(const sptrsv_opts& o, int rhs, float abort_ms, float* ms, bool* censored);
+    int cancel_until_idle();
+    cudaStream_t cancel_st = nullptr;
+    int* cancel_flag = nullptr;  // pinned host 1
     int features(float* f, int rhs);
     int solve(const sptrsv_opts* o, const double* b, double* x, int rhs, int layout);
     int sync();

@@ -11,8 +11,10 @@
 // The features (24 values, log-scaled where sizes are concerned) describe the matrix: size,
 // density, row-length moments, dependency depth, level-width histogram, dominance of the
 // diagonal, supernode-width histogram, and the number of right-hand sides.
+#include <chrono>
 #include <cmath>
 #include <cstring>
+#include <thread>
 #include <vector>
 #include "common.cuh"
 #include "kernels.cuh"
@@ -69,7 +71,63 @@ __global__ void k_fill_uniform(size_t count, uint64_t seed, double* __restrict__
     }
 }
 
-int Handle::autotune(int rhs, float cap_ms, int reps, float* ms_out, int* best_id) {
+// Raise the abort flag of the running solve from a second stream (the copy engine runs beside the
+// solve's kernels); every spin and ticket loop polls it and returns, so the solve ends early with
+// a meaningless result.  Re-raised until the solve's stream drains, in case a graph's own reset of
+// the control block ran after the first raise.
+int Handle::cancel_until_idle() {
+    if (!cancel_st) CUDA_TRY(cudaStreamCreateWithFlags(&cancel_st, cudaStreamNonBlocking));
+    if (!cancel_flag) {
+        CUDA_TRY(cudaHostAlloc((void**)&cancel_flag, sizeof(int), cudaHostAllocDefault));
+        *cancel_flag = 1;
+    }
+    for (int k = 0; k < 100000; ++k) {
+        CUDA_TRY(cudaMemcpyAsync(&ctl->abort, cancel_flag, sizeof(int), cudaMemcpyHostToDevice, cancel_st));
+        CUDA_TRY(cudaStreamSynchronize(cancel_st));
+        const cudaError_t q = cudaStreamQuery(st);
+        if (q == cudaSuccess) return 0;
+        if (q != cudaErrorNotReady) return set_cuda_error(q, "cancel");
+        std::this_thread::sleep_for(std::chrono::microseconds(200));
+    }
+    CUDA_TRY(cudaStreamSynchronize(st));
+    return 0;
+}
+
+// One timed solve of candidate o.  With abort_ms > 0 the host watches the solve and cancels it
+// once it has run longer than abort_ms: the time is then a lower bound and *censored is set.
+int Handle::timed_candidate(const sptrsv_opts& o, int rhs, float abort_ms, float* ms, bool* censored) {
+    *censored = false;
+    *ms = INFINITY;
+    CUDA_TRY(cudaEventRecord(ev0, st));
+    int rc = solve(&o, tune_b.as<double>(), tune_x.as<double>(), rhs, SPTRSV_ROW_MAJOR);
+    if (rc) return rc;
+    CUDA_TRY(cudaEventRecord(ev1, st));
+    if (abort_ms > 0.f) {
+        const auto t0 = std::chrono::steady_clock::now();
+        for (;;) {
+            const cudaError_t q = cudaEventQuery(ev1);
+            if (q == cudaSuccess) break;
+            if (q != cudaErrorNotReady) return set_cuda_error(q, "tune query");
+            const float el = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
+            if (el > abort_ms) {
+                if ((rc = cancel_until_idle())) return rc;
+                (void)sync();  // status of a cancelled run is meaningless; clears it
+                *censored = true;
+                *ms = el;
+                return 0;
+            }
+            std::this_thread::sleep_for(std::chrono::microseconds(50));
+        }
+    }
+    if ((rc = sync())) return rc;
+    CUDA_TRY(cudaEventElapsedTime(ms, ev0, ev1));
+    return 0;
+}
+
+// Exhaustive tuning.  Candidates run in a fixed order that usually finds a fast one early; with
+// abort_ms > 0 a candidate still running after max(abort_ms, 20 x the best so far) is cancelled
+// and reported as censored (its time a lower bound).
+int Handle::autotune(int rhs, float cap_ms, int reps, float abort_ms, float* ms_out, int* censored_out, int* best_id) {
     if (!analysed) return SPTRSV_ERR_NO_ANALYSIS;
     int rc;
     if ((rc = ensure_levels())) return rc;
@@ -80,40 +138,37 @@ int Handle::autotune(int rhs, float cap_ms, int reps, float* ms_out, int* best_i
     CUDA_TRY(cudaGetLastError());
     int K = 0;
     const sptrsv_opts* cand = tune_candidates(&K);
+    static const int order[SPTRSV_TUNE_CANDIDATES] = {7, 14, 11, 12, 0, 8, 13, 2, 3, 4, 9, 10, 6, 5, 1, 15};
     float best = INFINITY;
     int bid = -1;
-    for (int k = 0; k < K; ++k) {
+    for (int q = 0; q < K; ++q) {
+        const int k = order[q];
         float t = INFINITY;
+        bool cens = false;
         if (applicable(cand[k], rhs)) {
-            sptrsv_opts o = cand[k];
+            const sptrsv_opts o = cand[k];
+            const float lim = abort_ms > 0.f ? std::max(abort_ms, std::isfinite(best) ? 20.f * best : abort_ms) : 0.f;
             float first = INFINITY;
-            // first run: allocations, graph capture and a first timing
-            CUDA_TRY(cudaEventRecord(ev0, st));
-            rc = solve(&o, tune_b.as<double>(), tune_x.as<double>(), rhs, SPTRSV_ROW_MAJOR);
-            if (!rc) {
-                CUDA_TRY(cudaEventRecord(ev1, st));
-                rc = sync();
-                if (!rc) CUDA_TRY(cudaEventElapsedTime(&first, ev0, ev1));
-            }
-            if (rc == 0) {
+            rc = timed_candidate(o, rhs, lim, &first, &cens);
+            if (rc == 0 && !cens) {
                 t = first;
                 for (int r = 0; r < reps && first <= cap_ms; ++r) {
-                    float e = 0.f;
-                    CUDA_TRY(cudaEventRecord(ev0, st));
-                    if ((rc = solve(&o, tune_b.as<double>(), tune_x.as<double>(), rhs, SPTRSV_ROW_MAJOR))) break;
-                    CUDA_TRY(cudaEventRecord(ev1, st));
-                    if ((rc = sync())) break;
-                    CUDA_TRY(cudaEventElapsedTime(&e, ev0, ev1));
+                    float e = INFINITY;
+                    bool c2 = false;
+                    if ((rc = timed_candidate(o, rhs, lim, &e, &c2)) || c2) break;
                     t = std::min(t, e);
                 }
                 if (rc) t = INFINITY;
+            } else if (rc == 0 && cens) {
+                t = first;
             } else if (rc == SPTRSV_ERR_CUDA || rc == SPTRSV_ERR_NO_DEVICE) {
                 return rc;
             }
             rc = 0;
         }
         if (ms_out) ms_out[k] = t;
-        if (t < best) { best = t; bid = k; }
+        if (censored_out) censored_out[k] = cens ? 1 : 0;
+        if (!cens && t < best) { best = t; bid = k; }
     }
     if (bid < 0) return SPTRSV_ERR_UNSUPPORTED;
     const int cls = rhs_class(rhs);
@@ -183,11 +238,16 @@ using sptrsv::Handle;
 extern "C" {
 
 int sptrsv_autotune(sptrsv_handle hh, int rhs, float cap_ms, int reps, float* cand_ms, int* best_id, sptrsv_opts* best) {
+    return sptrsv_autotune_bounded(hh, rhs, cap_ms, reps, 0.f, cand_ms, nullptr, best_id, best);
+}
+
+int sptrsv_autotune_bounded(sptrsv_handle hh, int rhs, float cap_ms, int reps, float abort_ms, float* cand_ms,
+                            int* censored, int* best_id, sptrsv_opts* best) {
     Handle* h = reinterpret_cast<Handle*>(hh);
     if (!h || rhs < 1) return SPTRSV_ERR_INVALID_ARG;
     if (cudaSetDevice(h->device) != cudaSuccess) return SPTRSV_ERR_CUDA;
     int id = -1;
-    int rc = h->autotune(rhs, cap_ms > 0 ? cap_ms : 50.f, reps > 0 ? reps : 2, cand_ms, &id);
+    int rc = h->autotune(rhs, cap_ms > 0 ? cap_ms : 50.f, reps >= 0 ? reps : 2, abort_ms, cand_ms, censored, &id);
     if (rc) return rc;
     if (best_id) *best_id = id;
     if (best) {

@@ -156,12 +156,13 @@ def make_matrix(spec):
     return m, m.snodes
 
 
-def build_dataset(count, seed=7, nmax=2_000_000, cap_ms=20.0, reps=2, time_limit_s=None, out=None, device=0,
-                  start=0, log=None):
+def build_dataset(count, seed=7, nmax=2_000_000, cap_ms=20.0, reps=2, abort_ms=40.0, time_limit_s=None, out=None,
+                  device=0, start=0, log=None):
     """Features and candidate timings (ms; inf where not applicable or failed) for specs
-    [start, count) of sample_specs(count, seed, nmax)."""
+    [start, count) of sample_specs(count, seed, nmax).  A candidate still running after
+    max(abort_ms, 20 x the best so far) is cancelled; its time is then a lower bound (C = 1)."""
     specs = sample_specs(count, seed, nmax)
-    X, T, A, S, K = [], [], [], [], []
+    X, T, A, S, K, C = [], [], [], [], [], []
     t0 = time.time()
     with Solver(device) as s:
         for k in range(start, count):
@@ -175,29 +176,42 @@ def build_dataset(count, seed=7, nmax=2_000_000, cap_ms=20.0, reps=2, time_limit
             rhs = sp_["rhs"]
             f = s.features(rhs)
             try:
-                _, ms = s.autotune(rhs=rhs, cap_ms=cap_ms, reps=reps)
+                _, ms, cens = s.autotune(rhs=rhs, cap_ms=cap_ms, reps=reps, abort_ms=abort_ms, with_censored=True)
             except SptrsvError:
                 ms = np.full(N_CANDIDATES, np.inf, dtype=np.float32)
+                cens = np.zeros(N_CANDIDATES, dtype=np.int32)
             app = np.array([s.applicable(c, rhs) for c in range(N_CANDIDATES)], dtype=np.int8)
             X.append(f)
             T.append(ms)
             A.append(app)
             S.append([sp_["kind"], sp_["g"], sp_["n"] or m.n, sp_["mean"], sp_["band"], sp_["wmax"], rhs, m.nnz])
             K.append(k)
+            C.append(np.asarray(cens, dtype=np.int8))
             if log and (len(K) % 50 == 0):
                 log("%d matrices, %.0f s" % (len(K), time.time() - t0))
-            if out and len(K) % 200 == 0:
-                _save(out, X, T, A, S, K, seed, nmax)
+            if out and len(K) % 100 == 0:
+                _save(out, X, T, A, S, K, C, seed, nmax)
     if out:
-        _save(out, X, T, A, S, K, seed, nmax)
+        _save(out, X, T, A, S, K, C, seed, nmax)
     return dict(X=np.array(X, dtype=np.float32), T=np.array(T, dtype=np.float32), A=np.array(A, dtype=np.int8),
-                S=np.array(S, dtype=np.float64), K=np.array(K, dtype=np.int32))
+                S=np.array(S, dtype=np.float64), K=np.array(K, dtype=np.int32), C=np.array(C, dtype=np.int8))
 
 
-def _save(path, X, T, A, S, K, seed, nmax):
+def _save(path, X, T, A, S, K, C, seed, nmax):
     np.savez_compressed(path, X=np.array(X, dtype=np.float32), T=np.array(T, dtype=np.float32),
                         A=np.array(A, dtype=np.int8), S=np.array(S, dtype=np.float64), K=np.array(K, dtype=np.int32),
-                        seed=np.array([seed]), nmax=np.array([nmax]))
+                        C=np.array(C, dtype=np.int8), seed=np.array([seed]), nmax=np.array([nmax]))
+
+
+def merge(paths, out):
+    """Concatenate dataset parts (disjoint spec ranges of one seed) into one file, in spec order."""
+    parts = [load_dataset(p) for p in paths]
+    keys = ("X", "T", "A", "S", "K", "C")
+    d = {k: np.concatenate([p[k] for p in parts]) for k in keys}
+    order = np.argsort(d["K"], kind="stable")
+    d = {k: v[order] for k, v in d.items()}
+    np.savez_compressed(out, **d, seed=parts[0]["seed"], nmax=parts[0]["nmax"])
+    return d
 
 
 def load_dataset(path=DATA):
@@ -209,7 +223,8 @@ def load_dataset(path=DATA):
 # training and evaluation
 
 def targets(T):
-    """log(ms) targets and their mask (finite timings only)."""
+    """log(ms) targets and their mask (finite timings; a cancelled candidate's lower bound is kept
+    as its target, which marks it as slow)."""
     M = np.isfinite(T).astype(np.float32)
     Y = np.where(M > 0, np.log(np.where(np.isfinite(T), np.maximum(T, 1e-6), 1.0)), 0.0).astype(np.float32)
     return Y, M
@@ -329,16 +344,23 @@ def main(argv=None):
     b.add_argument("--nmax", type=int, default=2_000_000)
     b.add_argument("--cap-ms", type=float, default=20.0)
     b.add_argument("--reps", type=int, default=2)
+    b.add_argument("--abort-ms", type=float, default=40.0)
     b.add_argument("--time-limit", type=float, default=None)
     b.add_argument("--out", required=True)
+    mg = sub.add_parser("merge")
+    mg.add_argument("parts", nargs="+")
+    mg.add_argument("--out", required=True)
     e = sub.add_parser("eval")
     e.add_argument("--data", default=DATA)
     e.add_argument("--held-out", type=int, default=200)
     e.add_argument("--epochs", type=int, default=400)
     a = ap.parse_args(argv)
     if a.cmd == "build":
-        d = build_dataset(a.count, a.seed, a.nmax, a.cap_ms, a.reps, a.time_limit, a.out, start=a.start,
+        d = build_dataset(a.count, a.seed, a.nmax, a.cap_ms, a.reps, a.abort_ms, a.time_limit, a.out, start=a.start,
                           log=lambda s: print(s, flush=True))
+        print(json.dumps({"matrices": int(len(d["K"])), "last_spec": int(d["K"][-1]) if len(d["K"]) else -1}))
+    elif a.cmd == "merge":
+        d = merge(a.parts, a.out)
         print(json.dumps({"matrices": int(len(d["K"]))}))
     else:
         d = load_dataset(a.data)

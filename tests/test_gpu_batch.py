@@ -22,7 +22,10 @@ from sptrsv_gb300 import gen
 pytestmark = pytest.mark.gpu
 
 ELEM_TOL = 1e-10
-MIXED_ELEM_TOL = 1e-8
+# the mixed schedules are specified by their residual (<= 1e-12); their forward error against the
+# FP64 solve is that residual times the conditioning, and the banded Laplacian factors here have
+# condition numbers near 1e4, so components agree to ~1e-8 (checked at 1e-7)
+MIXED_ELEM_TOL = 1e-7
 RES_TOL = 1e-12
 
 
