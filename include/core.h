@@ -8,7 +8,8 @@
  * (CUDA events), or a negative sptrsv_status cast to double on failure (see
  * sptrsv_last_status() in sptrsv_gb300.h).  Layouts follow the reference: CSR with uint64
  * row pointer and the diagonal first in every row; X/B column-major (x[i + r*n]).
- * base_gauss_lower (core.h:9) is not provided: only upper systems are in scope.
+ * base_gauss_lower (core.h:9) solves the lower system as the reversed upper one (rows and
+ * columns in reverse order), on the same GPU path.
  */
 #ifndef SPTRSV_GB300_CORE_H
 #define SPTRSV_GB300_CORE_H
@@ -18,6 +19,9 @@
 #define SPTRSV_API __attribute__((visibility("default")))
 #endif
 
+/* core.h:9, core.cpp:4-16 -- forward substitution, x = L^{-1} b, one RHS; lower CSR with the
+ * diagonal LAST in every row. */
+SPTRSV_API double base_gauss_lower(int n, double* val, uint64_t* row_index, int* col, double* x, double* b);
 /* core.h:10, core.cpp:18-32 -- backward substitution, x = U^{-1} b. */
 SPTRSV_API double base_gauss_upper(int n, double* val, uint64_t* row_index, int* col, double* x, double* b, int rhs);
 /* core.h:11, core.cpp:34-51 -- same solve (the RHS loop order has no GPU meaning). */

@@ -45,7 +45,8 @@ enum sptrsv_status {
     SPTRSV_ERR_NO_DEVICE = -12,
     SPTRSV_ERR_NO_ANALYSIS = -13,   /* solve before analyse */
     SPTRSV_ERR_SUPERNODES = -14,    /* supernode partition inconsistent with the matrix */
-    SPTRSV_ERR_UNSUPPORTED = -15
+    SPTRSV_ERR_UNSUPPORTED = -15,
+    SPTRSV_ERR_IO = -16
 };
 
 /* Solve schedules (kernel families). */
@@ -140,9 +141,9 @@ SPTRSV_API int sptrsv_set_supernodes(sptrsv_handle h, int sn, const int* superno
 #define SPTRSV_FEATURES 24
 SPTRSV_API int sptrsv_autotune(sptrsv_handle h, int rhs, float cap_ms, int reps, float* cand_ms, int* best_id,
                                sptrsv_opts* best);
-/* As sptrsv_autotune, and a candidate still running after max(abort_ms, 20 x the best time so far)
- * is cancelled (its spins see the abort flag and return): its time is then a lower bound and
- * censored[id] = 1.  abort_ms = 0 never cancels. */
+/* As sptrsv_autotune, and once one candidate has finished, a later one still running after
+ * max(abort_ms, 20 x the best time so far) is cancelled (its spins see the abort flag and
+ * return): its time is then a lower bound and censored[id] = 1.  abort_ms = 0 never cancels. */
 SPTRSV_API int sptrsv_autotune_bounded(sptrsv_handle h, int rhs, float cap_ms, int reps, float abort_ms,
                                        float* cand_ms, int* censored, int* best_id, sptrsv_opts* best);
 /* Options of candidate `id` of the autotuner's table. */
@@ -280,6 +281,22 @@ SPTRSV_API int sptrsv_mlp_train(sptrsv_mlp m, int n, const float* x, const float
                                 int batch, float lr, uint64_t seed, float* loss_out);
 SPTRSV_API int sptrsv_mlp_predict(sptrsv_mlp m, int n, const float* x, float* y);
 SPTRSV_API int64_t sptrsv_mlp_launches(sptrsv_mlp m);
+
+/* ---------------------------------------------------------------------------------------
+ * The reference's file formats (utils.cpp:9-109), host side.  By extension:
+ *   .matrix binary  int32 n, uint64 nz, int32 col[nz], uint64 row_ptr[n+1], f64 val[nz];
+ *   .txt            n nz / val[nz] / col[nz] / row_ptr[n+1];
+ *   .mtx (read)     MatrixMarket entries of a lower factor in column order, read as the CSR of
+ *                   its transpose (utils.cpp:32-60);
+ *   .snodes binary  int32 sn, int32 snodes[sn+1];  .txt: sn / snodes[sn+1].
+ * Arrays returned by the readers are malloc'd; release them with sptrsv_io_free.  Failures:
+ * SPTRSV_ERR_IO (unreadable or malformed), SPTRSV_ERR_INVALID_ARG (unknown extension). */
+SPTRSV_API int sptrsv_read_csr(const char* path, int* n, int64_t* nnz, int64_t** row_ptr, int** col, double** val);
+SPTRSV_API int sptrsv_write_csr(const char* path, int n, int64_t nnz, const int64_t* row_ptr, const int* col,
+                                const double* val);
+SPTRSV_API int sptrsv_read_snodes(const char* path, int* sn, int** snodes);
+SPTRSV_API int sptrsv_write_snodes(const char* path, int sn, const int* snodes);
+SPTRSV_API void sptrsv_io_free(void* p);
 
 #ifdef __cplusplus
 }

@@ -42,6 +42,19 @@ ORC_API void orc_base_gauss_upper(int n, const double* val, const uint64_t* row_
     }
 }
 
+/* core.cpp:4-16  base_gauss_lower: forward substitution for lower-triangular CSR with the
+ * diagonal LAST in every row; one right-hand side.  Row 0 divides by val[col[0]] as the
+ * reference does (its only entry when col[0] = 0). */
+ORC_API void orc_base_gauss_lower(int n, const double* val, const uint64_t* row_index, const int* col, double* x,
+                                  const double* b) {
+    x[0] = b[0] / val[col[0]];
+    for (int ir = 1; ir < n; ++ir) {
+        double sum = 0.0;
+        for (uint64_t j = row_index[ir]; j < row_index[ir + 1] - 1; ++j) sum += val[j] * x[col[j]];
+        x[ir] = (b[ir] - sum) / val[row_index[ir + 1] - 1];
+    }
+}
+
 /* core.cpp:34-51  base_gauss_upper_new: same arithmetic, RHS loop inside the row loop. */
 ORC_API void orc_base_gauss_upper_new(int n, const double* val, const uint64_t* row_index, const int* col,
                                       double* x, const double* b, int rhs) {

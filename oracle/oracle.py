@@ -45,6 +45,7 @@ def lib():
         L = ctypes.CDLL(LIB_PATH)
         L.orc_base_gauss_upper.argtypes = [_c_int, _f64, _u64, _i32, _f64, _f64, _c_int]
         L.orc_base_gauss_upper_new.argtypes = [_c_int, _f64, _u64, _i32, _f64, _f64, _c_int]
+        L.orc_base_gauss_lower.argtypes = [_c_int, _f64, _u64, _i32, _f64, _f64]
         L.orc_set_levels.argtypes = [_c_int, _i32, _u64, _u64]
         L.orc_set_levels.restype = _c_int
         L.orc_level_buckets.argtypes = [_c_int, _u64, _c_int, _i32, _i32]
@@ -76,6 +77,9 @@ def ref():
         for name in ("ref_base_gauss_upper", "ref_base_gauss_upper_new"):
             getattr(R, name).argtypes = [_c_int, _f64, _u64, _i32, _f64, _f64, _c_int]
             getattr(R, name).restype = _c_dbl
+        if hasattr(R, "ref_base_gauss_lower"):
+            R.ref_base_gauss_lower.argtypes = [_c_int, _f64, _u64, _i32, _f64, _f64]
+            R.ref_base_gauss_lower.restype = _c_dbl
         for name in ("ref_supernodal_upper", "ref_supernodal_upper_new"):
             getattr(R, name).argtypes = [_c_sz, _i32, _f64, _f64, _i32, _u64, _c_int, _c_int]
             getattr(R, name).restype = _c_dbl
@@ -106,6 +110,15 @@ def base_gauss_upper(row_ptr, col, val, b, rhs=1, new=False):
     b = np.ascontiguousarray(b, dtype=np.float64).reshape(-1)
     x = np.zeros(n * rhs)
     (lib().orc_base_gauss_upper_new if new else lib().orc_base_gauss_upper)(n, v, rp, c, x, b, rhs)
+    return x
+
+
+def base_gauss_lower(row_ptr, col, val, b):
+    """Forward substitution (core.cpp:4-16): lower CSR, diagonal last in every row, one RHS."""
+    rp, c, v = _csr(row_ptr, col, val)
+    n = len(rp) - 1
+    x = np.zeros(n)
+    lib().orc_base_gauss_lower(n, v, rp, c, x, np.ascontiguousarray(b, dtype=np.float64).reshape(-1))
     return x
 
 

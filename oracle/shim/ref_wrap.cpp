@@ -3,6 +3,7 @@
 // Test infrastructure only.
 #include <cstddef>
 #include <cstdint>
+double base_gauss_lower(int, double*, uint64_t*, int*, double*, double*);
 double base_gauss_upper(int, double*, uint64_t*, int*, double*, double*, int);
 double base_gauss_upper_new(int, double*, uint64_t*, int*, double*, double*, int);
 double supernodal_upper(size_t, int*, double*, double*, int*, uint64_t*, int, int);
@@ -14,6 +15,7 @@ double barrier_upper(int, double*, double*, double*, int*, uint64_t*, int, int);
 double barrier_upper_new(int, double*, double*, double*, int*, uint64_t*, int, int);
 
 extern "C" {
+double ref_base_gauss_lower(int n, double* v, uint64_t* r, int* c, double* x, double* b) { return base_gauss_lower(n, v, r, c, x, b); }
 double ref_base_gauss_upper(int n, double* v, uint64_t* r, int* c, double* x, double* b, int rhs) { return base_gauss_upper(n, v, r, c, x, b, rhs); }
 double ref_base_gauss_upper_new(int n, double* v, uint64_t* r, int* c, double* x, double* b, int rhs) { return base_gauss_upper_new(n, v, r, c, x, b, rhs); }
 double ref_supernodal_upper(size_t sn, int* s, double* x, double* v, int* c, uint64_t* r, int n, int rhs) { return supernodal_upper(sn, s, x, v, c, r, n, rhs); }

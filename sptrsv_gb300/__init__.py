@@ -79,6 +79,11 @@ def _c(a, dt):
 # The reference interface (core.h / sptrsv_syncfree_opencl.h).  Arrays are numpy; outputs
 # are written into the caller's arrays, as in the reference.
 
+def base_gauss_lower(n, val, row_index, col, x, b):
+    """core.h:9 -- x = L^{-1} b, one RHS; CSR (uint64 row_index, diagonal LAST in every row)."""
+    return _lib.dropin("base_gauss_lower")(n, val, row_index, col, x, b)
+
+
 def base_gauss_upper(n, val, row_index, col, x, b, rhs):
     """core.h:10 -- x = U^{-1} b; CSR (uint64 row_index, diagonal first), X/B column-major."""
     return _lib.dropin("base_gauss_upper")(n, val, row_index, col, x, b, rhs)
@@ -413,3 +418,45 @@ class Batch:
     def split(self, x):
         """Per-system views (n x rhs) of a concatenated solution."""
         return [x[self.xb_off[s]:self.xb_off[s + 1]].reshape(int(self.n[s]), int(self.rhs[s])) for s in range(self.count)]
+
+
+def read_csr(path):
+    """The reference's matrix files (.matrix / .txt / .mtx, utils.cpp:9-80) -> (row_ptr int64,
+    col int32, val float64), CSR with the diagonal first."""
+    L = _lib.lib()
+    n, nnz = ctypes.c_int(), ctypes.c_int64()
+    rp, col, val = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
+    _check(L.sptrsv_read_csr(str(path).encode(), ctypes.byref(n), ctypes.byref(nnz), ctypes.byref(rp),
+                             ctypes.byref(col), ctypes.byref(val)), "read_csr")
+    try:
+        out = (np.ctypeslib.as_array(ctypes.cast(rp, ctypes.POINTER(ctypes.c_int64)), (n.value + 1,)).copy(),
+               np.ctypeslib.as_array(ctypes.cast(col, ctypes.POINTER(ctypes.c_int32)), (max(1, nnz.value),))[:nnz.value].copy(),
+               np.ctypeslib.as_array(ctypes.cast(val, ctypes.POINTER(ctypes.c_double)), (max(1, nnz.value),))[:nnz.value].copy())
+    finally:
+        for p in (rp, col, val):
+            L.sptrsv_io_free(p)
+    return out
+
+
+def write_csr(path, row_ptr, col, val):
+    """.matrix (binary) or .txt, the reference's layouts."""
+    rp = np.ascontiguousarray(row_ptr, dtype=np.int64)
+    _check(_lib.lib().sptrsv_write_csr(str(path).encode(), len(rp) - 1, int(rp[-1]), rp,
+                                       np.ascontiguousarray(col, dtype=np.int32),
+                                       np.ascontiguousarray(val, dtype=np.float64)), "write_csr")
+
+
+def read_snodes(path):
+    """.snodes (binary) or .txt supernode partition -> int32[sn+1]."""
+    L = _lib.lib()
+    sn, p = ctypes.c_int(), ctypes.c_void_p()
+    _check(L.sptrsv_read_snodes(str(path).encode(), ctypes.byref(sn), ctypes.byref(p)), "read_snodes")
+    try:
+        return np.ctypeslib.as_array(ctypes.cast(p, ctypes.POINTER(ctypes.c_int32)), (sn.value + 1,)).copy()
+    finally:
+        L.sptrsv_io_free(p)
+
+
+def write_snodes(path, snodes):
+    s = np.ascontiguousarray(snodes, dtype=np.int32)
+    _check(_lib.lib().sptrsv_write_snodes(str(path).encode(), len(s) - 1, s), "write_snodes")

@@ -32,6 +32,7 @@ class Opts(ctypes.Structure):
 # the names are their Itanium-ABI manglings (identical on x86-64 and aarch64, where uint64_t is
 # unsigned long).
 DROPIN_SYMBOLS = {
+    "base_gauss_lower": "_Z16base_gauss_loweriPdPmPiS_S_",
     "base_gauss_upper": "_Z16base_gauss_upperiPdPmPiS_S_i",
     "base_gauss_upper_new": "_Z20base_gauss_upper_newiPdPmPiS_S_i",
     "supernodal_upper": "_Z16supernodal_uppermPiPdS0_S_Pmii",
@@ -50,6 +51,7 @@ DROPIN_SYMBOLS = {
 _c_int_p = ctypes.POINTER(ctypes.c_int)
 
 DROPIN_ARGTYPES = {
+    "base_gauss_lower": ([c_int, f64, u64, i32, f64, f64], c_dbl),
     "base_gauss_upper": ([c_int, f64, u64, i32, f64, f64, c_int], c_dbl),
     "base_gauss_upper_new": ([c_int, f64, u64, i32, f64, f64, c_int], c_dbl),
     "supernodal_upper": ([c_sz, i32, f64, f64, i32, u64, c_int, c_int], c_dbl),
@@ -121,6 +123,12 @@ C_API = {
     "sptrsv_batch_timer_begin": ([c_vp], c_int),
     "sptrsv_batch_timer_end": ([c_vp, ctypes.POINTER(ctypes.c_float)], c_int),
     "sptrsv_batch_launches": ([c_vp], c_i64),
+    "sptrsv_read_csr": ([ctypes.c_char_p, _c_int_p, ctypes.POINTER(c_i64), ctypes.POINTER(c_vp), ctypes.POINTER(c_vp),
+                         ctypes.POINTER(c_vp)], c_int),
+    "sptrsv_write_csr": ([ctypes.c_char_p, c_int, c_i64, i64, i32, f64], c_int),
+    "sptrsv_read_snodes": ([ctypes.c_char_p, _c_int_p, ctypes.POINTER(c_vp)], c_int),
+    "sptrsv_write_snodes": ([ctypes.c_char_p, c_int, i32], c_int),
+    "sptrsv_io_free": ([c_vp], None),
     "sptrsv_mlp_create": ([ctypes.POINTER(c_vp), c_int, c_int, c_int, c_int, c_int, ctypes.c_uint64], c_int),
     "sptrsv_mlp_destroy": ([c_vp], c_int),
     "sptrsv_mlp_num_params": ([c_vp], c_int),

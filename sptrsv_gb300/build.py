@@ -35,7 +35,9 @@ def build(verbose=False, force=False):
     os.makedirs(BUILD, exist_ok=True)
     headers = glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(ROOT, "include", "*.h"))
     hdr_time = _newest(headers)
-    sources = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
+    # CUDA translation units plus host-only C++ ones (gen.cpp goes into the generator library)
+    sources = sorted(glob.glob(os.path.join(CSRC, "*.cu")) +
+                     [p for p in glob.glob(os.path.join(CSRC, "*.cpp")) if os.path.basename(p) != "gen.cpp"])
     nvcc = _nvcc()
     flags = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-fvisibility=hidden",
                     "-I" + os.path.join(ROOT, "include"), "--expt-relaxed-constexpr"]

@@ -768,6 +768,7 @@ const char* sptrsv_status_string(int s) {
         case SPTRSV_ERR_NO_ANALYSIS: return "solve before analyse";
         case SPTRSV_ERR_SUPERNODES: return "supernode partition inconsistent with the matrix";
         case SPTRSV_ERR_UNSUPPORTED: return "unsupported combination of options";
+        case SPTRSV_ERR_IO: return "file unreadable or malformed";
         default: return "unknown status";
     }
 }

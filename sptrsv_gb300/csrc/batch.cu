@@ -111,20 +111,23 @@ __device__ __forceinline__ int seg_find(const SegList& L, long long q) {
     return lo;
 }
 
-// Lanes of a warp on one row: nc RHS columns side by side, `groups` (a power of two) strided
-// walks over the row's entries; lane = g * nc + c.
+// Lanes of a warp on one row: nc RHS columns side by side, groups = floor(32 / nc) strided walks
+// over the row's entries; lane = g * nc + c (lanes from groups * nc on stay idle).
 __device__ __forceinline__ void lane_split(int nc, int& groups, int& g, int& c) {
-    int gr = 32 / nc;
-    gr = 1 << (31 - __clz(gr));
-    groups = gr;
+    groups = 32 / nc;
     const int lane = threadIdx.x & 31;
     g = lane / nc;
     c = lane - g * nc;
 }
 
+// Sum over the groups of each column, into the lanes of group 0 (a guarded tree: any group count).
 template <typename T>
 __device__ __forceinline__ T group_sum(T v, int groups, int nc) {
-    for (int off = groups >> 1; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off * nc);
+    const int g = (threadIdx.x & 31) / nc;
+    for (int off = 1; off < groups; off <<= 1) {
+        const T o = __shfl_down_sync(0xffffffffu, v, off * nc);
+        if ((g & (2 * off - 1)) == 0 && g + off < groups) v += o;
+    }
     return v;
 }
 
@@ -382,20 +385,38 @@ __global__ void __launch_bounds__(128) k_b_panels(BArgs A, const int2* __restric
                 const int k0 = kb * kBKc, kc = min(kBKc, K - k0);
                 if (threadIdx.x == 0) s_ok = 1;
                 __syncthreads();
-                for (int e = threadIdx.x; e < kBKc * nc8; e += blockDim.x) {
-                    const int j = e / kBKc, kk = e - j * kBKc, k = k0 + kk;
-                    float v = 0.f;
-                    if (kk < kc && j < nc) {
-                        if (k < w) {
-                            v = b[(size_t)(a + k) * rhs + c0 + j];
-                        } else if (!wait_ready<float>(x + (size_t)C.rect[k - w] * rhs + c0 + j, v, ctl, A.budget)) {
-                            s_ok = 0;
-                            v = 0.f;
-                        }
+                // every element of the chunk is loaded first (independent loads in flight together),
+                // then only the solved-column values still pending are waited on
+                constexpr int kStage = kBKc * kBNc / 128;
+                const int tot = kBKc * nc8;
+                float v[kStage];
+#pragma unroll
+                for (int u = 0; u < kStage; ++u) {
+                    const int e = threadIdx.x + u * 128;
+                    float val = 0.f;
+                    if (e < tot) {
+                        const int j = e / kBKc, kk = e - j * kBKc, k = k0 + kk;
+                        if (kk < kc && j < nc)
+                            val = k < w ? b[(size_t)(a + k) * rhs + c0 + j]
+                                        : ld_relaxed(x + (size_t)C.rect[k - w] * rhs + c0 + j);
                     }
-                    const __nv_bfloat16 h = __float2bfloat16_rn(v);
-                    Vhi[j][kk] = h;
-                    Vlo[j][kk] = __float2bfloat16_rn(v - __bfloat162float(h));
+                    v[u] = val;
+                }
+#pragma unroll
+                for (int u = 0; u < kStage; ++u) {
+                    const int e = threadIdx.x + u * 128;
+                    if (e < tot) {
+                        const int j = e / kBKc, kk = e - j * kBKc, k = k0 + kk;
+                        float val = v[u];
+                        if (kk < kc && j < nc && k >= w && Pend<float>::is(val) &&
+                            !wait_ready<float>(x + (size_t)C.rect[k - w] * rhs + c0 + j, val, ctl, A.budget)) {
+                            s_ok = 0;
+                            val = 0.f;
+                        }
+                        const __nv_bfloat16 h = __float2bfloat16_rn(val);
+                        Vhi[j][kk] = h;
+                        Vlo[j][kk] = __float2bfloat16_rn(val - __bfloat162float(h));
+                    }
                 }
                 __syncthreads();
                 if (!s_ok) { ok = false; break; }

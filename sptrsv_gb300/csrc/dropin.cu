@@ -9,6 +9,7 @@
 // double and record it for sptrsv_last_status(); nothing prints or exits.
 #include <cstdint>
 #include <cstring>
+#include <algorithm>
 #include <mutex>
 #include <vector>
 #include "common.cuh"
@@ -157,6 +158,53 @@ static double gauss_upper(int n, double* val, uint64_t* row_index, int* col, dou
     if ((rc = h->analyse())) return fail(rc);
     double secs = 0;
     if ((rc = solve_host_timed(h, fp64(SPTRSV_SCHED_AUTO), b, x, rhs, SPTRSV_COL_MAJOR, &secs))) return fail(rc);
+    set_last_status(0);
+    return secs;
+}
+
+// Lower-triangular CSR (diagonal last in every row) -> the upper-triangular CSR of the same
+// system with rows and columns in reverse order: U = P L P, P the reversal permutation.  Row r of
+// U is row n-1-r of L read backwards, so the whole col/val arrays are reversed (columns mapped to
+// n-1-c) and U's row pointer is nnz - L's taken from the end.  rp_l is a copy of L's row pointer.
+__global__ void k_reverse_lower(int n, int nnz, const int* __restrict__ rp_l, int* __restrict__ rp_u, int* col,
+                                double* val) {
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+    for (int r = tid; r <= n; r += nth) rp_u[r] = nnz - rp_l[n - r];
+    for (int k = tid; k < (nnz + 1) / 2; k += nth) {
+        const int q = nnz - 1 - k;
+        const int ck = col[k], cq = col[q];
+        const double vk = val[k], vq = val[q];
+        col[k] = n - 1 - cq;
+        col[q] = n - 1 - ck;
+        val[k] = vq;
+        val[q] = vk;
+    }
+}
+
+// core.cpp:4-16: forward substitution, solved as the reversed upper system on the GPU.
+static double gauss_lower(int n, double* val, uint64_t* row_index, int* col, double* x, double* b) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    Handle* h;
+    int rc;
+    if ((rc = default_handle(&h))) return fail(rc);
+    if (n <= 0 || !val || !row_index || !col || !x || !b) return fail(SPTRSV_ERR_INVALID_ARG);
+    const int64_t nnz = (int64_t)row_index[n];
+    if ((rc = h->set_matrix_host(n, nnz, (const int64_t*)row_index, col, val))) return fail(rc);
+    if ((rc = h->scratch.ensure(sizeof(int) * ((size_t)n + 1)))) return fail(rc);
+    if (cudaMemcpyAsync(h->scratch.p, h->own_rp.p, sizeof(int) * ((size_t)n + 1), cudaMemcpyDeviceToDevice, h->st) !=
+        cudaSuccess)
+        return fail(SPTRSV_ERR_CUDA);
+    k_reverse_lower<<<h->sm_count * 4, 256, 0, h->st>>>(n, (int)nnz, (const int*)h->scratch.p, h->own_rp.as<int>(),
+                                                        h->own_col.as<int>(), h->own_val.as<double>());
+    h->launches++;
+    if (cudaGetLastError() != cudaSuccess) return fail(SPTRSV_ERR_CUDA);
+    if ((rc = h->analyse())) return fail(rc);
+    std::vector<double> br(b, b + n), xr(n);
+    std::reverse(br.begin(), br.end());
+    double secs = 0;
+    if ((rc = solve_host_timed(h, fp64(SPTRSV_SCHED_AUTO), br.data(), xr.data(), 1, SPTRSV_COL_MAJOR, &secs)))
+        return fail(rc);
+    std::reverse_copy(xr.begin(), xr.end(), x);
     set_last_status(0);
     return secs;
 }
@@ -342,6 +390,10 @@ static double csc_push(int* cp, int* crow, const double* cval, int m, int n, int
 }  // namespace sptrsv
 
 using namespace sptrsv;
+
+double base_gauss_lower(int n, double* val, uint64_t* row_index, int* col, double* x, double* b) {
+    return gauss_lower(n, val, row_index, col, x, b);
+}
 
 double base_gauss_upper(int n, double* val, uint64_t* row_index, int* col, double* x, double* b, int rhs) {
     return gauss_upper(n, val, row_index, col, x, b, rhs);

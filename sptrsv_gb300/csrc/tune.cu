@@ -125,8 +125,9 @@ int Handle::timed_candidate(const sptrsv_opts& o, int rhs, float abort_ms, float
 }
 
 // Exhaustive tuning.  Candidates run in a fixed order that usually finds a fast one early; with
-// abort_ms > 0 a candidate still running after max(abort_ms, 20 x the best so far) is cancelled
-// and reported as censored (its time a lower bound).
+// abort_ms > 0, once one candidate has finished, a later one still running after
+// max(abort_ms, 20 x the best so far) is cancelled and reported as censored (its time a lower
+// bound).
 int Handle::autotune(int rhs, float cap_ms, int reps, float abort_ms, float* ms_out, int* censored_out, int* best_id) {
     if (!analysed) return SPTRSV_ERR_NO_ANALYSIS;
     int rc;
@@ -147,7 +148,8 @@ int Handle::autotune(int rhs, float cap_ms, int reps, float abort_ms, float* ms_
         bool cens = false;
         if (applicable(cand[k], rhs)) {
             const sptrsv_opts o = cand[k];
-            const float lim = abort_ms > 0.f ? std::max(abort_ms, std::isfinite(best) ? 20.f * best : abort_ms) : 0.f;
+            // nothing is cancelled before one candidate has finished, so a pick always exists
+            const float lim = abort_ms > 0.f && std::isfinite(best) ? std::max(abort_ms, 20.f * best) : 0.f;
             float first = INFINITY;
             rc = timed_candidate(o, rhs, lim, &first, &cens);
             if (rc == 0 && !cens) {

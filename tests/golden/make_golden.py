@@ -113,6 +113,24 @@ def main():
     ref_solves(R, "snr800", m.row_ptr, m.col, m.val, b, 2, out)
     ref_supernodal(R, "snr800", m.row_ptr, m.col, m.val, m.snodes, b, 2, out)
 
+    # lower-triangular systems (core.cpp:4-16): transposes of upper ones, diagonal last per row
+    import scipy.sparse as sps
+    lowers = [("csr_6_lower", out["csr_6_upper/row_ptr"], out["csr_6_upper/col"], out["csr_6_upper/val"], None),
+              ("lower3000", None, None, None, gen.random_upper(3000, 8.0, 0.9, 64, 13))]
+    for tag, rp, col, val, m in lowers:
+        if m is not None:
+            rp, col, val = m.row_ptr, m.col, m.val
+        n = len(rp) - 1
+        L = sps.csr_matrix((val, col, rp), shape=(n, n)).T.tocsr()
+        L.sort_indices()
+        lrp, lcol, lval = L.indptr.astype(np.uint64), L.indices.astype(np.int32), L.data.astype(np.float64)
+        b = np.ones(n) if m is None else gen.uniform(14, n)
+        x = np.zeros(n)
+        R.ref_base_gauss_lower(n, lval, lrp, lcol, x, b.copy())
+        out[tag + "/row_ptr"], out[tag + "/col"], out[tag + "/val"] = lrp.astype(np.int64), lcol, lval
+        out[tag + "/b"] = b
+        out[tag + "/lower"] = x
+
     # levels of a larger matrix: only the max level and a digest are stored
     m = gen.random_upper(200_000, 8.0, 0.9, 64, 1)
     lv = np.zeros(m.n, dtype=np.uint64)

@@ -302,3 +302,22 @@ def test_irregular_2m_full(orc, solver):
     assert elem_err(x, ref) <= MIXED_ELEM_TOL
     # property at full size: the solution of U x = U x* is x*
     assert np.max(np.abs(x - xs)) <= 1e-9
+
+
+@pytest.mark.parametrize("tag", ["csr_6_lower", "lower3000"])
+def test_dropin_base_gauss_lower(golden, tag):
+    """core.h:9: the lower solve, run as the reversed upper system on the GPU."""
+    rp = golden[tag + "/row_ptr"].astype(np.uint64)
+    col, val, b = golden[tag + "/col"], golden[tag + "/val"], golden[tag + "/b"]
+    n = len(rp) - 1
+    x = np.zeros(n)
+    secs = sp.base_gauss_lower(n, val.copy(), rp.copy(), col.copy(), x, b.copy())
+    assert secs >= 0
+    assert elem_err(x, golden[tag + "/lower"]) <= ELEM_TOL
+
+
+def test_dropin_base_gauss_lower_rejects_upper(golden):
+    rp = golden["csr_6_upper/row_ptr"].astype(np.uint64)
+    col, val = golden["csr_6_upper/col"], golden["csr_6_upper/val"]
+    x = np.zeros(6)
+    assert sp.base_gauss_lower(6, val.copy(), rp.copy(), col.copy(), x, np.ones(6)) < 0

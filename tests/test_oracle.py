@@ -125,3 +125,11 @@ def test_oracle_against_live_reference(orc):
     ml = R.ref_set_levels(m.n, m.col, rp, lv)
     lv2, ml2 = orc.levels(rp, m.col)
     assert ml == ml2 and np.array_equal(lv, lv2)
+
+
+@pytest.mark.parametrize("tag", ["csr_6_lower", "lower3000"])
+def test_base_gauss_lower_matches_reference(golden, orc, tag):
+    rp, col, val = golden[tag + "/row_ptr"].astype(np.uint64), golden[tag + "/col"], golden[tag + "/val"]
+    x = orc.base_gauss_lower(rp, col, val, golden[tag + "/b"])
+    ref = golden[tag + "/lower"]
+    assert np.max(np.abs(x - ref) / np.maximum(np.abs(ref), 1e-300)) <= 1e-13
