@@ -254,6 +254,14 @@ SPTRSV_API int sptrsv_batch_stats(sptrsv_batch b, int* status, int* steps, doubl
 SPTRSV_API int sptrsv_batch_info(sptrsv_batch b, int64_t* totals, float* ratio);
 /* The selector's SPTRSV_FEATURES features of system s (with its own rhs). */
 SPTRSV_API int sptrsv_batch_features(sptrsv_batch b, int s, float* features);
+/* One solve driven from the host with CUDA events around every kernel (same kernels and loop
+ * decisions as the graph, read back after each check); per kernel kind the summed device time
+ * and launch count, and the time of its first launch (SPTRSV_BATCH_KINDS kinds: fill x, FP64
+ * pull, state init, mixed init, step begin, fill d, panels, FP32 pull, Jacobi sweep, sweep check,
+ * axpy, residual, step check). */
+#define SPTRSV_BATCH_KINDS 13
+SPTRSV_API int sptrsv_batch_profile(sptrsv_batch b, int mode, const double* d_b, double* d_x, float* kind_ms,
+                                    int* kind_launches, float* kind_first_ms);
 SPTRSV_API int sptrsv_batch_timer_begin(sptrsv_batch b);
 SPTRSV_API int sptrsv_batch_timer_end(sptrsv_batch b, float* ms);
 SPTRSV_API int64_t sptrsv_batch_launches(sptrsv_batch b);

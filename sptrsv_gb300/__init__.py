@@ -404,6 +404,19 @@ class Batch:
         _check(_lib.lib().sptrsv_batch_features(self._h, int(s), f), "batch_features")
         return f
 
+    KINDS = ("fill_x", "pull_f64", "state_init", "mixed_init", "step_begin", "fill_d", "panels_bf16x3",
+             "pull_f32", "jacobi_sweep", "sweep_check", "axpy", "residual_f64", "step_check")
+
+    def profile(self, d_b, d_x, mode="chosen"):
+        """One host-driven solve with CUDA events around every kernel:
+        {kind: (total ms, launches, first launch ms)}."""
+        ms = np.zeros(len(self.KINDS), dtype=np.float32)
+        cnt = np.zeros(len(self.KINDS), dtype=np.int32)
+        first = np.zeros(len(self.KINDS), dtype=np.float32)
+        _check(_lib.lib().sptrsv_batch_profile(self._h, BATCH_MODE.get(mode, mode), ctypes.c_void_p(d_b),
+                                               ctypes.c_void_p(d_x), ms, cnt, first), "batch_profile")
+        return {k: (float(ms[i]), int(cnt[i]), float(first[i])) for i, k in enumerate(self.KINDS) if cnt[i]}
+
     def timer_begin(self):
         _check(_lib.lib().sptrsv_batch_timer_begin(self._h), "batch_timer")
 

@@ -120,6 +120,7 @@ C_API = {
     "sptrsv_batch_stats": ([c_vp, i32, i32, f64, i32], c_int),
     "sptrsv_batch_info": ([c_vp, i64, _P(dtype=np.float32, flags="C_CONTIGUOUS")], c_int),
     "sptrsv_batch_features": ([c_vp, c_int, _P(dtype=np.float32, flags="C_CONTIGUOUS")], c_int),
+    "sptrsv_batch_profile": ([c_vp, c_int, c_vp, c_vp, f32, i32, f32], c_int),
     "sptrsv_batch_timer_begin": ([c_vp], c_int),
     "sptrsv_batch_timer_end": ([c_vp, ctypes.POINTER(ctypes.c_float)], c_int),
     "sptrsv_batch_launches": ([c_vp], c_i64),

@@ -38,9 +38,10 @@ constexpr int kBPanel = 64;     // rows per panel work item (4 warps x 16-row MM
 constexpr int kBKc = 128;       // K rows staged per chunk
 constexpr int kBNc = 32;        // right-hand-side columns per pass
 constexpr int kBRowChunk = 32;  // rows per warp task in the row kernels
+constexpr int kBatchKinds = 13;  // kernel kinds of the profiled replay
 
 struct BSys {
-    int n, rhs, sched, pad;
+    int n, rhs, sched, groups;  // groups: lanes per row in the row kernels (row_lanes)
     long long rp0, nz0, row0, xb0;
 };
 
@@ -383,6 +384,16 @@ __global__ void __launch_bounds__(128) k_b_panels(BArgs A, const int2* __restric
             const int nk = (K + kBKc - 1) / kBKc;
             for (int kb = nk - 1; kb >= 0; --kb) {
                 const int k0 = kb * kBKc, kc = min(kBKc, K - k0);
+                // this chunk's G fragments are loaded before any wait on solved columns, so their
+                // memory latency overlaps the wait instead of following it
+                uint32_t ahs[kBKc / 16][4], als[kBKc / 16][4];
+#pragma unroll
+                for (int u = 0; u < kBKc / 16; ++u) {
+                    if (row0 < w && u * 16 < kc) {
+                        load_a(C.ghi, L, row0, w, k0 + u * 16, ahs[u]);
+                        load_a(C.glo, L, row0, w, k0 + u * 16, als[u]);
+                    }
+                }
                 if (threadIdx.x == 0) s_ok = 1;
                 __syncthreads();
                 // every element of the chunk is loaded first (independent loads in flight together),
@@ -421,11 +432,10 @@ __global__ void __launch_bounds__(128) k_b_panels(BArgs A, const int2* __restric
                 __syncthreads();
                 if (!s_ok) { ok = false; break; }
                 if (row0 < w) {
-                    for (int ks = 0; ks < kc; ks += 16) {
-                        uint32_t ah[4], al[4];
-                        load_a(C.ghi, L, row0, w, k0 + ks, ah);
-                        load_a(C.glo, L, row0, w, k0 + ks, al);
-                        const int kb2 = ks + (lane & 3) * 2;
+#pragma unroll
+                    for (int u = 0; u < kBKc / 16; ++u) {
+                        if (u * 16 >= kc) break;
+                        const int kb2 = u * 16 + (lane & 3) * 2;
 #pragma unroll
                         for (int q = 0; q < kBNc / 8; ++q) {
                             if (q * 8 >= nc) break;
@@ -434,9 +444,9 @@ __global__ void __launch_bounds__(128) k_b_panels(BArgs A, const int2* __restric
                             const uint32_t bh1 = *reinterpret_cast<const uint32_t*>(&Vhi[nn][kb2 + 8]);
                             const uint32_t bl0 = *reinterpret_cast<const uint32_t*>(&Vlo[nn][kb2]);
                             const uint32_t bl1 = *reinterpret_cast<const uint32_t*>(&Vlo[nn][kb2 + 8]);
-                            mma_bf16(acc[q], ah, bh0, bh1);
-                            mma_bf16(acc[q], ah, bl0, bl1);
-                            mma_bf16(acc[q], al, bh0, bh1);
+                            mma_bf16(acc[q], ahs[u], bh0, bh1);
+                            mma_bf16(acc[q], ahs[u], bl0, bl1);
+                            mma_bf16(acc[q], als[u], bh0, bh1);
                         }
                     }
                 }
@@ -461,48 +471,88 @@ __global__ void __launch_bounds__(128) k_b_panels(BArgs A, const int2* __restric
     }
 }
 
+// --- row tasks ---------------------------------------------------------------------------------
+
+// A row task: up to kTaskRows consecutive rows of one system.  A warp takes a task and works on
+// `rpw` rows of it at a time: lane = slot * (nc * G) + g * nc + c, where nc = min(rhs, 32) RHS
+// columns sit side by side, G (a power of two, BSys::groups) lanes stride over a row's entries,
+// and rpw = 32 / (nc * G) rows run side by side.  G follows the system's mean row length, so short
+// rows put many independent rows in one warp and long rows many lanes on one row.
+constexpr int kTaskRows = 256;
+
+struct RowLanes {
+    int nc, G, rpw, slot, g, c;
+    bool on;
+};
+
+__device__ __forceinline__ RowLanes row_lanes(int rhs, int G) {
+    RowLanes L;
+    L.nc = min(rhs, 32);
+    L.G = rhs > 32 ? 1 : G;
+    const int width = L.nc * L.G;
+    L.rpw = max(1, 32 / width);
+    const int lane = threadIdx.x & 31;
+    L.slot = lane / width;
+    L.g = (lane % width) / L.nc;
+    L.c = lane % L.nc;
+    L.on = L.slot < L.rpw;
+    return L;
+}
+
+// sum over the G entry groups of a row slot, into its g = 0 lanes (G a power of two)
+template <typename T>
+__device__ __forceinline__ T slot_sum(T v, const RowLanes& L) {
+    for (int off = L.G >> 1; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off * L.nc);
+    return v;
+}
+
 // --- FP32 Jacobi sweep ------------------------------------------------------------------------
 
 // d_new = (r - N d_old) * invd for the Jacobi systems still sweeping (sweep k reads d[k & 1] and
 // writes d[(k + 1) & 1]; sweep 0 starts from d = 0), with per-system max |d_new| and
-// max |d_new - d_old|.
-__global__ void __launch_bounds__(256) k_b_jacobi(BArgs A, SegList rows) {
+// max |d_new - d_old| (flushed once per task).
+__global__ void __launch_bounds__(256) k_b_jacobi(BArgs A, const int4* __restrict__ tasks, int ntasks) {
     const int k = *(volatile const int*)&A.bc->sweep_k;
     const float* src = (k & 1) ? A.d1 : A.d0;
     float* dst = (k & 1) ? A.d0 : A.d1;
     const int lane = threadIdx.x & 31;
-    float mx = 0.f, ch = 0.f;
-    for_rows(
-        rows,
-        [&](int s, int i) {
-            const BState& T = A.st[s];
-            if (T.done || T.inner_done) return;
-            const BSys S = A.sys[s];
-            const int r = S.rhs;
-            const int* rp = A.rp + S.rp0;
-            const int beg = rp[i], end = rp[i + 1];
-            const int* cl = A.col + S.nz0;
-            const float* vl = A.val32 + S.nz0;
-            const float dinv = A.invd32[S.row0 + i];
-            const float* rr = A.r32 + S.xb0;
-            const float* so = src + S.xb0;
-            float* dd = dst + S.xb0;
+    const long long gw = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+    const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long t = gw; t < ntasks; t += nw) {
+        const int4 T = tasks[t];
+        const int s = T.x;
+        const BState& St = A.st[s];
+        if (St.done || St.inner_done) continue;
+        const BSys S = A.sys[s];
+        const int r = S.rhs;
+        const RowLanes L = row_lanes(r, S.groups);
+        const int* rp = A.rp + S.rp0;
+        const int* cl = A.col + S.nz0;
+        const float* vl = A.val32 + S.nz0;
+        const float* rr = A.r32 + S.xb0;
+        const float* so = src + S.xb0;
+        float* dd = dst + S.xb0;
+        float mx = 0.f, ch = 0.f;
+        for (int i0 = T.y; i0 < T.y + T.z; i0 += L.rpw) {
+            const int i = i0 + L.slot;
+            const bool on = L.on && i < T.y + T.z;
+            const int beg = on ? rp[i] : 0, end = on ? rp[i + 1] : 0;
+            const float dinv = on ? A.invd32[S.row0 + i] : 0.f;
             for (int c0 = 0; c0 < r; c0 += 32) {
-                const int nc = min(32, r - c0);
-                int groups, g, c;
-                lane_split(nc, groups, g, c);
+                const int cc = c0 + L.c;
+                const bool col_on = on && cc < r;
                 float s0 = 0.f, s1 = 0.f;
-                if (k > 0 && g < groups) {
-                    int q = beg + 1 + g;
-                    for (; q + groups < end; q += 2 * groups) {
-                        s0 = fmaf(vl[q], so[(size_t)cl[q] * r + c0 + c], s0);
-                        s1 = fmaf(vl[q + groups], so[(size_t)cl[q + groups] * r + c0 + c], s1);
+                if (k > 0 && col_on) {
+                    int q = beg + 1 + L.g;
+                    for (; q + L.G < end; q += 2 * L.G) {
+                        s0 = fmaf(vl[q], so[(size_t)cl[q] * r + cc], s0);
+                        s1 = fmaf(vl[q + L.G], so[(size_t)cl[q + L.G] * r + cc], s1);
                     }
-                    if (q < end) s0 = fmaf(vl[q], so[(size_t)cl[q] * r + c0 + c], s0);
+                    if (q < end) s0 = fmaf(vl[q], so[(size_t)cl[q] * r + cc], s0);
                 }
-                const float sum = group_sum(s0 + s1, groups, nc);
-                if (lane < nc) {
-                    const size_t o = (size_t)i * r + c0 + lane;
+                const float sum = slot_sum(s0 + s1, L);
+                if (col_on && L.g == 0) {
+                    const size_t o = (size_t)i * r + cc;
                     const float dn = (rr[o] - sum) * dinv;
                     const float old = k > 0 ? so[o] : 0.f;
                     dd[o] = dn;
@@ -510,64 +560,66 @@ __global__ void __launch_bounds__(256) k_b_jacobi(BArgs A, SegList rows) {
                     ch = fmaxf(ch, fabsf(dn - old));
                 }
             }
-        },
-        [&](int s) {
-            const float m1 = warp_max(mx), m2 = warp_max(ch);
-            if (lane == 0 && (m1 > 0.f || m2 > 0.f)) {
-                atomicMax(&A.st[s].dmax_bits, __float_as_uint(m1));
-                atomicMax(&A.st[s].dchg_bits, __float_as_uint(m2));
-            }
-            mx = ch = 0.f;
-        });
+        }
+        const float m1 = warp_max(mx), m2 = warp_max(ch);
+        if (lane == 0 && (m1 > 0.f || m2 > 0.f)) {
+            atomicMax(&A.st[s].dmax_bits, __float_as_uint(m1));
+            atomicMax(&A.st[s].dchg_bits, __float_as_uint(m2));
+        }
+    }
 }
 
 // --- FP64 residual ----------------------------------------------------------------------------
 
-// r = b - U x in FP64 for the systems still refining; r32 = (float) r; ||r||^2 per system.
-__global__ void __launch_bounds__(256) k_b_residual(BArgs A, SegList rows) {
+// r = b - U x in FP64 for the systems still refining; r32 = (float) r; ||r||^2 per system
+// (flushed once per task).
+__global__ void __launch_bounds__(256) k_b_residual(BArgs A, const int4* __restrict__ tasks, int ntasks) {
     const int lane = threadIdx.x & 31;
-    double acc = 0.0;
-    for_rows(
-        rows,
-        [&](int s, int i) {
-            if (A.st[s].done) return;
-            const BSys S = A.sys[s];
-            const int r = S.rhs;
-            const int* rp = A.rp + S.rp0;
-            const int beg = rp[i], end = rp[i + 1];
-            const int* cl = A.col + S.nz0;
-            const double* vl = A.val + S.nz0;
-            const double* xx = A.x + S.xb0;
-            const double* bb = A.b + S.xb0;
+    const long long gw = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+    const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long t = gw; t < ntasks; t += nw) {
+        const int4 T = tasks[t];
+        const int s = T.x;
+        if (A.st[s].done) continue;
+        const BSys S = A.sys[s];
+        const int r = S.rhs;
+        const RowLanes L = row_lanes(r, S.groups);
+        const int* rp = A.rp + S.rp0;
+        const int* cl = A.col + S.nz0;
+        const double* vl = A.val + S.nz0;
+        const double* xx = A.x + S.xb0;
+        const double* bb = A.b + S.xb0;
+        double acc = 0.0;
+        for (int i0 = T.y; i0 < T.y + T.z; i0 += L.rpw) {
+            const int i = i0 + L.slot;
+            const bool on = L.on && i < T.y + T.z;
+            const int beg = on ? rp[i] : 0, end = on ? rp[i + 1] : 0;
             for (int c0 = 0; c0 < r; c0 += 32) {
-                const int nc = min(32, r - c0);
-                int groups, g, c;
-                lane_split(nc, groups, g, c);
+                const int cc = c0 + L.c;
+                const bool col_on = on && cc < r;
                 double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
-                if (g < groups) {
-                    int q = beg + g;
-                    for (; q + 3 * groups < end; q += 4 * groups) {
-                        s0 = fma(__ldg(vl + q), xx[(size_t)__ldg(cl + q) * r + c0 + c], s0);
-                        s1 = fma(__ldg(vl + q + groups), xx[(size_t)__ldg(cl + q + groups) * r + c0 + c], s1);
-                        s2 = fma(__ldg(vl + q + 2 * groups), xx[(size_t)__ldg(cl + q + 2 * groups) * r + c0 + c], s2);
-                        s3 = fma(__ldg(vl + q + 3 * groups), xx[(size_t)__ldg(cl + q + 3 * groups) * r + c0 + c], s3);
+                if (col_on) {
+                    int q = beg + L.g;
+                    for (; q + 3 * L.G < end; q += 4 * L.G) {
+                        s0 = fma(__ldg(vl + q), xx[(size_t)__ldg(cl + q) * r + cc], s0);
+                        s1 = fma(__ldg(vl + q + L.G), xx[(size_t)__ldg(cl + q + L.G) * r + cc], s1);
+                        s2 = fma(__ldg(vl + q + 2 * L.G), xx[(size_t)__ldg(cl + q + 2 * L.G) * r + cc], s2);
+                        s3 = fma(__ldg(vl + q + 3 * L.G), xx[(size_t)__ldg(cl + q + 3 * L.G) * r + cc], s3);
                     }
-                    for (; q < end; q += groups) s0 = fma(__ldg(vl + q), xx[(size_t)__ldg(cl + q) * r + c0 + c], s0);
+                    for (; q < end; q += L.G) s0 = fma(__ldg(vl + q), xx[(size_t)__ldg(cl + q) * r + cc], s0);
                 }
-                const double sum = group_sum((s0 + s1) + (s2 + s3), groups, nc);
-                if (lane < nc) {
-                    const size_t o = (size_t)i * r + c0 + lane;
+                const double sum = slot_sum((s0 + s1) + (s2 + s3), L);
+                if (col_on && L.g == 0) {
+                    const size_t o = (size_t)i * r + cc;
                     const double rv = bb[o] - sum;
                     A.r32[S.xb0 + o] = (float)rv;
                     acc = fma(rv, rv, acc);
                 }
             }
-        },
-        [&](int s) {
-            const double v = warp_sum(acc);
-            if (lane == 0 && v != 0.0) atomicAdd(&A.st[s].rnorm2, v);
-            acc = 0.0;
-        });
+        }
+        const double v = warp_sum(acc);
+        if (lane == 0 && v != 0.0) atomicAdd(&A.st[s].rnorm2, v);
+    }
 }
 
 // --- control (one block) ------------------------------------------------------------------------
@@ -633,7 +685,7 @@ __global__ void k_b_inner_begin(BArgs A, int count, cudaGraphConditionalHandle i
 
 // After a Jacobi sweep: per-system change test |d_new - d_old| <= eps |d_new| (max norms) or the
 // sweep cap.
-__global__ void k_b_jcheck(BArgs A, int count, cudaGraphConditionalHandle inner) {
+__global__ void k_b_jcheck(BArgs A, int count, cudaGraphConditionalHandle inner, bool set_cond) {
     const int k = A.bc->sweep_k;
     int still = 0, swept = 0;
     for (int s0 = 0; s0 < count; s0 += blockDim.x) {
@@ -663,12 +715,12 @@ __global__ void k_b_jcheck(BArgs A, int count, cudaGraphConditionalHandle inner)
         A.bc->jac_active = still;
         A.bc->sweep_k = k + 1;
         A.bc->total_sweeps += swept > 0 ? 1 : 0;
-        cudaGraphSetConditional(inner, still > 0 && !A.bc->c.status ? 1u : 0u);
+        if (set_cond) cudaGraphSetConditional(inner, still > 0 && !A.bc->c.status ? 1u : 0u);
     }
 }
 
 // After the residual: per-system convergence; the step loop runs while any system refines.
-__global__ void k_b_check(BArgs A, int count, cudaGraphConditionalHandle outer) {
+__global__ void k_b_check(BArgs A, int count, cudaGraphConditionalHandle outer, bool set_cond) {
     int act = 0;
     for (int s0 = 0; s0 < count; s0 += blockDim.x) {
         const int s = s0 + threadIdx.x;
@@ -695,7 +747,7 @@ __global__ void k_b_check(BArgs A, int count, cudaGraphConditionalHandle outer) 
     if (threadIdx.x == 0) {
         A.bc->active = act;
         A.bc->outer += 1;
-        cudaGraphSetConditional(outer, act > 0 && !A.bc->c.status ? 1u : 0u);
+        if (set_cond) cudaGraphSetConditional(outer, act > 0 && !A.bc->c.status ? 1u : 0u);
     }
 }
 
@@ -744,7 +796,8 @@ struct Batch {
     DevBuf rp, col, val, val32, invd, invd32, dsys, dstate, dctl;
     DevBuf r32, d0, d1, bw, xw;
     // schedule-dependent work lists
-    DevBuf order_all, order_plain, order_sf32, items, chunks;
+    DevBuf order_all, order_plain, order_sf32, items, chunks, tasks_mixed, tasks_jac;
+    int n_tasks_mixed = 0, n_tasks_jac = 0;
     unsigned n_order_all = 0, n_order_plain = 0, n_order_sf32 = 0, n_items = 0;
     DevSeg all_rows, all_el, mixed_rows, mixed_el, jac_rows, pend_el, plain_el;
     std::vector<DevBuf> gbufs;            // per panel system: hi, lo, rect
@@ -776,6 +829,7 @@ struct Batch {
     int build_graph(int mode, const double* b, double* x, cudaGraphExec_t* out, int64_t* fixed);
     int solve(int mode, const double* b, double* x);
     int sync(int64_t* kernels);
+    int profile(int mode, const double* b, double* x, float* kind_ms, int* kind_launches, float* kind_first_ms);
     void drop_graphs() {
         for (auto& g : graphs) if (g.exec) cudaGraphExecDestroy(g.exec);
         graphs.clear();
@@ -786,7 +840,7 @@ Batch::~Batch() {
     if (device >= 0) cudaSetDevice(device);
     drop_graphs();
     DevBuf* bufs[] = {&rp, &col, &val, &val32, &invd, &invd32, &dsys, &dstate, &dctl, &r32, &d0, &d1, &bw, &xw,
-                      &order_all, &order_plain, &order_sf32, &items, &chunks};
+                      &order_all, &order_plain, &order_sf32, &items, &chunks, &tasks_mixed, &tasks_jac};
     for (DevBuf* b : bufs) b->release();
     DevSeg* segs[] = {&all_rows, &all_el, &mixed_rows, &mixed_el, &jac_rows, &pend_el, &plain_el};
     for (DevSeg* s : segs) s->release();
@@ -937,6 +991,19 @@ int Batch::build_lists() {
         if (sched[s] == BS_PANEL || sched[s] == BS_SF32) pe.add(s, ne);
         if (sched[s] == BS_SF32) sf32.push_back(s);
     }
+    // row tasks of the mixed systems and of the Jacobi ones
+    std::vector<int4> tm, tj;
+    for (int s = 0; s < count; ++s) {
+        if (sched[s] == BS_PLAIN) continue;
+        for (int r0 = 0; r0 < sys[s].n; r0 += kTaskRows) {
+            const int4 t = make_int4(s, r0, std::min(kTaskRows, sys[s].n - r0), 0);
+            tm.push_back(t);
+            if (sched[s] == BS_JACOBI) tj.push_back(t);
+        }
+    }
+    n_tasks_mixed = (int)tm.size();
+    n_tasks_jac = (int)tj.size();
+    if ((rc = upload_vec(tasks_mixed, tm, st)) || (rc = upload_vec(tasks_jac, tj, st))) return rc;
     if ((rc = upload_vec(dsys, sys, st))) return rc;
     if ((rc = mixed_rows.upload(mr, st)) || (rc = mixed_el.upload(me, st)) || (rc = jac_rows.upload(jr, st)) ||
         (rc = pend_el.upload(pe, st)) || (rc = plain_el.upload(pl, st)))
@@ -979,6 +1046,10 @@ static int resident(const void* kernel, int threads, int sm_count, long long wan
 
 static int elem_grid(int sm_count, long long total) {
     return (int)std::max(1LL, std::min((long long)sm_count * 16, (total + 255) / 256));
+}
+
+static int task_grid(int sm_count, long long tasks) {
+    return (int)std::max(1LL, std::min((long long)sm_count * 8, (tasks + 7) / 8));
 }
 
 static int row_grid(int sm_count, long long rows) {
@@ -1078,8 +1149,8 @@ int Batch::build_graph(int mode, const double* b, double* x, cudaGraphExec_t* ou
             }
             if (jac_rows.nseg && add_while(obody, hi, &ibody) != cudaSuccess) rc = SPTRSV_ERR_CUDA;
             k_b_axpy<<<elem_grid(sm_count, mixed_el.total), 256, 0, st>>>(A, mixed_el.list());
-            k_b_residual<<<row_grid(sm_count, mixed_rows.total), 256, 0, st>>>(A, mixed_rows.list());
-            k_b_check<<<1, 512, 0, st>>>(A, count, ho);
+            k_b_residual<<<task_grid(sm_count, n_tasks_mixed), 256, 0, st>>>(A, tasks_mixed.as<int4>(), n_tasks_mixed);
+            k_b_check<<<1, 512, 0, st>>>(A, count, ho, true);
             nk += 3;
             per_outer = nk - k0;
             e = cudaStreamEndCapture(st, &g2);
@@ -1091,8 +1162,8 @@ int Batch::build_graph(int mode, const double* b, double* x, cudaGraphExec_t* ou
     if (!rc && ibody) {
         e = cudaStreamBeginCaptureToGraph(st, ibody, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
         if (e == cudaSuccess) {
-            k_b_jacobi<<<row_grid(sm_count, jac_rows.total), 256, 0, st>>>(A, jac_rows.list());
-            k_b_jcheck<<<1, 512, 0, st>>>(A, count, hi);
+            k_b_jacobi<<<task_grid(sm_count, n_tasks_jac), 256, 0, st>>>(A, tasks_jac.as<int4>(), n_tasks_jac);
+            k_b_jcheck<<<1, 512, 0, st>>>(A, count, hi, true);
             e = cudaStreamEndCapture(st, &g2);
             if (!rc && e != cudaSuccess) rc = set_cuda_error(e, "batch capture inner");
         } else {
@@ -1132,6 +1203,110 @@ int Batch::solve(int mode, const double* b, double* x) {
     last_mode = mode;
     last_fixed = hit->fixed;
     return 0;
+}
+
+// The same solve as the graph, driven from the host with CUDA events around every kernel (the
+// loop decisions are read back from the device after each check): per-kernel-kind device time.
+// Kinds: 0 fill x, 1 FP64 pull, 2 state init, 3 mixed init, 4 step begin, 5 fill d, 6 panels,
+// 7 FP32 pull, 8 Jacobi sweep, 9 sweep check, 10 axpy, 11 residual, 12 step check.
+int Batch::profile(int mode, const double* b, double* x, float* kind_ms, int* kind_launches, float* kind_first_ms) {
+    if ((mode != 0 && mode != 1) || !b || !x) return SPTRSV_ERR_INVALID_ARG;
+    int rc = mode == 1 ? build_lists() : 0;
+    if (rc) return rc;
+    int seen[kBatchKinds] = {0};
+    for (int k = 0; k < kBatchKinds; ++k) {
+        if (kind_ms) kind_ms[k] = 0.f;
+        if (kind_launches) kind_launches[k] = 0;
+        if (kind_first_ms) kind_first_ms[k] = 0.f;
+    }
+    const BArgs A = args(b, x);
+    cudaEvent_t e0, e1;
+    CUDA_TRY(cudaEventCreate(&e0));
+    CUDA_TRY(cudaEventCreate(&e1));
+    int64_t nk = 0;
+    auto timed = [&](int kind, auto launch) -> int {
+        CUDA_TRY(cudaEventRecord(e0, st));
+        launch();
+        CUDA_TRY(cudaEventRecord(e1, st));
+        CUDA_TRY(cudaEventSynchronize(e1));
+        CUDA_TRY(cudaGetLastError());
+        float ms = 0.f;
+        CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+        if (kind_ms) kind_ms[kind] += ms;
+        if (kind_launches) ++kind_launches[kind];
+        if (kind_first_ms && !seen[kind]++) kind_first_ms[kind] = ms;
+        ++nk;
+        return 0;
+    };
+    auto read_ctl = [&](BCtl* c) -> int {
+        CUDA_TRY(cudaMemcpyAsync(c, dctl.p, sizeof(BCtl), cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaStreamSynchronize(st));
+        return 0;
+    };
+    cudaGraphConditionalHandle none = 0;
+    CUDA_TRY(cudaMemsetAsync(A.bc, 0, sizeof(BCtl), st));
+    CUDA_TRY(cudaMemsetAsync(A.st, 0, sizeof(BState) * count, st));
+    auto pull64 = [&](const DevBuf& order, unsigned n) {
+        const int grid = resident((const void*)k_b_pull<double>, 256, sm_count, ((long long)n + 7) / 8);
+        return timed(1, [&] { k_b_pull<double><<<grid, 256, 0, st>>>(A, order.as<int2>(), n, b, x, A.val, A.invd, 0, false); });
+    };
+    if (mode == 0) {
+        if ((rc = timed(0, [&] { k_b_fill_pending<double><<<elem_grid(sm_count, all_el.total), 256, 0, st>>>(A, all_el.list(), x, false); })) ||
+            (rc = pull64(order_all, n_order_all)))
+            goto out;
+    } else {
+        if ((rc = timed(2, [&] { k_b_state_init<<<1, 512, 0, st>>>(A, count, none, false); }))) goto out;
+        if (n_order_plain &&
+            ((rc = timed(0, [&] { k_b_fill_pending<double><<<elem_grid(sm_count, plain_el.total), 256, 0, st>>>(A, plain_el.list(), x, false); })) ||
+             (rc = pull64(order_plain, n_order_plain))))
+            goto out;
+        if (mixed_el.nseg) {
+            if ((rc = timed(3, [&] { k_b_init_mixed<<<elem_grid(sm_count, mixed_el.total), 256, 0, st>>>(A, mixed_el.list()); })))
+                goto out;
+            BCtl c{};
+            for (int step = 0; step < 1000; ++step) {
+                if ((rc = timed(4, [&] { k_b_inner_begin<<<1, 512, 0, st>>>(A, count, none, false); }))) goto out;
+                if (pend_el.nseg &&
+                    (rc = timed(5, [&] { k_b_fill_pending<float><<<elem_grid(sm_count, pend_el.total), 256, 0, st>>>(A, pend_el.list(), A.d0, true); })))
+                    goto out;
+                if (n_items) {
+                    const int grid = resident((const void*)k_b_panels, 128, sm_count, n_items);
+                    if ((rc = timed(6, [&] { k_b_panels<<<grid, 128, 0, st>>>(A, items.as<int2>(), n_items, chunks.as<BChunk>()); })))
+                        goto out;
+                }
+                if (n_order_sf32) {
+                    const int grid = resident((const void*)k_b_pull<float>, 256, sm_count, ((long long)n_order_sf32 + 7) / 8);
+                    if ((rc = timed(7, [&] {
+                             k_b_pull<float><<<grid, 256, 0, st>>>(A, order_sf32.as<int2>(), n_order_sf32, A.r32, A.d0,
+                                                                   A.val32, A.invd32, 1, true);
+                         })))
+                        goto out;
+                }
+                if (jac_rows.nseg) {
+                    if ((rc = read_ctl(&c))) goto out;
+                    for (int sw = 0; sw < 100000 && c.jac_active > 0 && !c.c.status; ++sw) {
+                        if ((rc = timed(8, [&] { k_b_jacobi<<<task_grid(sm_count, n_tasks_jac), 256, 0, st>>>(A, tasks_jac.as<int4>(), n_tasks_jac); })) ||
+                            (rc = timed(9, [&] { k_b_jcheck<<<1, 512, 0, st>>>(A, count, none, false); })) ||
+                            (rc = read_ctl(&c)))
+                            goto out;
+                    }
+                }
+                if ((rc = timed(10, [&] { k_b_axpy<<<elem_grid(sm_count, mixed_el.total), 256, 0, st>>>(A, mixed_el.list()); })) ||
+                    (rc = timed(11, [&] { k_b_residual<<<task_grid(sm_count, n_tasks_mixed), 256, 0, st>>>(A, tasks_mixed.as<int4>(), n_tasks_mixed); })) ||
+                    (rc = timed(12, [&] { k_b_check<<<1, 512, 0, st>>>(A, count, none, false); })) || (rc = read_ctl(&c)))
+                    goto out;
+                if (c.active == 0 || c.c.status) break;
+            }
+        }
+    }
+out:
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    launches += nk;
+    BCtl c{};
+    CUDA_TRY(cudaMemcpy(&c, dctl.p, sizeof(c), cudaMemcpyDeviceToHost));
+    return c.c.status;
 }
 
 int Batch::sync(int64_t* kernels) {
@@ -1192,7 +1367,12 @@ int sptrsv_batch_create(sptrsv_batch* out, int device, int count, const int* n, 
         if (r[n[s]] > 0x7fffffffLL) return SPTRSV_ERR_TOO_LARGE;
         if ((long long)n[s] * rhs[s] > 0x7fffffffLL) return SPTRSV_ERR_TOO_LARGE;
         nnz[s] = r[n[s]];
-        sys[s] = BSys{n[s], rhs[s], BS_PLAIN, 0, rp0, nz0, row0, xb0};
+        // lanes per row: about four entries per lane, a power of two, within the 32 / nc lanes
+        const int nc = std::min(rhs[s], 32);
+        const double mean = (double)nnz[s] / n[s];
+        int G = 1;
+        while (G * 2 * nc <= 32 && G * 4 < mean) G *= 2;
+        sys[s] = BSys{n[s], rhs[s], BS_PLAIN, G, rp0, nz0, row0, xb0};
         rp0 += n[s] + 1;
         nz0 += nnz[s];
         row0 += n[s];
@@ -1359,6 +1539,14 @@ int sptrsv_batch_solve_host(sptrsv_batch bh, int mode, const double* h_b, double
     if ((rc = B->solve(mode, B->bw.as<double>(), B->xw.as<double>()))) return rc;
     CUDA_TRY(cudaMemcpyAsync(h_x, B->xw.p, bytes, cudaMemcpyDeviceToHost, B->st));
     return 0;
+}
+
+int sptrsv_batch_profile(sptrsv_batch bh, int mode, const double* d_b, double* d_x, float* kind_ms,
+                         int* kind_launches, float* kind_first_ms) {
+    BH();
+    const int rc = B->profile(mode, d_b, d_x, kind_ms, kind_launches, kind_first_ms);
+    sptrsv::set_last_status(rc);
+    return rc;
 }
 
 int sptrsv_batch_stats(sptrsv_batch bh, int* status, int* steps, double* rel, int* sweeps) {

@@ -294,15 +294,17 @@ def evaluate(mlp, X, T, A, default_id):
 # ---------------------------------------------------------------------------------------------
 # the batched path's schedules from the network
 
-# single-system candidate -> batched schedule (0 plain FP64, 1 Jacobi, 2 panels, 3 FP32 sync-free)
+# single-system candidate -> batched schedule (0 plain FP64, 1 Jacobi, 2 panels, 3 FP32 sync-free):
+# the supernodal candidates (FP64 or mixed) become dense panels, Jacobi stays Jacobi, the other
+# mixed ones the FP32 pull, the other FP64 ones the plain FP64 pull
 def batch_kind(cand_id):
     o = candidate(cand_id)
+    if o.schedule == 6:
+        return 2
     if o.precision == 0:
         return 0
     if o.schedule == 5:
         return 1
-    if o.schedule == 6:
-        return 2
     return 3
 
 
@@ -354,6 +356,7 @@ def main(argv=None):
     e.add_argument("--data", default=DATA)
     e.add_argument("--held-out", type=int, default=200)
     e.add_argument("--epochs", type=int, default=400)
+    e.add_argument("--save", default=None, help="write the trained network (params, normalisation) here")
     a = ap.parse_args(argv)
     if a.cmd == "build":
         d = build_dataset(a.count, a.seed, a.nmax, a.cap_ms, a.reps, a.abort_ms, a.time_limit, a.out, start=a.start,
@@ -365,9 +368,14 @@ def main(argv=None):
     else:
         d = load_dataset(a.data)
         tr, te = split(len(d["X"]), a.held_out)
+        t0 = time.time()
         mlp, losses = train(d["X"][tr], d["T"][tr], epochs=a.epochs)
+        t_train = time.time() - t0
         rep = evaluate(mlp, d["X"][te], d["T"][te], d["A"][te], fixed_default(d["T"][tr]))
-        rep["final_loss"] = float(losses[-1])
+        rep.update(train_matrices=int(len(tr)), held_out=int(len(te)), epochs=a.epochs, train_s=t_train,
+                   first_loss=float(losses[0]), final_loss=float(losses[-1]), kernel_launches=mlp.launches())
+        if a.save:
+            mlp.save(a.save)
         print(json.dumps(rep))
 
 

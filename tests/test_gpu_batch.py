@@ -215,3 +215,30 @@ def test_features_of_a_system(mixsys):
         assert f.shape == (sp.N_FEATURES,) and np.all(np.isfinite(f))
         assert abs(f[0] - math.log2(B.n[3])) < 1e-5
         assert abs(f[23] - math.log2(B.rhs[3])) < 1e-5
+
+
+def test_profile_replay_matches_graph(orc, mixsys):
+    """The host-driven, event-timed replay runs the same kernels and loop decisions as the graph."""
+    import ctypes
+    L = sp._lib.lib()
+    with mixsys.batch() as B, sp.Solver(0) as s:
+        nb = 8 * len(mixsys.b)
+        d_b, d_x = ctypes.c_void_p(), ctypes.c_void_p()
+        assert L.sptrsv_device_alloc(s.handle, nb, ctypes.byref(d_b)) == 0
+        assert L.sptrsv_device_alloc(s.handle, nb, ctypes.byref(d_x)) == 0
+        L.sptrsv_copy_h2d(s.handle, d_b, mixsys.b.ctypes.data, nb)
+        assert s.sync() == 0
+        prof = B.profile(d_b.value, d_x.value, "chosen")
+        for k in ("residual_f64", "panels_bf16x3", "jacobi_sweep", "axpy", "step_check"):
+            assert k in prof and prof[k][0] > 0 and prof[k][1] >= 1, k
+        assert prof["residual_f64"][1] == prof["step_check"][1] == max(B.stats()["steps"])
+        st = B.stats()
+        assert np.all(st["status"] == 0) and np.all(st["rel"] <= RES_TOL)
+        x = np.empty_like(mixsys.b)
+        L.sptrsv_copy_d2h(s.handle, x.ctypes.data, d_x, nb)
+        assert s.sync() == 0
+        mixsys.check(orc, B, x, [True] * B.count)
+        pp = B.profile(d_b.value, d_x.value, "plain")
+        assert set(pp) == {"fill_x", "pull_f64"}
+        L.sptrsv_device_free(s.handle, d_b)
+        L.sptrsv_device_free(s.handle, d_x)
