@@ -617,6 +617,8 @@ def run_batch(args, dist):
         "speedup_vs_plain": value / dist.ws / plain_sps,
         "max_abs_err_vs_xstar": worst,
         "refine_steps_max": int(np.max(st["steps"])), "rel_residual_max": float(np.max(st["rel"])),
+        "refine_steps_by_schedule": {k: np.bincount(st["steps"][sched == v], minlength=4).tolist()
+                                     for k, v in sp.BATCH_SCHED.items() if np.any(sched == v)},
         "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": nb, "d2h_bytes_per_step": nb},
         "roofline": ({"bound": "hbm", "kernel": {"residual_f64": "k_b_residual", "jacobi_sweep": "k_b_jacobi"}[dom],
                       "achieved": dom_bytes / (dom_first * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",

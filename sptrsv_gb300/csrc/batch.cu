@@ -13,8 +13,8 @@
 //     long), so all systems advance together and the longest chain sets the makespan;
 //   * chosen: every system by its own schedule (BS_*), the mixed ones inside one device-driven
 //     FP64 iterative refinement (conditional WHILE nodes): per step an FP32 inner solve (Jacobi
-//     sweeps to a relative change test, BF16x3 tensor-core products over dense panels, or the
-//     FP32 sync-free pull), x += d in FP64 and the FP64 residual r = b - U x, until every
+//     sweeps to a relative change test, tensor-core products over dense panels with both operands
+//     split into three BF16 terms (six products, FP32-level accuracy), or the FP32 sync-free pull), x += d in FP64 and the FP64 residual r = b - U x, until every
 //     system's ||r||_F / ||b||_F <= tol.  Converged systems drop out of the later steps.
 //     Systems scheduled BS_PLAIN are solved exactly in FP64 first, by the same persistent pull.
 //
@@ -35,7 +35,7 @@ namespace sptrsv {
 enum { BS_PLAIN = 0, BS_JACOBI = 1, BS_PANEL = 2, BS_SF32 = 3, BS_COUNT = 4 };
 
 constexpr int kBPanel = 64;     // rows per panel work item (4 warps x 16-row MMA tiles)
-constexpr int kBKc = 128;       // K rows staged per chunk
+constexpr int kBKc = 64;        // K rows staged per chunk (a multiple of 16: chunk starts stay aligned)
 constexpr int kBNc = 32;        // right-hand-side columns per pass
 constexpr int kBRowChunk = 32;  // rows per warp task in the row kernels
 constexpr int kBatchKinds = 13;  // kernel kinds of the profiled replay
@@ -69,7 +69,8 @@ struct BCtl {
 
 struct BChunk {
     int sys, a, w, m, ld, pad;
-    const __nv_bfloat16* ghi;
+    const __nv_bfloat16* ghi;  // G = ghi + gmi + glo (three BF16 terms, 24 significant bits)
+    const __nv_bfloat16* gmi;
     const __nv_bfloat16* glo;
     const int* rect;
 };
@@ -349,12 +350,13 @@ __global__ void __launch_bounds__(256) k_b_pull(BArgs A, const int2* __restrict_
 // --- BF16x3 panel products (persistent) -------------------------------------------------------
 
 // One 64-row panel of a dense chunk G = [T^-1 | -T^-1 Rect] per work item: d[rows] = G [r ; d_R].
-// K chunks are taken farthest-first, so the columns solved last (the nearest rows) are waited on
-// last.  Items of converged systems are skipped (nobody waits on them: only the same system's
+// The panel's own right-hand side chunk first, then the solved columns farthest-first, so the
+// columns solved last (the nearest rows) are waited on last.  Items of converged systems are skipped (nobody waits on them: only the same system's
 // panels read its rows).
-__global__ void __launch_bounds__(128) k_b_panels(BArgs A, const int2* __restrict__ items, unsigned nitems,
+__global__ void __launch_bounds__(128, 4) k_b_panels(BArgs A, const int2* __restrict__ items, unsigned nitems,
                                                   const BChunk* __restrict__ chunks) {
     __shared__ __align__(16) __nv_bfloat16 Vhi[kBNc][kBKc + 8];
+    __shared__ __align__(16) __nv_bfloat16 Vmi[kBNc][kBKc + 8];
     __shared__ __align__(16) __nv_bfloat16 Vlo[kBNc][kBKc + 8];
     __shared__ unsigned s_t;
     __shared__ int s_ok;
@@ -381,16 +383,21 @@ __global__ void __launch_bounds__(128) k_b_panels(BArgs A, const int2* __restric
             float acc[kBNc / 8][4];
 #pragma unroll
             for (int q = 0; q < kBNc / 8; ++q) acc[q][0] = acc[q][1] = acc[q][2] = acc[q][3] = 0.f;
+            // chunk 0 (the panel's own right-hand side, never waited on) first, then the solved
+            // columns from the farthest chunk to the nearest, so that only the last chunk's
+            // products follow the arrival of the rows solved just before this panel
             const int nk = (K + kBKc - 1) / kBKc;
-            for (int kb = nk - 1; kb >= 0; --kb) {
+            for (int ci = 0; ci < nk; ++ci) {
+                const int kb = ci == 0 ? 0 : nk - ci;
                 const int k0 = kb * kBKc, kc = min(kBKc, K - k0);
                 // this chunk's G fragments are loaded before any wait on solved columns, so their
                 // memory latency overlaps the wait instead of following it
-                uint32_t ahs[kBKc / 16][4], als[kBKc / 16][4];
+                uint32_t ahs[kBKc / 16][4], ams[kBKc / 16][4], als[kBKc / 16][4];
 #pragma unroll
                 for (int u = 0; u < kBKc / 16; ++u) {
                     if (row0 < w && u * 16 < kc) {
                         load_a(C.ghi, L, row0, w, k0 + u * 16, ahs[u]);
+                        load_a(C.gmi, L, row0, w, k0 + u * 16, ams[u]);
                         load_a(C.glo, L, row0, w, k0 + u * 16, als[u]);
                     }
                 }
@@ -424,9 +431,13 @@ __global__ void __launch_bounds__(128) k_b_panels(BArgs A, const int2* __restric
                             s_ok = 0;
                             val = 0.f;
                         }
+                        // three BF16 terms: hi + mid + lo carries the FP32 value's 24 bits
                         const __nv_bfloat16 h = __float2bfloat16_rn(val);
+                        const float r1 = val - __bfloat162float(h);
+                        const __nv_bfloat16 m = __float2bfloat16_rn(r1);
                         Vhi[j][kk] = h;
-                        Vlo[j][kk] = __float2bfloat16_rn(val - __bfloat162float(h));
+                        Vmi[j][kk] = m;
+                        Vlo[j][kk] = __float2bfloat16_rn(r1 - __bfloat162float(m));
                     }
                 }
                 __syncthreads();
@@ -442,11 +453,17 @@ __global__ void __launch_bounds__(128) k_b_panels(BArgs A, const int2* __restric
                             const int nn = q * 8 + (lane >> 2);
                             const uint32_t bh0 = *reinterpret_cast<const uint32_t*>(&Vhi[nn][kb2]);
                             const uint32_t bh1 = *reinterpret_cast<const uint32_t*>(&Vhi[nn][kb2 + 8]);
+                            const uint32_t bm0 = *reinterpret_cast<const uint32_t*>(&Vmi[nn][kb2]);
+                            const uint32_t bm1 = *reinterpret_cast<const uint32_t*>(&Vmi[nn][kb2 + 8]);
                             const uint32_t bl0 = *reinterpret_cast<const uint32_t*>(&Vlo[nn][kb2]);
                             const uint32_t bl1 = *reinterpret_cast<const uint32_t*>(&Vlo[nn][kb2 + 8]);
-                            mma_bf16(acc[q], ahs[u], bh0, bh1);
-                            mma_bf16(acc[q], ahs[u], bl0, bl1);
+                            // the six products down to 2^-16 relative, smallest first
                             mma_bf16(acc[q], als[u], bh0, bh1);
+                            mma_bf16(acc[q], ahs[u], bl0, bl1);
+                            mma_bf16(acc[q], ams[u], bm0, bm1);
+                            mma_bf16(acc[q], ams[u], bh0, bh1);
+                            mma_bf16(acc[q], ahs[u], bm0, bm1);
+                            mma_bf16(acc[q], ahs[u], bh0, bh1);
                         }
                     }
                 }
@@ -473,12 +490,14 @@ __global__ void __launch_bounds__(128) k_b_panels(BArgs A, const int2* __restric
 
 // --- row tasks ---------------------------------------------------------------------------------
 
-// A row task: up to kTaskRows consecutive rows of one system.  A warp takes a task and works on
-// `rpw` rows of it at a time: lane = slot * (nc * G) + g * nc + c, where nc = min(rhs, 32) RHS
-// columns sit side by side, G (a power of two, BSys::groups) lanes stride over a row's entries,
-// and rpw = 32 / (nc * G) rows run side by side.  G follows the system's mean row length, so short
-// rows put many independent rows in one warp and long rows many lanes on one row.
-constexpr int kTaskRows = 256;
+// A row task: consecutive rows of one system (about the same number of entries x RHS columns in
+// every task, so long-row systems get short tasks).  A warp takes a task and works on `rpw` rows of
+// it at a time: lane = slot * (nc * G) + g * nc + c, where nc = min(rhs, 32) RHS columns sit side
+// by side, G (BSys::groups) lanes stride over a row's entries, and rpw = 32 / (nc * G) rows run
+// side by side.  G follows the system's mean row length, so short rows put many independent rows
+// in one warp and long rows use every lane that the column count leaves.
+constexpr int kTaskWork = 1 << 16;  // entries x columns per task
+constexpr int kTaskRowsMax = 256;
 
 struct RowLanes {
     int nc, G, rpw, slot, g, c;
@@ -499,10 +518,13 @@ __device__ __forceinline__ RowLanes row_lanes(int rhs, int G) {
     return L;
 }
 
-// sum over the G entry groups of a row slot, into its g = 0 lanes (G a power of two)
+// sum over the G entry groups of a row slot, into its g = 0 lanes (a guarded tree: any G)
 template <typename T>
 __device__ __forceinline__ T slot_sum(T v, const RowLanes& L) {
-    for (int off = L.G >> 1; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off * L.nc);
+    for (int off = 1; off < L.G; off <<= 1) {
+        const T o = __shfl_down_sync(0xffffffffu, v, off * L.nc);
+        if ((L.g & (2 * off - 1)) == 0 && L.g + off < L.G) v += o;
+    }
     return v;
 }
 
@@ -903,6 +925,21 @@ static int upload_vec(DevBuf& d, const std::vector<T>& h, cudaStream_t st) {
     return 0;
 }
 
+// G (FP64) -> three BF16 terms hi + mid + lo (the FP32-level split of the batched panels)
+__global__ void k_b_split3(long long count, const double* __restrict__ G, __nv_bfloat16* __restrict__ hi,
+                           __nv_bfloat16* __restrict__ mi, __nv_bfloat16* __restrict__ lo) {
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < count;
+         p += (long long)gridDim.x * blockDim.x) {
+        const double g = G[p];
+        const __nv_bfloat16 h = __double2bfloat16(g);
+        const double r1 = g - (double)__bfloat162float(h);
+        const __nv_bfloat16 m = __double2bfloat16(r1);
+        hi[p] = h;
+        mi[p] = m;
+        lo[p] = __double2bfloat16(r1 - (double)__bfloat162float(m));
+    }
+}
+
 // Dense panels of system s: uniform 64-row chunks (each one a skyline or exact supernode chunk),
 // G = [T^-1 | -T^-1 Rect] formed in FP64 by the single-system supernodal analysis and kept as
 // its BF16 hi/lo split.
@@ -942,14 +979,17 @@ int Batch::build_panels(int s) {
     CUDA_TRY(cudaMemcpy(goff.data(), H.sn_goff.p, sizeof(long long) * (C + 1), cudaMemcpyDeviceToHost));
     const long long gtot = goff[C];
     const int k0 = (int)gbufs.size();
-    gbufs.resize(k0 + 3);
+    gbufs.resize(k0 + 4);
     if ((rc = gbufs[k0].ensure(2 * (size_t)gtot)) || (rc = gbufs[k0 + 1].ensure(2 * (size_t)gtot)) ||
-        (rc = gbufs[k0 + 2].ensure(sizeof(int) * ((size_t)roff[C] + 1))))
+        (rc = gbufs[k0 + 2].ensure(2 * (size_t)gtot)) ||
+        (rc = gbufs[k0 + 3].ensure(sizeof(int) * ((size_t)roff[C] + 1))))
         return rc;
-    CUDA_TRY(cudaMemcpyAsync(gbufs[k0].p, H.sn_Ghi.p, 2 * (size_t)gtot, cudaMemcpyDeviceToDevice, st));
-    CUDA_TRY(cudaMemcpyAsync(gbufs[k0 + 1].p, H.sn_Glo.p, 2 * (size_t)gtot, cudaMemcpyDeviceToDevice, st));
+    k_b_split3<<<sm_count * 16, 256, 0, st>>>(gtot, H.sn_G.as<double>(), gbufs[k0].as<__nv_bfloat16>(),
+                                             gbufs[k0 + 1].as<__nv_bfloat16>(), gbufs[k0 + 2].as<__nv_bfloat16>());
+    ++launches;
+    CUDA_TRY(cudaGetLastError());
     if (roff[C] > 0)
-        CUDA_TRY(cudaMemcpyAsync(gbufs[k0 + 2].p, H.sn_rect.p, sizeof(int) * roff[C], cudaMemcpyDeviceToDevice, st));
+        CUDA_TRY(cudaMemcpyAsync(gbufs[k0 + 3].p, H.sn_rect.p, sizeof(int) * roff[C], cudaMemcpyDeviceToDevice, st));
     CUDA_TRY(cudaStreamSynchronize(st));
     gidx[s] = k0;
     pchunks[s].clear();
@@ -961,8 +1001,9 @@ int Batch::build_panels(int s) {
         ch.m = mm[c];
         ch.ld = ld[c];
         ch.ghi = gbufs[k0].as<__nv_bfloat16>() + goff[c];
-        ch.glo = gbufs[k0 + 1].as<__nv_bfloat16>() + goff[c];
-        ch.rect = gbufs[k0 + 2].as<int>() + roff[c];
+        ch.gmi = gbufs[k0 + 1].as<__nv_bfloat16>() + goff[c];
+        ch.glo = gbufs[k0 + 2].as<__nv_bfloat16>() + goff[c];
+        ch.rect = gbufs[k0 + 3].as<int>() + roff[c];
         pchunks[s].push_back(ch);
     }
     H.drop_matrix();
@@ -995,8 +1036,14 @@ int Batch::build_lists() {
     std::vector<int4> tm, tj;
     for (int s = 0; s < count; ++s) {
         if (sched[s] == BS_PLAIN) continue;
-        for (int r0 = 0; r0 < sys[s].n; r0 += kTaskRows) {
-            const int4 t = make_int4(s, r0, std::min(kTaskRows, sys[s].n - r0), 0);
+        const long long nnz_s = (s + 1 < count ? sys[s + 1].nz0 : tot_nnz) - sys[s].nz0;
+        const int nc = std::min(sys[s].rhs, 32);
+        const int rpw = std::max(1, 32 / (nc * sys[s].groups));
+        const double per_row = std::max(1.0, (double)nnz_s / sys[s].n) * nc;
+        int rows = (int)std::min<double>(kTaskRowsMax, std::max<double>(rpw, kTaskWork / per_row));
+        rows = std::max(rpw, rows / rpw * rpw);
+        for (int r0 = 0; r0 < sys[s].n; r0 += rows) {
+            const int4 t = make_int4(s, r0, std::min(rows, sys[s].n - r0), 0);
             tm.push_back(t);
             if (sched[s] == BS_JACOBI) tj.push_back(t);
         }
@@ -1367,11 +1414,10 @@ int sptrsv_batch_create(sptrsv_batch* out, int device, int count, const int* n, 
         if (r[n[s]] > 0x7fffffffLL) return SPTRSV_ERR_TOO_LARGE;
         if ((long long)n[s] * rhs[s] > 0x7fffffffLL) return SPTRSV_ERR_TOO_LARGE;
         nnz[s] = r[n[s]];
-        // lanes per row: about four entries per lane, a power of two, within the 32 / nc lanes
+        // lanes per row: about four entries per lane, within the 32 / nc lanes
         const int nc = std::min(rhs[s], 32);
         const double mean = (double)nnz[s] / n[s];
-        int G = 1;
-        while (G * 2 * nc <= 32 && G * 4 < mean) G *= 2;
+        const int G = (int)std::max(1.0, std::min((double)(32 / nc), std::ceil(mean / 4.0)));
         sys[s] = BSys{n[s], rhs[s], BS_PLAIN, G, rp0, nz0, row0, xb0};
         rp0 += n[s] + 1;
         nz0 += nnz[s];
