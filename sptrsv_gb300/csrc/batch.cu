@@ -13,8 +13,8 @@
 //     long), so all systems advance together and the longest chain sets the makespan;
 //   * chosen: every system by its own schedule (BS_*), the mixed ones inside one device-driven
 //     FP64 iterative refinement (conditional WHILE nodes): per step an FP32 inner solve (Jacobi
-//     sweeps to a relative change test, tensor-core products over dense panels with both operands
-//     split into three BF16 terms (six products, FP32-level accuracy), or the FP32 sync-free pull), x += d in FP64 and the FP64 residual r = b - U x, until every
+//     sweeps to a relative change test, BF16x3 tensor-core products over dense panels, or the
+//     FP32 sync-free pull), x += d in FP64 and the FP64 residual r = b - U x, until every
 //     system's ||r||_F / ||b||_F <= tol.  Converged systems drop out of the later steps.
 //     Systems scheduled BS_PLAIN are solved exactly in FP64 first, by the same persistent pull.
 //
@@ -69,8 +69,7 @@ struct BCtl {
 
 struct BChunk {
     int sys, a, w, m, ld, pad;
-    const __nv_bfloat16* ghi;  // G = ghi + gmi + glo (three BF16 terms, 24 significant bits)
-    const __nv_bfloat16* gmi;
+    const __nv_bfloat16* ghi;  // G ~ ghi + glo (two BF16 terms)
     const __nv_bfloat16* glo;
     const int* rect;
 };
@@ -356,7 +355,6 @@ __global__ void __launch_bounds__(256) k_b_pull(BArgs A, const int2* __restrict_
 __global__ void __launch_bounds__(128, 4) k_b_panels(BArgs A, const int2* __restrict__ items, unsigned nitems,
                                                   const BChunk* __restrict__ chunks) {
     __shared__ __align__(16) __nv_bfloat16 Vhi[kBNc][kBKc + 8];
-    __shared__ __align__(16) __nv_bfloat16 Vmi[kBNc][kBKc + 8];
     __shared__ __align__(16) __nv_bfloat16 Vlo[kBNc][kBKc + 8];
     __shared__ unsigned s_t;
     __shared__ int s_ok;
@@ -392,12 +390,11 @@ __global__ void __launch_bounds__(128, 4) k_b_panels(BArgs A, const int2* __rest
                 const int k0 = kb * kBKc, kc = min(kBKc, K - k0);
                 // this chunk's G fragments are loaded before any wait on solved columns, so their
                 // memory latency overlaps the wait instead of following it
-                uint32_t ahs[kBKc / 16][4], ams[kBKc / 16][4], als[kBKc / 16][4];
+                uint32_t ahs[kBKc / 16][4], als[kBKc / 16][4];
 #pragma unroll
                 for (int u = 0; u < kBKc / 16; ++u) {
                     if (row0 < w && u * 16 < kc) {
                         load_a(C.ghi, L, row0, w, k0 + u * 16, ahs[u]);
-                        load_a(C.gmi, L, row0, w, k0 + u * 16, ams[u]);
                         load_a(C.glo, L, row0, w, k0 + u * 16, als[u]);
                     }
                 }
@@ -431,13 +428,9 @@ __global__ void __launch_bounds__(128, 4) k_b_panels(BArgs A, const int2* __rest
                             s_ok = 0;
                             val = 0.f;
                         }
-                        // three BF16 terms: hi + mid + lo carries the FP32 value's 24 bits
                         const __nv_bfloat16 h = __float2bfloat16_rn(val);
-                        const float r1 = val - __bfloat162float(h);
-                        const __nv_bfloat16 m = __float2bfloat16_rn(r1);
                         Vhi[j][kk] = h;
-                        Vmi[j][kk] = m;
-                        Vlo[j][kk] = __float2bfloat16_rn(r1 - __bfloat162float(m));
+                        Vlo[j][kk] = __float2bfloat16_rn(val - __bfloat162float(h));
                     }
                 }
                 __syncthreads();
@@ -453,16 +446,11 @@ __global__ void __launch_bounds__(128, 4) k_b_panels(BArgs A, const int2* __rest
                             const int nn = q * 8 + (lane >> 2);
                             const uint32_t bh0 = *reinterpret_cast<const uint32_t*>(&Vhi[nn][kb2]);
                             const uint32_t bh1 = *reinterpret_cast<const uint32_t*>(&Vhi[nn][kb2 + 8]);
-                            const uint32_t bm0 = *reinterpret_cast<const uint32_t*>(&Vmi[nn][kb2]);
-                            const uint32_t bm1 = *reinterpret_cast<const uint32_t*>(&Vmi[nn][kb2 + 8]);
                             const uint32_t bl0 = *reinterpret_cast<const uint32_t*>(&Vlo[nn][kb2]);
                             const uint32_t bl1 = *reinterpret_cast<const uint32_t*>(&Vlo[nn][kb2 + 8]);
-                            // the six products down to 2^-16 relative, smallest first
+                            // BF16x3: the cross terms first, then hi x hi
                             mma_bf16(acc[q], als[u], bh0, bh1);
                             mma_bf16(acc[q], ahs[u], bl0, bl1);
-                            mma_bf16(acc[q], ams[u], bm0, bm1);
-                            mma_bf16(acc[q], ams[u], bh0, bh1);
-                            mma_bf16(acc[q], ahs[u], bm0, bm1);
                             mma_bf16(acc[q], ahs[u], bh0, bh1);
                         }
                     }
@@ -563,16 +551,20 @@ __global__ void __launch_bounds__(256) k_b_jacobi(BArgs A, const int4* __restric
             for (int c0 = 0; c0 < r; c0 += 32) {
                 const int cc = c0 + L.c;
                 const bool col_on = on && cc < r;
-                float s0 = 0.f, s1 = 0.f;
+                float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
                 if (k > 0 && col_on) {
                     int q = beg + 1 + L.g;
-                    for (; q + L.G < end; q += 2 * L.G) {
-                        s0 = fmaf(vl[q], so[(size_t)cl[q] * r + cc], s0);
-                        s1 = fmaf(vl[q + L.G], so[(size_t)cl[q + L.G] * r + cc], s1);
+                    for (; q + 3 * L.G < end; q += 4 * L.G) {  // four entries' loads in flight together
+                        const int j0 = cl[q], j1 = cl[q + L.G], j2 = cl[q + 2 * L.G], j3 = cl[q + 3 * L.G];
+                        const float v0 = vl[q], v1 = vl[q + L.G], v2 = vl[q + 2 * L.G], v3 = vl[q + 3 * L.G];
+                        s0 = fmaf(v0, so[(size_t)j0 * r + cc], s0);
+                        s1 = fmaf(v1, so[(size_t)j1 * r + cc], s1);
+                        s2 = fmaf(v2, so[(size_t)j2 * r + cc], s2);
+                        s3 = fmaf(v3, so[(size_t)j3 * r + cc], s3);
                     }
-                    if (q < end) s0 = fmaf(vl[q], so[(size_t)cl[q] * r + cc], s0);
+                    for (; q < end; q += L.G) s0 = fmaf(vl[q], so[(size_t)cl[q] * r + cc], s0);
                 }
-                const float sum = slot_sum(s0 + s1, L);
+                const float sum = slot_sum((s0 + s1) + (s2 + s3), L);
                 if (col_on && L.g == 0) {
                     const size_t o = (size_t)i * r + cc;
                     const float dn = (rr[o] - sum) * dinv;
@@ -925,21 +917,6 @@ static int upload_vec(DevBuf& d, const std::vector<T>& h, cudaStream_t st) {
     return 0;
 }
 
-// G (FP64) -> three BF16 terms hi + mid + lo (the FP32-level split of the batched panels)
-__global__ void k_b_split3(long long count, const double* __restrict__ G, __nv_bfloat16* __restrict__ hi,
-                           __nv_bfloat16* __restrict__ mi, __nv_bfloat16* __restrict__ lo) {
-    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < count;
-         p += (long long)gridDim.x * blockDim.x) {
-        const double g = G[p];
-        const __nv_bfloat16 h = __double2bfloat16(g);
-        const double r1 = g - (double)__bfloat162float(h);
-        const __nv_bfloat16 m = __double2bfloat16(r1);
-        hi[p] = h;
-        mi[p] = m;
-        lo[p] = __double2bfloat16(r1 - (double)__bfloat162float(m));
-    }
-}
-
 // Dense panels of system s: uniform 64-row chunks (each one a skyline or exact supernode chunk),
 // G = [T^-1 | -T^-1 Rect] formed in FP64 by the single-system supernodal analysis and kept as
 // its BF16 hi/lo split.
@@ -979,17 +956,14 @@ int Batch::build_panels(int s) {
     CUDA_TRY(cudaMemcpy(goff.data(), H.sn_goff.p, sizeof(long long) * (C + 1), cudaMemcpyDeviceToHost));
     const long long gtot = goff[C];
     const int k0 = (int)gbufs.size();
-    gbufs.resize(k0 + 4);
+    gbufs.resize(k0 + 3);
     if ((rc = gbufs[k0].ensure(2 * (size_t)gtot)) || (rc = gbufs[k0 + 1].ensure(2 * (size_t)gtot)) ||
-        (rc = gbufs[k0 + 2].ensure(2 * (size_t)gtot)) ||
-        (rc = gbufs[k0 + 3].ensure(sizeof(int) * ((size_t)roff[C] + 1))))
+        (rc = gbufs[k0 + 2].ensure(sizeof(int) * ((size_t)roff[C] + 1))))
         return rc;
-    k_b_split3<<<sm_count * 16, 256, 0, st>>>(gtot, H.sn_G.as<double>(), gbufs[k0].as<__nv_bfloat16>(),
-                                             gbufs[k0 + 1].as<__nv_bfloat16>(), gbufs[k0 + 2].as<__nv_bfloat16>());
-    ++launches;
-    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaMemcpyAsync(gbufs[k0].p, H.sn_Ghi.p, 2 * (size_t)gtot, cudaMemcpyDeviceToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(gbufs[k0 + 1].p, H.sn_Glo.p, 2 * (size_t)gtot, cudaMemcpyDeviceToDevice, st));
     if (roff[C] > 0)
-        CUDA_TRY(cudaMemcpyAsync(gbufs[k0 + 3].p, H.sn_rect.p, sizeof(int) * roff[C], cudaMemcpyDeviceToDevice, st));
+        CUDA_TRY(cudaMemcpyAsync(gbufs[k0 + 2].p, H.sn_rect.p, sizeof(int) * roff[C], cudaMemcpyDeviceToDevice, st));
     CUDA_TRY(cudaStreamSynchronize(st));
     gidx[s] = k0;
     pchunks[s].clear();
@@ -1001,9 +975,8 @@ int Batch::build_panels(int s) {
         ch.m = mm[c];
         ch.ld = ld[c];
         ch.ghi = gbufs[k0].as<__nv_bfloat16>() + goff[c];
-        ch.gmi = gbufs[k0 + 1].as<__nv_bfloat16>() + goff[c];
-        ch.glo = gbufs[k0 + 2].as<__nv_bfloat16>() + goff[c];
-        ch.rect = gbufs[k0 + 3].as<int>() + roff[c];
+        ch.glo = gbufs[k0 + 1].as<__nv_bfloat16>() + goff[c];
+        ch.rect = gbufs[k0 + 2].as<int>() + roff[c];
         pchunks[s].push_back(ch);
     }
     H.drop_matrix();
@@ -1414,10 +1387,11 @@ int sptrsv_batch_create(sptrsv_batch* out, int device, int count, const int* n, 
         if (r[n[s]] > 0x7fffffffLL) return SPTRSV_ERR_TOO_LARGE;
         if ((long long)n[s] * rhs[s] > 0x7fffffffLL) return SPTRSV_ERR_TOO_LARGE;
         nnz[s] = r[n[s]];
-        // lanes per row: about four entries per lane, within the 32 / nc lanes
+        // lanes per row: about eight entries per lane, within the 32 / nc lanes (short rows:
+        // several rows side by side in a warp)
         const int nc = std::min(rhs[s], 32);
         const double mean = (double)nnz[s] / n[s];
-        const int G = (int)std::max(1.0, std::min((double)(32 / nc), std::ceil(mean / 4.0)));
+        const int G = (int)std::max(1.0, std::min((double)(32 / nc), std::ceil(mean / 8.0)));
         sys[s] = BSys{n[s], rhs[s], BS_PLAIN, G, rp0, nz0, row0, xb0};
         rp0 += n[s] + 1;
         nz0 += nnz[s];

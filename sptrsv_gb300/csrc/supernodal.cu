@@ -207,31 +207,33 @@ __global__ void __launch_bounds__(128) k_sn_solve_f64(SnArgs A, const double* __
                 const int kc = min(kKc, K - k0);
                 if (threadIdx.x == 0) s_ok = 1;
                 __syncthreads();
-                // loads of the whole chunk first (in flight together), then waits on pending values
-                constexpr int kStage = kKc * kNc / 128;
-                double v[kStage];
+                // eight loads per thread in flight together, then waits only on pending values
+                constexpr int kStage = 8;
+                for (int base = 0; base < kc * nc; base += 128 * kStage) {
+                    double v[kStage];
 #pragma unroll
-                for (int u = 0; u < kStage; ++u) {
-                    const int e = threadIdx.x + u * 128;
-                    double val = 0.0;
-                    if (e < kc * nc) {
-                        const int kk = e / nc, j = e % nc, k = k0 + kk;
-                        val = k < w ? b[(size_t)(a + k) * rhs + c0 + j] : ld_relaxed(x + (size_t)rc[k - w] * rhs + c0 + j);
-                    }
-                    v[u] = val;
-                }
-#pragma unroll
-                for (int u = 0; u < kStage; ++u) {
-                    const int e = threadIdx.x + u * 128;
-                    if (e < kc * nc) {
-                        const int kk = e / nc, j = e % nc, k = k0 + kk;
-                        double val = v[u];
-                        if (k >= w && Pend<double>::is(val) &&
-                            !wait_ready<double>(x + (size_t)rc[k - w] * rhs + c0 + j, val, ctl, budget)) {
-                            s_ok = 0;
-                            val = 0.0;
+                    for (int u = 0; u < kStage; ++u) {
+                        const int e = base + threadIdx.x + u * 128;
+                        double val = 0.0;
+                        if (e < kc * nc) {
+                            const int kk = e / nc, j = e % nc, k = k0 + kk;
+                            val = k < w ? b[(size_t)(a + k) * rhs + c0 + j] : ld_relaxed(x + (size_t)rc[k - w] * rhs + c0 + j);
                         }
-                        V[kk][j] = val;
+                        v[u] = val;
+                    }
+#pragma unroll
+                    for (int u = 0; u < kStage; ++u) {
+                        const int e = base + threadIdx.x + u * 128;
+                        if (e < kc * nc) {
+                            const int kk = e / nc, j = e % nc, k = k0 + kk;
+                            double val = v[u];
+                            if (k >= w && Pend<double>::is(val) &&
+                                !wait_ready<double>(x + (size_t)rc[k - w] * rhs + c0 + j, val, ctl, budget)) {
+                                s_ok = 0;
+                                val = 0.0;
+                            }
+                            V[kk][j] = val;
+                        }
                     }
                 }
                 __syncthreads();
@@ -299,33 +301,35 @@ __global__ void __launch_bounds__(128) k_sn_solve_bf16x3(SnArgs A, const __nv_bf
                 const int kc = min(kKc, K - k0);
                 if (threadIdx.x == 0) s_ok = 1;
                 __syncthreads();
-                // loads of the whole chunk first (in flight together), then waits on pending values
-                constexpr int kStage = kKc * kNc / 128;
+                // eight loads per thread in flight together, then waits only on pending values
+                constexpr int kStage = 8;
                 const int nc8 = (nc + 7) & ~7;
-                float v[kStage];
+                for (int base = 0; base < kKc * nc8; base += 128 * kStage) {
+                    float v[kStage];
 #pragma unroll
-                for (int u = 0; u < kStage; ++u) {
-                    const int e = threadIdx.x + u * 128;
-                    float val = 0.f;
-                    const int j = e / kKc, kk = e % kKc, k = k0 + kk;
-                    if (j < nc8 && kk < kc && j < nc)
-                        val = k < w ? b[(size_t)(a + k) * rhs + c0 + j] : ld_relaxed(x + (size_t)rc[k - w] * rhs + c0 + j);
-                    v[u] = val;
-                }
+                    for (int u = 0; u < kStage; ++u) {
+                        const int e = base + threadIdx.x + u * 128;
+                        float val = 0.f;
+                        const int j = e / kKc, kk = e % kKc, k = k0 + kk;
+                        if (j < nc8 && kk < kc && j < nc)
+                            val = k < w ? b[(size_t)(a + k) * rhs + c0 + j] : ld_relaxed(x + (size_t)rc[k - w] * rhs + c0 + j);
+                        v[u] = val;
+                    }
 #pragma unroll
-                for (int u = 0; u < kStage; ++u) {
-                    const int e = threadIdx.x + u * 128;
-                    const int j = e / kKc, kk = e % kKc, k = k0 + kk;
-                    if (j < nc8) {
-                        float val = v[u];
-                        if (kk < kc && j < nc && k >= w && Pend<float>::is(val) &&
-                            !wait_ready<float>(x + (size_t)rc[k - w] * rhs + c0 + j, val, ctl, budget)) {
-                            s_ok = 0;
-                            val = 0.f;
+                    for (int u = 0; u < kStage; ++u) {
+                        const int e = base + threadIdx.x + u * 128;
+                        const int j = e / kKc, kk = e % kKc, k = k0 + kk;
+                        if (j < nc8) {
+                            float val = v[u];
+                            if (kk < kc && j < nc && k >= w && Pend<float>::is(val) &&
+                                !wait_ready<float>(x + (size_t)rc[k - w] * rhs + c0 + j, val, ctl, budget)) {
+                                s_ok = 0;
+                                val = 0.f;
+                            }
+                            const __nv_bfloat16 h = __float2bfloat16_rn(val);
+                            Vhi[j][kk] = h;
+                            Vlo[j][kk] = __float2bfloat16_rn(val - __bfloat162float(h));
                         }
-                        const __nv_bfloat16 h = __float2bfloat16_rn(val);
-                        Vhi[j][kk] = h;
-                        Vlo[j][kk] = __float2bfloat16_rn(val - __bfloat162float(h));
                     }
                 }
                 __syncthreads();
