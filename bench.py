@@ -22,6 +22,17 @@ Reported (one JSON line on rank 0):
 --impl reference runs the reference's CPU implementation (oracle/_ref when it was compiled
 from the reference sources on this host, else the oracle's C restatement) as the arm of
 comparison.  Multi-GPU: replicas (one system per rank, no collective); value sums all ranks.
+
+Other workloads (their own JSON line, same keys where they apply):
+  --workload batch       the batched uneven mix: 512 systems, n log-uniform in [1k, 200k], half
+                         banded 2D-Laplacian Cholesky factors, half random dominant factors, RHS
+                         1-16, seed 2.  value = systems solved per second by the per-system
+                         schedules the trained selector picks (one CUDA graph, device-driven
+                         refinement); plain_fp64_syncfree = every system by the FP64 pull in one
+                         persistent launch; per-kernel device times from an event-timed replay.
+  --workload supernodal  the 40^3 nested-dissection factor at 1, 8, 32 and 128 right-hand sides:
+                         FP64 supernodal, BF16x3 supernodal + FP64 refinement, plain FP64
+                         sync-free, serial CPU.
 """
 import argparse
 import csv

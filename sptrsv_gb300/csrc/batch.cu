@@ -520,8 +520,13 @@ __device__ __forceinline__ T slot_sum(T v, const RowLanes& L) {
 
 // d_new = (r - N d_old) * invd for the Jacobi systems still sweeping (sweep k reads d[k & 1] and
 // writes d[(k + 1) & 1]; sweep 0 starts from d = 0), with per-system max |d_new| and
-// max |d_new - d_old| (flushed once per task).
+// max |d_new - d_old| (flushed once per task).  One thread per (row, RHS column) element: the
+// lanes of a warp cover 32 consecutive elements of the row-major n x rhs block (coalesced r, d
+// accesses; the lanes of one row read the same entries), each thread walks its row's entries
+// eight at a time (all eight column/value loads, then all eight gathers, in flight together) and
+// fetches the row pointers of its next element before it starts on the current one.
 __global__ void __launch_bounds__(256) k_b_jacobi(BArgs A, const int4* __restrict__ tasks, int ntasks) {
+    constexpr int kB = 8;
     const int k = *(volatile const int*)&A.bc->sweep_k;
     const float* src = (k & 1) ? A.d1 : A.d0;
     float* dst = (k & 1) ? A.d0 : A.d1;
@@ -534,46 +539,55 @@ __global__ void __launch_bounds__(256) k_b_jacobi(BArgs A, const int4* __restric
         const BState& St = A.st[s];
         if (St.done || St.inner_done) continue;
         const BSys S = A.sys[s];
-        const int r = S.rhs;
-        const RowLanes L = row_lanes(r, S.groups);
+        const int m = S.rhs;
         const int* rp = A.rp + S.rp0;
         const int* cl = A.col + S.nz0;
         const float* vl = A.val32 + S.nz0;
+        const float* invd = A.invd32 + S.row0;
         const float* rr = A.r32 + S.xb0;
         const float* so = src + S.xb0;
         float* dd = dst + S.xb0;
+        const long long e_end = (long long)(T.y + T.z) * m;
+        long long e = (long long)T.y * m + lane;
+        int i = (int)(e / m);
+        int beg = 0, end = 0;
+        if (e < e_end) { beg = __ldg(rp + i); end = __ldg(rp + i + 1); }
         float mx = 0.f, ch = 0.f;
-        for (int i0 = T.y; i0 < T.y + T.z; i0 += L.rpw) {
-            const int i = i0 + L.slot;
-            const bool on = L.on && i < T.y + T.z;
-            const int beg = on ? rp[i] : 0, end = on ? rp[i + 1] : 0;
-            const float dinv = on ? A.invd32[S.row0 + i] : 0.f;
-            for (int c0 = 0; c0 < r; c0 += 32) {
-                const int cc = c0 + L.c;
-                const bool col_on = on && cc < r;
-                float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
-                if (k > 0 && col_on) {
-                    int q = beg + 1 + L.g;
-                    for (; q + 3 * L.G < end; q += 4 * L.G) {  // four entries' loads in flight together
-                        const int j0 = cl[q], j1 = cl[q + L.G], j2 = cl[q + 2 * L.G], j3 = cl[q + 3 * L.G];
-                        const float v0 = vl[q], v1 = vl[q + L.G], v2 = vl[q + 2 * L.G], v3 = vl[q + 3 * L.G];
-                        s0 = fmaf(v0, so[(size_t)j0 * r + cc], s0);
-                        s1 = fmaf(v1, so[(size_t)j1 * r + cc], s1);
-                        s2 = fmaf(v2, so[(size_t)j2 * r + cc], s2);
-                        s3 = fmaf(v3, so[(size_t)j3 * r + cc], s3);
+        for (; e - lane < e_end; e += 32) {
+            const bool on = e < e_end;
+            const int c = (int)(e - (long long)i * m);
+            // the next element's row pointers, in flight while this one is summed
+            const long long en = e + 32;
+            const int inext = (int)(en / m);
+            int bn = 0, ennd = 0;
+            if (en < e_end) { bn = __ldg(rp + inext); ennd = __ldg(rp + inext + 1); }
+            float sum = 0.f;
+            if (on && k > 0) {
+                for (int q0 = beg + 1; q0 < end; q0 += kB) {
+                    int jj[kB];
+                    float vv[kB], gg[kB];
+#pragma unroll
+                    for (int u = 0; u < kB; ++u) {
+                        const bool in = q0 + u < end;
+                        jj[u] = in ? __ldg(cl + q0 + u) : i;
+                        vv[u] = in ? __ldg(vl + q0 + u) : 0.f;
                     }
-                    for (; q < end; q += L.G) s0 = fmaf(vl[q], so[(size_t)cl[q] * r + cc], s0);
-                }
-                const float sum = slot_sum((s0 + s1) + (s2 + s3), L);
-                if (col_on && L.g == 0) {
-                    const size_t o = (size_t)i * r + cc;
-                    const float dn = (rr[o] - sum) * dinv;
-                    const float old = k > 0 ? so[o] : 0.f;
-                    dd[o] = dn;
-                    mx = fmaxf(mx, fabsf(dn));
-                    ch = fmaxf(ch, fabsf(dn - old));
+#pragma unroll
+                    for (int u = 0; u < kB; ++u) gg[u] = so[(size_t)jj[u] * m + c];
+#pragma unroll
+                    for (int u = 0; u < kB; ++u) sum = fmaf(vv[u], gg[u], sum);
                 }
             }
+            if (on) {
+                const float dn = (rr[e] - sum) * __ldg(invd + i);
+                const float old = k > 0 ? so[e] : 0.f;
+                dd[e] = dn;
+                mx = fmaxf(mx, fabsf(dn));
+                ch = fmaxf(ch, fabsf(dn - old));
+            }
+            i = inext;
+            beg = bn;
+            end = ennd;
         }
         const float m1 = warp_max(mx), m2 = warp_max(ch);
         if (lane == 0 && (m1 > 0.f || m2 > 0.f)) {
@@ -1015,10 +1029,11 @@ int Batch::build_lists() {
         const double per_row = std::max(1.0, (double)nnz_s / sys[s].n) * nc;
         int rows = (int)std::min<double>(kTaskRowsMax, std::max<double>(rpw, kTaskWork / per_row));
         rows = std::max(rpw, rows / rpw * rpw);
-        for (int r0 = 0; r0 < sys[s].n; r0 += rows) {
-            const int4 t = make_int4(s, r0, std::min(rows, sys[s].n - r0), 0);
-            tm.push_back(t);
-            if (sched[s] == BS_JACOBI) tj.push_back(t);
+        for (int r0 = 0; r0 < sys[s].n; r0 += rows) tm.push_back(make_int4(s, r0, std::min(rows, sys[s].n - r0), 0));
+        if (sched[s] == BS_JACOBI) {
+            const int jrows = std::max(1, 1024 / sys[s].rhs);  // about 1,024 (row, column) elements per task
+            for (int r0 = 0; r0 < sys[s].n; r0 += jrows)
+                tj.push_back(make_int4(s, r0, std::min(jrows, sys[s].n - r0), 0));
         }
     }
     n_tasks_mixed = (int)tm.size();
