@@ -223,7 +223,8 @@ SPTRSV_API int sptrsv_profile_read(sptrsv_handle h, int* kinds, float* ms, int c
  * n[s] x rhs[s] per system, one system after another (sum n[s] rhs[s] doubles).
  * Schedules per system: SPTRSV_BATCH_PLAIN (exact FP64 sync-free), _JACOBI (FP32 Jacobi inside
  * the FP64 refinement), _PANEL (BF16x3 tensor-core dense 64-row panels inside the refinement;
- * rows must form skyline or supernode chunks), _SF32 (FP32 sync-free inside the refinement).
+ * rows must form skyline or supernode chunks), _SF32 (FP32 sync-free inside the refinement),
+ * _PANEL64 (exact FP64 on the same dense panels, each panel's product split over CTAs).
  * Mode 0 solves every system with the plain FP64 schedule in one persistent launch; mode 1
  * solves each with its own schedule (set_schedule; the default comes from the analysis), the
  * mixed ones until ||b - U x||_F <= tol ||b||_F per system. */
@@ -232,6 +233,7 @@ typedef struct sptrsv_batch_s* sptrsv_batch;
 #define SPTRSV_BATCH_JACOBI 1
 #define SPTRSV_BATCH_PANEL 2
 #define SPTRSV_BATCH_SF32 3
+#define SPTRSV_BATCH_PANEL64 4
 SPTRSV_API int sptrsv_batch_create(sptrsv_batch* out, int device, int count, const int* n, const int* rhs,
                                    const int64_t* row_ptr, const int* col, const double* val);
 SPTRSV_API int sptrsv_batch_destroy(sptrsv_batch b);
@@ -258,8 +260,8 @@ SPTRSV_API int sptrsv_batch_features(sptrsv_batch b, int s, float* features);
  * decisions as the graph, read back after each check); per kernel kind the summed device time
  * and launch count, and the time of its first launch (SPTRSV_BATCH_KINDS kinds: fill x, FP64
  * pull, state init, mixed init, step begin, fill d, panels, FP32 pull, Jacobi sweep, sweep check,
- * axpy, residual, step check). */
-#define SPTRSV_BATCH_KINDS 13
+ * axpy, residual, step check, FP64 panels). */
+#define SPTRSV_BATCH_KINDS 14
 SPTRSV_API int sptrsv_batch_profile(sptrsv_batch b, int mode, const double* d_b, double* d_x, float* kind_ms,
                                     int* kind_launches, float* kind_first_ms);
 SPTRSV_API int sptrsv_batch_timer_begin(sptrsv_batch b);

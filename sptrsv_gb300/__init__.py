@@ -299,7 +299,7 @@ class Solver:
 
 
 
-BATCH_SCHED = {"plain": 0, "jacobi": 1, "panel": 2, "sf32": 3}
+BATCH_SCHED = {"plain": 0, "jacobi": 1, "panel": 2, "sf32": 3, "panel64": 4}
 BATCH_MODE = {"plain": 0, "chosen": 1}
 
 
@@ -405,7 +405,7 @@ class Batch:
         return f
 
     KINDS = ("fill_x", "pull_f64", "state_init", "mixed_init", "step_begin", "fill_d", "panels_bf16x3",
-             "pull_f32", "jacobi_sweep", "sweep_check", "axpy", "residual_f64", "step_check")
+             "pull_f32", "jacobi_sweep", "sweep_check", "axpy", "residual_f64", "step_check", "panels_f64")
 
     def profile(self, d_b, d_x, mode="chosen"):
         """One host-driven solve with CUDA events around every kernel:

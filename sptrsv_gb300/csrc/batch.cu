@@ -16,7 +16,10 @@
 //     sweeps to a relative change test, BF16x3 tensor-core products over dense panels, or the
 //     FP32 sync-free pull), x += d in FP64 and the FP64 residual r = b - U x, until every
 //     system's ||r||_F / ||b||_F <= tol.  Converged systems drop out of the later steps.
-//     Systems scheduled BS_PLAIN are solved exactly in FP64 first, by the same persistent pull.
+//     Systems scheduled BS_PLAIN are solved exactly in FP64 first, by the same persistent pull;
+//     systems scheduled BS_PANEL64 exactly in FP64 on their dense panels, each panel's product
+//     split into 64-column blocks taken by different CTAs (the FP64 work spreads over the GPU,
+//     only the block of the nearest solved rows lies on the dependency chain).
 //
 // Every wait is a bounded pending-sentinel poll (common.cuh); per-system reductions are flushed
 // once per run of rows of one system, so no address sees one atomic per row.
@@ -32,13 +35,15 @@
 
 namespace sptrsv {
 
-enum { BS_PLAIN = 0, BS_JACOBI = 1, BS_PANEL = 2, BS_SF32 = 3, BS_COUNT = 4 };
+enum { BS_PLAIN = 0, BS_JACOBI = 1, BS_PANEL = 2, BS_SF32 = 3, BS_PANEL64 = 4, BS_COUNT = 5 };
 
 constexpr int kBPanel = 64;     // rows per panel work item (4 warps x 16-row MMA tiles)
 constexpr int kBKc = 64;        // K rows staged per chunk (a multiple of 16: chunk starts stay aligned)
 constexpr int kBNc = 32;        // right-hand-side columns per pass
 constexpr int kBRowChunk = 32;  // rows per warp task in the row kernels
-constexpr int kBatchKinds = 13;  // kernel kinds of the profiled replay
+constexpr int kBatchKinds = 14;  // kernel kinds of the profiled replay
+constexpr int kP64 = 64;         // columns of G per FP64 panel work item
+constexpr int kP64Nc = 16;       // right-hand-side columns per pass of an FP64 panel work item
 
 struct BSys {
     int n, rhs, sched, groups;  // groups: lanes per row in the row kernels (row_lanes)
@@ -71,7 +76,10 @@ struct BChunk {
     int sys, a, w, m, ld, pad;
     const __nv_bfloat16* ghi;  // G ~ ghi + glo (two BF16 terms)
     const __nv_bfloat16* glo;
+    const double* g64;         // G in FP64 (the exact panel schedule)
     const int* rect;
+    long long poff;            // FP64 schedule: first partial-sum slot of the chunk
+    int nblk;                  // FP64 schedule: 64-column blocks of G
 };
 
 // A list of systems with the prefix of their row (or element) counts.
@@ -476,6 +484,110 @@ __global__ void __launch_bounds__(128, 4) k_b_panels(BArgs A, const int2* __rest
     }
 }
 
+// --- exact FP64 panels, split over CTAs ---------------------------------------------------------
+
+// Work item (chunk, block): the block's 64 columns of G times the matching rows of [b ; x_R]
+// (waiting on solved rows), written to the chunk's partial-sum slot for that block.  The CTA that
+// completes a chunk's last block sums the partials in block order (deterministic) and publishes
+// the chunk's rows of x.  Blocks of a chunk depend only on rows of later chunks, whose items hold
+// smaller tickets, so the ticket order guarantees progress.
+__global__ void __launch_bounds__(128) k_b_panels64(BArgs A, const int2* __restrict__ items, unsigned nitems,
+                                                    const BChunk* __restrict__ chunks, double* __restrict__ part,
+                                                    int* __restrict__ cnt) {
+    __shared__ double Gs[kBPanel][kP64 + 1];
+    __shared__ double Vs[kP64][kP64Nc + 1];
+    __shared__ unsigned s_t;
+    __shared__ int s_ok, s_last;
+    Ctl* ctl = &A.bc->c;
+    for (;;) {
+        if (threadIdx.x == 0) s_t = aborted(ctl) ? 0xFFFFFFFFu : atomicAdd(&ctl->ticket2, 1u);
+        __syncthreads();
+        const unsigned t = s_t;
+        __syncthreads();
+        if (t >= nitems) break;
+        const int2 it = items[t];
+        const BChunk C = chunks[it.x];
+        const BSys S = A.sys[C.sys];
+        const int a = C.a, w = C.w, K = C.w + C.m, L = C.ld, m = S.rhs, blk = it.y;
+        const int k0 = blk * kP64, kc = min(kP64, K - k0);
+        const double* b = A.b + S.xb0;
+        double* x = A.x + S.xb0;
+        double* pb = part + C.poff + (long long)blk * w * m;
+        // the block of G (rows of the chunk, columns k0 .. k0+kc), staged once for every RHS pass
+        for (int e = threadIdx.x; e < kBPanel * kP64; e += blockDim.x) {
+            const int r = e / kP64, kk = e - r * kP64;
+            Gs[r][kk] = (r < w && kk < kc) ? C.g64[(size_t)r * L + k0 + kk] : 0.0;
+        }
+        bool ok = true;
+        for (int c0 = 0; c0 < m; c0 += kP64Nc) {
+            const int nc = min(kP64Nc, m - c0);
+            if (threadIdx.x == 0) s_ok = 1;
+            __syncthreads();
+            // eight loads per thread in flight together, then waits only on pending values
+            constexpr int kStage = 8;
+            for (int base = 0; base < kc * nc; base += 128 * kStage) {
+                double v[kStage];
+#pragma unroll
+                for (int u = 0; u < kStage; ++u) {
+                    const int e = base + threadIdx.x + u * 128;
+                    double val = 0.0;
+                    if (e < kc * nc) {
+                        const int kk = e / nc, j = e - kk * nc, k = k0 + kk;
+                        val = k < w ? b[(size_t)(a + k) * m + c0 + j] : ld_relaxed(x + (size_t)C.rect[k - w] * m + c0 + j);
+                    }
+                    v[u] = val;
+                }
+#pragma unroll
+                for (int u = 0; u < kStage; ++u) {
+                    const int e = base + threadIdx.x + u * 128;
+                    if (e < kc * nc) {
+                        const int kk = e / nc, j = e - kk * nc, k = k0 + kk;
+                        double val = v[u];
+                        if (k >= w && Pend<double>::is(val) &&
+                            !wait_ready<double>(x + (size_t)C.rect[k - w] * m + c0 + j, val, ctl, A.budget)) {
+                            s_ok = 0;
+                            val = 0.0;
+                        }
+                        Vs[kk][j] = val;
+                    }
+                }
+            }
+            __syncthreads();
+            if (!s_ok) { ok = false; break; }
+            for (int o = threadIdx.x; o < w * nc; o += blockDim.x) {
+                const int r = o / nc, j = o - r * nc;
+                double s0 = 0.0, s1 = 0.0;
+                int kk = 0;
+                for (; kk + 1 < kc; kk += 2) {
+                    s0 = fma(Gs[r][kk], Vs[kk][j], s0);
+                    s1 = fma(Gs[r][kk + 1], Vs[kk + 1][j], s1);
+                }
+                if (kk < kc) s0 = fma(Gs[r][kk], Vs[kk][j], s0);
+                pb[(size_t)r * m + c0 + j] = s0 + s1;
+            }
+            __syncthreads();
+        }
+        __threadfence();  // this thread's partial sums visible before the chunk's count moves
+        if (__syncthreads_or(!ok)) break;
+        // the last block of the chunk sums the partials in block order and publishes the rows
+        if (threadIdx.x == 0) {
+            __threadfence();
+            s_last = atomicAdd(&cnt[it.x], 1) == C.nblk - 1;
+            if (s_last) __threadfence();
+        }
+        __syncthreads();
+        if (s_last) {
+            const double* p0 = part + C.poff;
+            for (int o = threadIdx.x; o < w * m; o += blockDim.x) {
+                double v = 0.0;
+                for (int q = 0; q < C.nblk; ++q) v += __ldcg(p0 + (long long)q * w * m + o);
+                const int r = o / m, j = o - r * m;
+                st_relaxed(x + (size_t)(a + r) * m + j, Pend<double>::fix(v));
+            }
+        }
+    }
+}
+
 // --- row tasks ---------------------------------------------------------------------------------
 
 // A row task: consecutive rows of one system (about the same number of entries x RHS columns in
@@ -672,7 +784,7 @@ __global__ void k_b_state_init(BArgs A, int count, cudaGraphConditionalHandle ou
         int m = 0;
         if (s < count) {
             BState& T = A.st[s];
-            T.done = A.sys[s].sched == BS_PLAIN ? 1 : 0;
+            T.done = (A.sys[s].sched == BS_PLAIN || A.sys[s].sched == BS_PANEL64) ? 1 : 0;
             m = !T.done;
         }
         mine += block_count(m);
@@ -820,12 +932,16 @@ struct Batch {
     std::vector<float> ratio;
     std::vector<int> sched;
     std::vector<int> panel_ok;  // -1 unknown, 0 no, 1 yes
+    std::vector<char> have_bf16, have_f64;
     long long tot_rows = 0, tot_nnz = 0, tot_x = 0, tot_rp = 0;
     DevBuf rp, col, val, val32, invd, invd32, dsys, dstate, dctl;
     DevBuf r32, d0, d1, bw, xw;
     // schedule-dependent work lists
     DevBuf order_all, order_plain, order_sf32, items, chunks, tasks_mixed, tasks_jac;
     int n_tasks_mixed = 0, n_tasks_jac = 0;
+    DevBuf items64, chunks64, part64, cnt64;  // exact FP64 panels
+    unsigned n_items64 = 0;
+    int n_chunks64 = 0;
     unsigned n_order_all = 0, n_order_plain = 0, n_order_sf32 = 0, n_items = 0;
     DevSeg all_rows, all_el, mixed_rows, mixed_el, jac_rows, pend_el, plain_el;
     std::vector<DevBuf> gbufs;            // per panel system: hi, lo, rect
@@ -853,7 +969,7 @@ struct Batch {
     ~Batch();
     BArgs args(const double* b, double* x) const;
     int build_lists();
-    int build_panels(int s);
+    int build_panels(int s, bool f64);
     int build_graph(int mode, const double* b, double* x, cudaGraphExec_t* out, int64_t* fixed);
     int solve(int mode, const double* b, double* x);
     int sync(int64_t* kernels);
@@ -868,7 +984,8 @@ Batch::~Batch() {
     if (device >= 0) cudaSetDevice(device);
     drop_graphs();
     DevBuf* bufs[] = {&rp, &col, &val, &val32, &invd, &invd32, &dsys, &dstate, &dctl, &r32, &d0, &d1, &bw, &xw,
-                      &order_all, &order_plain, &order_sf32, &items, &chunks, &tasks_mixed, &tasks_jac};
+                      &order_all, &order_plain, &order_sf32, &items, &chunks, &tasks_mixed, &tasks_jac,
+                      &items64, &chunks64, &part64, &cnt64};
     for (DevBuf* b : bufs) b->release();
     DevSeg* segs[] = {&all_rows, &all_el, &mixed_rows, &mixed_el, &jac_rows, &pend_el, &plain_el};
     for (DevSeg* s : segs) s->release();
@@ -934,8 +1051,9 @@ static int upload_vec(DevBuf& d, const std::vector<T>& h, cudaStream_t st) {
 // Dense panels of system s: uniform 64-row chunks (each one a skyline or exact supernode chunk),
 // G = [T^-1 | -T^-1 Rect] formed in FP64 by the single-system supernodal analysis and kept as
 // its BF16 hi/lo split.
-int Batch::build_panels(int s) {
-    if (panel_ok[s] >= 0) return panel_ok[s] ? 0 : SPTRSV_ERR_SUPERNODES;
+int Batch::build_panels(int s, bool f64) {
+    if (panel_ok[s] == 0) return SPTRSV_ERR_SUPERNODES;
+    if (panel_ok[s] == 1 && (f64 ? have_f64[s] : have_bf16[s])) return 0;
     int rc;
     if (!scratch) {
         sptrsv_handle h = nullptr;
@@ -969,17 +1087,23 @@ int Batch::build_panels(int s) {
     CUDA_TRY(cudaMemcpy(ld.data(), H.sn_ld.p, sizeof(int) * C, cudaMemcpyDeviceToHost));
     CUDA_TRY(cudaMemcpy(goff.data(), H.sn_goff.p, sizeof(long long) * (C + 1), cudaMemcpyDeviceToHost));
     const long long gtot = goff[C];
+    // buffers of this system: [bf16 hi, bf16 lo] and/or [f64], then the rectangle columns
     const int k0 = (int)gbufs.size();
-    gbufs.resize(k0 + 3);
-    if ((rc = gbufs[k0].ensure(2 * (size_t)gtot)) || (rc = gbufs[k0 + 1].ensure(2 * (size_t)gtot)) ||
-        (rc = gbufs[k0 + 2].ensure(sizeof(int) * ((size_t)roff[C] + 1))))
-        return rc;
-    CUDA_TRY(cudaMemcpyAsync(gbufs[k0].p, H.sn_Ghi.p, 2 * (size_t)gtot, cudaMemcpyDeviceToDevice, st));
-    CUDA_TRY(cudaMemcpyAsync(gbufs[k0 + 1].p, H.sn_Glo.p, 2 * (size_t)gtot, cudaMemcpyDeviceToDevice, st));
+    gbufs.resize(k0 + 4);
+    if ((rc = gbufs[k0 + 3].ensure(sizeof(int) * ((size_t)roff[C] + 1)))) return rc;
+    if (!f64) {
+        if ((rc = gbufs[k0].ensure(2 * (size_t)gtot)) || (rc = gbufs[k0 + 1].ensure(2 * (size_t)gtot))) return rc;
+        CUDA_TRY(cudaMemcpyAsync(gbufs[k0].p, H.sn_Ghi.p, 2 * (size_t)gtot, cudaMemcpyDeviceToDevice, st));
+        CUDA_TRY(cudaMemcpyAsync(gbufs[k0 + 1].p, H.sn_Glo.p, 2 * (size_t)gtot, cudaMemcpyDeviceToDevice, st));
+    } else {
+        if ((rc = gbufs[k0 + 2].ensure(sizeof(double) * (size_t)gtot))) return rc;
+        CUDA_TRY(cudaMemcpyAsync(gbufs[k0 + 2].p, H.sn_G.p, sizeof(double) * (size_t)gtot, cudaMemcpyDeviceToDevice, st));
+    }
     if (roff[C] > 0)
-        CUDA_TRY(cudaMemcpyAsync(gbufs[k0 + 2].p, H.sn_rect.p, sizeof(int) * roff[C], cudaMemcpyDeviceToDevice, st));
+        CUDA_TRY(cudaMemcpyAsync(gbufs[k0 + 3].p, H.sn_rect.p, sizeof(int) * roff[C], cudaMemcpyDeviceToDevice, st));
     CUDA_TRY(cudaStreamSynchronize(st));
-    gidx[s] = k0;
+    // keep the other precision's pointers of an earlier build
+    std::vector<BChunk> old = pchunks[s];
     pchunks[s].clear();
     for (int c = 0; c < C; ++c) {
         BChunk ch{};
@@ -988,13 +1112,24 @@ int Batch::build_panels(int s) {
         ch.w = ss[c + 1] - ss[c];
         ch.m = mm[c];
         ch.ld = ld[c];
-        ch.ghi = gbufs[k0].as<__nv_bfloat16>() + goff[c];
-        ch.glo = gbufs[k0 + 1].as<__nv_bfloat16>() + goff[c];
-        ch.rect = gbufs[k0 + 2].as<int>() + roff[c];
+        ch.nblk = (ch.w + ch.m + kP64 - 1) / kP64;
+        if (!f64) {
+            ch.ghi = gbufs[k0].as<__nv_bfloat16>() + goff[c];
+            ch.glo = gbufs[k0 + 1].as<__nv_bfloat16>() + goff[c];
+            if ((int)old.size() == C) ch.g64 = old[c].g64;
+        } else {
+            ch.g64 = gbufs[k0 + 2].as<double>() + goff[c];
+            if ((int)old.size() == C) {
+                ch.ghi = old[c].ghi;
+                ch.glo = old[c].glo;
+            }
+        }
+        ch.rect = gbufs[k0 + 3].as<int>() + roff[c];
         pchunks[s].push_back(ch);
     }
     H.drop_matrix();
     panel_ok[s] = 1;
+    (f64 ? have_f64 : have_bf16)[s] = 1;
     return 0;
 }
 
@@ -1002,14 +1137,15 @@ int Batch::build_lists() {
     if (lists_ready) return 0;
     int rc;
     for (int s = 0; s < count; ++s)
-        if (sched[s] == BS_PANEL && (rc = build_panels(s))) return rc;
+        if ((sched[s] == BS_PANEL || sched[s] == BS_PANEL64) && (rc = build_panels(s, sched[s] == BS_PANEL64)))
+            return rc;
     std::vector<int> plain, sf32;
     HostSeg mr, me, jr, pe, pl;
     for (int s = 0; s < count; ++s) {
         const long long n = sys[s].n, ne = n * sys[s].rhs;
         sys[s].sched = sched[s];
-        if (sched[s] == BS_PLAIN) {
-            plain.push_back(s);
+        if (sched[s] == BS_PLAIN || sched[s] == BS_PANEL64) {
+            if (sched[s] == BS_PLAIN) plain.push_back(s);
             pl.add(s, ne);
             continue;
         }
@@ -1022,7 +1158,7 @@ int Batch::build_lists() {
     // row tasks of the mixed systems and of the Jacobi ones
     std::vector<int4> tm, tj;
     for (int s = 0; s < count; ++s) {
-        if (sched[s] == BS_PLAIN) continue;
+        if (sched[s] == BS_PLAIN || sched[s] == BS_PANEL64) continue;
         const long long nnz_s = (s + 1 < count ? sys[s + 1].nz0 : tot_nnz) - sys[s].nz0;
         const int nc = std::min(sys[s].rhs, 32);
         const int rpw = std::max(1, 32 / (nc * sys[s].groups));
@@ -1067,6 +1203,40 @@ int Batch::build_lists() {
             if (t < v.size()) it.push_back(v[t]);
     n_items = (unsigned)it.size();
     if ((rc = upload_vec(chunks, ch, st)) || (rc = upload_vec(items, it, st))) return rc;
+    // exact FP64 panel items: per chunk (last first) its own right-hand-side blocks, then the solved
+    // column blocks farthest first; chunks interleaved across systems; partial-sum slots per chunk
+    std::vector<BChunk> ch64;
+    std::vector<std::vector<int2>> per64;
+    long long poff = 0;
+    for (int s = 0; s < count; ++s) {
+        if (sched[s] != BS_PANEL64) continue;
+        const int base = (int)ch64.size();
+        std::vector<int2> its;
+        for (int c = (int)pchunks[s].size() - 1; c >= 0; --c) {
+            const BChunk& b = pchunks[s][c];
+            const int own = (b.w + kP64 - 1) / kP64;
+            for (int q = 0; q < own && q < b.nblk; ++q) its.push_back(make_int2(base + c, q));
+            for (int q = b.nblk - 1; q >= own; --q) its.push_back(make_int2(base + c, q));
+        }
+        for (BChunk b : pchunks[s]) {
+            b.poff = poff;
+            poff += (long long)b.nblk * b.w * sys[s].rhs;
+            ch64.push_back(b);
+        }
+        per64.push_back(std::move(its));
+    }
+    std::vector<int2> it64;
+    size_t longest64 = 0;
+    for (auto& v : per64) longest64 = std::max(longest64, v.size());
+    for (size_t t = 0; t < longest64; ++t)
+        for (auto& v : per64)
+            if (t < v.size()) it64.push_back(v[t]);
+    n_items64 = (unsigned)it64.size();
+    n_chunks64 = (int)ch64.size();
+    if ((rc = upload_vec(chunks64, ch64, st)) || (rc = upload_vec(items64, it64, st))) return rc;
+    if (n_chunks64 && ((rc = part64.ensure(sizeof(double) * (size_t)std::max(1LL, poff))) ||
+                       (rc = cnt64.ensure(sizeof(int) * (size_t)n_chunks64))))
+        return rc;
     lists_ready = true;
     drop_graphs();
     return 0;
@@ -1145,10 +1315,17 @@ int Batch::build_graph(int mode, const double* b, double* x, cudaGraphExec_t* ou
     } else {
         k_b_state_init<<<1, 512, 0, st>>>(A, count, ho, mixed_el.nseg > 0);
         ++nk;
-        if (n_order_plain) {
+        if (plain_el.nseg) {
             k_b_fill_pending<double><<<elem_grid(sm_count, plain_el.total), 256, 0, st>>>(A, plain_el.list(), x, false);
             ++nk;
-            launch_pull64(order_plain, n_order_plain);
+        }
+        if (n_order_plain) launch_pull64(order_plain, n_order_plain);
+        if (n_items64) {
+            cudaMemsetAsync(cnt64.p, 0, sizeof(int) * n_chunks64, st);
+            const int grid = resident((const void*)k_b_panels64, 128, sm_count, n_items64);
+            k_b_panels64<<<grid, 128, 0, st>>>(A, items64.as<int2>(), n_items64, chunks64.as<BChunk>(),
+                                               part64.as<double>(), cnt64.as<int>());
+            ++nk;
         }
         if (mixed_el.nseg) {
             k_b_init_mixed<<<elem_grid(sm_count, mixed_el.total), 256, 0, st>>>(A, mixed_el.list());
@@ -1243,7 +1420,7 @@ int Batch::solve(int mode, const double* b, double* x) {
 // The same solve as the graph, driven from the host with CUDA events around every kernel (the
 // loop decisions are read back from the device after each check): per-kernel-kind device time.
 // Kinds: 0 fill x, 1 FP64 pull, 2 state init, 3 mixed init, 4 step begin, 5 fill d, 6 panels,
-// 7 FP32 pull, 8 Jacobi sweep, 9 sweep check, 10 axpy, 11 residual, 12 step check.
+// 7 FP32 pull, 8 Jacobi sweep, 9 sweep check, 10 axpy, 11 residual, 12 step check, 13 FP64 panels.
 int Batch::profile(int mode, const double* b, double* x, float* kind_ms, int* kind_launches, float* kind_first_ms) {
     if ((mode != 0 && mode != 1) || !b || !x) return SPTRSV_ERR_INVALID_ARG;
     int rc = mode == 1 ? build_lists() : 0;
@@ -1291,10 +1468,19 @@ int Batch::profile(int mode, const double* b, double* x, float* kind_ms, int* ki
             goto out;
     } else {
         if ((rc = timed(2, [&] { k_b_state_init<<<1, 512, 0, st>>>(A, count, none, false); }))) goto out;
-        if (n_order_plain &&
-            ((rc = timed(0, [&] { k_b_fill_pending<double><<<elem_grid(sm_count, plain_el.total), 256, 0, st>>>(A, plain_el.list(), x, false); })) ||
-             (rc = pull64(order_plain, n_order_plain))))
+        if (plain_el.nseg &&
+            (rc = timed(0, [&] { k_b_fill_pending<double><<<elem_grid(sm_count, plain_el.total), 256, 0, st>>>(A, plain_el.list(), x, false); })))
             goto out;
+        if (n_order_plain && (rc = pull64(order_plain, n_order_plain))) goto out;
+        if (n_items64) {
+            CUDA_TRY(cudaMemsetAsync(cnt64.p, 0, sizeof(int) * n_chunks64, st));
+            const int grid = resident((const void*)k_b_panels64, 128, sm_count, n_items64);
+            if ((rc = timed(13, [&] {
+                     k_b_panels64<<<grid, 128, 0, st>>>(A, items64.as<int2>(), n_items64, chunks64.as<BChunk>(),
+                                                        part64.as<double>(), cnt64.as<int>());
+                 })))
+                goto out;
+        }
         if (mixed_el.nseg) {
             if ((rc = timed(3, [&] { k_b_init_mixed<<<elem_grid(sm_count, mixed_el.total), 256, 0, st>>>(A, mixed_el.list()); })))
                 goto out;
@@ -1425,6 +1611,8 @@ int sptrsv_batch_create(sptrsv_batch* out, int device, int count, const int* n, 
     B->tot_x = xb0;
     B->sched.assign(count, BS_PLAIN);
     B->panel_ok.assign(count, -1);
+    B->have_bf16.assign(count, 0);
+    B->have_f64.assign(count, 0);
     B->gidx.assign(count, -1);
     B->pchunks.resize(count);
     int rc = 0;
@@ -1527,8 +1715,8 @@ int sptrsv_batch_set_schedule(sptrsv_batch bh, const int* sched) {
     for (int s = 0; s < B->count; ++s)
         if (sched[s] < -1 || sched[s] >= BS_COUNT) return SPTRSV_ERR_INVALID_ARG;
     for (int s = 0; s < B->count; ++s) {
-        if (sched[s] == BS_PANEL) {
-            const int rc = B->build_panels(s);
+        if (sched[s] == BS_PANEL || sched[s] == BS_PANEL64) {
+            const int rc = B->build_panels(s, sched[s] == BS_PANEL64);
             if (rc) return rc;
         }
         if (sched[s] == BS_JACOBI && !(B->ratio[s] < 1.f)) return SPTRSV_ERR_UNSUPPORTED;

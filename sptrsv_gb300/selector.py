@@ -294,13 +294,14 @@ def evaluate(mlp, X, T, A, default_id):
 # ---------------------------------------------------------------------------------------------
 # the batched path's schedules from the network
 
-# single-system candidate -> batched schedule (0 plain FP64, 1 Jacobi, 2 panels, 3 FP32 sync-free):
-# the supernodal candidates (FP64 or mixed) become dense panels, Jacobi stays Jacobi, the other
-# mixed ones the FP32 pull, the other FP64 ones the plain FP64 pull
+# single-system candidate -> batched schedule (0 plain FP64, 1 Jacobi, 2 BF16x3 panels in the
+# refinement, 3 FP32 sync-free, 4 exact FP64 panels): the supernodal candidates become dense panels
+# of their precision, Jacobi stays Jacobi, the other mixed ones the FP32 pull, the other FP64 ones
+# the plain FP64 pull
 def batch_kind(cand_id):
     o = candidate(cand_id)
     if o.schedule == 6:
-        return 2
+        return 4 if o.precision == 0 else 2
     if o.precision == 0:
         return 0
     if o.schedule == 5:
@@ -325,7 +326,7 @@ def batch_schedule(batch, mlp):
                 continue  # single-RHS candidates
             if kind == 1 and not info["ratio"][s] < 1.0:
                 continue
-            if kind == 2 and F[s, 21] == 0.0:
+            if kind in (2, 4) and F[s, 21] == 0.0:
                 continue  # no panel structure
             if o.schedule == 6 and F[s, 21] == 0.0:
                 continue

@@ -140,20 +140,33 @@ def test_chosen_default_schedules(orc, mixsys):
         assert np.array_equal(x, x2)
 
 
-@pytest.mark.parametrize("kind", ["plain", "jacobi", "sf32", "panel"])
+@pytest.mark.parametrize("kind", ["plain", "jacobi", "sf32", "panel", "panel64"])
 def test_every_schedule(orc, mixsys, kind):
     with mixsys.batch() as B:
         want = sp.BATCH_SCHED[kind]
         sched = B.schedule.copy()
         for s in range(B.count):
-            if kind != "panel" or s % 2 == 0:
+            if not kind.startswith("panel") or s % 2 == 0:
                 sched[s] = want
         B.schedule = sched
         x = B.solve(mixsys.b, mode="chosen")
         st = B.stats()
         assert np.all(st["status"] == 0)
-        mixed = [int(v) != 0 for v in B.schedule]
+        mixed = [int(v) not in (0, 4) for v in B.schedule]
         mixsys.check(orc, B, x, mixed)
+
+
+def test_panel_schedules_switch_both_ways(orc, mixsys):
+    """A banded system moved between the BF16x3 and the exact FP64 panels keeps both builds."""
+    with mixsys.batch() as B:
+        sched = B.schedule.copy()
+        for kinds in ((4, 2), (2, 4)):
+            for k in kinds:
+                sched[0] = sched[2] = k
+                B.schedule = sched
+                x = B.solve(mixsys.b, mode="chosen")
+                assert np.all(B.stats()["status"] == 0)
+                mixsys.check(orc, B, x, [int(v) not in (0, 4) for v in B.schedule])
 
 
 def test_panel_needs_dense_rows(mixsys):
@@ -238,6 +251,14 @@ def test_profile_replay_matches_graph(orc, mixsys):
         L.sptrsv_copy_d2h(s.handle, x.ctypes.data, d_x, nb)
         assert s.sync() == 0
         mixsys.check(orc, B, x, [True] * B.count)
+        sched = B.schedule.copy()
+        sched[0::2] = 4  # the banded systems on the exact FP64 panels
+        B.schedule = sched
+        prof = B.profile(d_b.value, d_x.value, "chosen")
+        assert prof["panels_f64"][1] == 1 and "panels_bf16x3" not in prof
+        L.sptrsv_copy_d2h(s.handle, x.ctypes.data, d_x, nb)
+        assert s.sync() == 0
+        mixsys.check(orc, B, x, [int(v) not in (0, 4) for v in B.schedule])
         pp = B.profile(d_b.value, d_x.value, "plain")
         assert set(pp) == {"fill_x", "pull_f64"}
         L.sptrsv_device_free(s.handle, d_b)
