@@ -44,6 +44,7 @@ constexpr int kBRowChunk = 32;  // rows per warp task in the row kernels
 constexpr int kBatchKinds = 14;  // kernel kinds of the profiled replay
 constexpr int kP64 = 64;         // columns of G per FP64 panel work item
 constexpr int kP64Nc = 16;       // right-hand-side columns per pass of an FP64 panel work item
+constexpr int kP64CtasPerSm = 2; // FP64 panel CTAs per SM while the refinement runs beside them
 
 struct BSys {
     int n, rhs, sched, groups;  // groups: lanes per row in the row kernels (row_lanes)
@@ -70,6 +71,8 @@ struct BCtl {
     int outer;       // refinement steps taken
     int total_sweeps;
     int nmixed;
+    unsigned ticket_p64;  // work queue of the exact FP64 panels (runs beside the refinement)
+    int pad;
 };
 
 struct BChunk {
@@ -486,6 +489,32 @@ __global__ void __launch_bounds__(128, 4) k_b_panels(BArgs A, const int2* __rest
 
 // --- exact FP64 panels, split over CTAs ---------------------------------------------------------
 
+// Column blocks of a chunk's G (w own columns, then K - w solved columns): block 0 the own part;
+// blocks 1..nnear the nearest 64 solved columns in 16-column pieces (the rows published last, so
+// only one narrow block per CTA lies on the dependency chain); then 64-column blocks.
+constexpr int kP64Near = 16;
+__host__ __device__ __forceinline__ int p64_nnear(int w, int K) {
+    const int R = K - w;
+    return R <= 0 ? 0 : min(kP64 / kP64Near, (R + kP64Near - 1) / kP64Near);
+}
+__host__ __device__ __forceinline__ int p64_nblk(int w, int K) {
+    const int R = K - w;
+    return 1 + p64_nnear(w, K) + (R > kP64 ? (R - kP64 + kP64 - 1) / kP64 : 0);
+}
+__host__ __device__ __forceinline__ void p64_block(int w, int K, int blk, int& k0, int& kc) {
+    const int nn = p64_nnear(w, K);
+    if (blk == 0) {
+        k0 = 0;
+        kc = w;
+    } else if (blk <= nn) {
+        k0 = w + (blk - 1) * kP64Near;
+        kc = min(kP64Near, K - k0);
+    } else {
+        k0 = w + kP64 + (blk - 1 - nn) * kP64;
+        kc = min(kP64, K - k0);
+    }
+}
+
 // Work item (chunk, block): the block's 64 columns of G times the matching rows of [b ; x_R]
 // (waiting on solved rows), written to the chunk's partial-sum slot for that block.  The CTA that
 // completes a chunk's last block sums the partials in block order (deterministic) and publishes
@@ -500,7 +529,7 @@ __global__ void __launch_bounds__(128) k_b_panels64(BArgs A, const int2* __restr
     __shared__ int s_ok, s_last;
     Ctl* ctl = &A.bc->c;
     for (;;) {
-        if (threadIdx.x == 0) s_t = aborted(ctl) ? 0xFFFFFFFFu : atomicAdd(&ctl->ticket2, 1u);
+        if (threadIdx.x == 0) s_t = aborted(ctl) ? 0xFFFFFFFFu : atomicAdd(&A.bc->ticket_p64, 1u);
         __syncthreads();
         const unsigned t = s_t;
         __syncthreads();
@@ -509,7 +538,8 @@ __global__ void __launch_bounds__(128) k_b_panels64(BArgs A, const int2* __restr
         const BChunk C = chunks[it.x];
         const BSys S = A.sys[C.sys];
         const int a = C.a, w = C.w, K = C.w + C.m, L = C.ld, m = S.rhs, blk = it.y;
-        const int k0 = blk * kP64, kc = min(kP64, K - k0);
+        int k0, kc;
+        p64_block(w, K, blk, k0, kc);
         const double* b = A.b + S.xb0;
         double* x = A.x + S.xb0;
         double* pb = part + C.poff + (long long)blk * w * m;
@@ -926,6 +956,8 @@ struct Batch {
     int device = 0;
     cudaStream_t st = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaStream_t st2 = nullptr;                // the exact FP64 panels, beside the refinement
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     int sm_count = 0;
     int count = 0;
     std::vector<BSys> sys;
@@ -993,6 +1025,9 @@ Batch::~Batch() {
     if (scratch) sptrsv_destroy(reinterpret_cast<sptrsv_handle>(scratch));
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_join) cudaEventDestroy(ev_join);
+    if (st2) cudaStreamDestroy(st2);
     if (st) cudaStreamDestroy(st);
 }
 
@@ -1112,7 +1147,7 @@ int Batch::build_panels(int s, bool f64) {
         ch.w = ss[c + 1] - ss[c];
         ch.m = mm[c];
         ch.ld = ld[c];
-        ch.nblk = (ch.w + ch.m + kP64 - 1) / kP64;
+        ch.nblk = p64_nblk(ch.w, ch.w + ch.m);
         if (!f64) {
             ch.ghi = gbufs[k0].as<__nv_bfloat16>() + goff[c];
             ch.glo = gbufs[k0 + 1].as<__nv_bfloat16>() + goff[c];
@@ -1214,9 +1249,7 @@ int Batch::build_lists() {
         std::vector<int2> its;
         for (int c = (int)pchunks[s].size() - 1; c >= 0; --c) {
             const BChunk& b = pchunks[s][c];
-            const int own = (b.w + kP64 - 1) / kP64;
-            for (int q = 0; q < own && q < b.nblk; ++q) its.push_back(make_int2(base + c, q));
-            for (int q = b.nblk - 1; q >= own; --q) its.push_back(make_int2(base + c, q));
+            for (int q = 0; q < b.nblk; ++q) its.push_back(make_int2(base + c, q == 0 ? 0 : b.nblk - q));
         }
         for (BChunk b : pchunks[s]) {
             b.poff = poff;
@@ -1319,20 +1352,27 @@ int Batch::build_graph(int mode, const double* b, double* x, cudaGraphExec_t* ou
             k_b_fill_pending<double><<<elem_grid(sm_count, plain_el.total), 256, 0, st>>>(A, plain_el.list(), x, false);
             ++nk;
         }
-        if (n_order_plain) launch_pull64(order_plain, n_order_plain);
         if (n_items64) {
-            cudaMemsetAsync(cnt64.p, 0, sizeof(int) * n_chunks64, st);
-            const int grid = resident((const void*)k_b_panels64, 128, sm_count, n_items64);
-            k_b_panels64<<<grid, 128, 0, st>>>(A, items64.as<int2>(), n_items64, chunks64.as<BChunk>(),
-                                               part64.as<double>(), cnt64.as<int>());
+            // the exact FP64 panels on a second captured stream, beside everything below (their
+            // CTAs take a fraction of the SMs; the refinement's kernels fill the rest)
+            cudaEventRecord(ev_fork, st);
+            cudaStreamWaitEvent(st2, ev_fork, 0);
+            cudaMemsetAsync(cnt64.p, 0, sizeof(int) * n_chunks64, st2);
+            const int grid = (int)std::min<long long>(resident((const void*)k_b_panels64, 128, sm_count, n_items64),
+                                                      (long long)sm_count * kP64CtasPerSm);
+            k_b_panels64<<<grid, 128, 0, st2>>>(A, items64.as<int2>(), n_items64, chunks64.as<BChunk>(),
+                                                part64.as<double>(), cnt64.as<int>());
+            cudaEventRecord(ev_join, st2);
             ++nk;
         }
+        if (n_order_plain) launch_pull64(order_plain, n_order_plain);
         if (mixed_el.nseg) {
             k_b_init_mixed<<<elem_grid(sm_count, mixed_el.total), 256, 0, st>>>(A, mixed_el.list());
             ++nk;
             if (add_while(g, ho, &obody) != cudaSuccess) rc = SPTRSV_ERR_CUDA;
         }
     }
+    if (mode == 1 && n_items64) cudaStreamWaitEvent(st, ev_join, 0);
     cudaGraph_t g2 = nullptr;
     e = cudaStreamEndCapture(st, &g2);
     if (!rc && e != cudaSuccess) rc = set_cuda_error(e, "batch capture end");
@@ -1623,6 +1663,9 @@ int sptrsv_batch_create(sptrsv_batch* out, int device, int count, const int* n, 
     cudaError_t er;
     if ((er = cudaStreamCreateWithFlags(&B->st, cudaStreamNonBlocking)) != cudaSuccess ||
         (er = cudaEventCreate(&B->ev0)) != cudaSuccess || (er = cudaEventCreate(&B->ev1)) != cudaSuccess ||
+        (er = cudaStreamCreateWithFlags(&B->st2, cudaStreamNonBlocking)) != cudaSuccess ||
+        (er = cudaEventCreateWithFlags(&B->ev_fork, cudaEventDisableTiming)) != cudaSuccess ||
+        (er = cudaEventCreateWithFlags(&B->ev_join, cudaEventDisableTiming)) != cudaSuccess ||
         (er = cudaDeviceGetAttribute(&B->sm_count, cudaDevAttrMultiProcessorCount, device)) != cudaSuccess)
         return fail(set_cuda_error(er, "batch setup"));
     {

@@ -295,13 +295,15 @@ def evaluate(mlp, X, T, A, default_id):
 # the batched path's schedules from the network
 
 # single-system candidate -> batched schedule (0 plain FP64, 1 Jacobi, 2 BF16x3 panels in the
-# refinement, 3 FP32 sync-free, 4 exact FP64 panels): the supernodal candidates become dense panels
-# of their precision, Jacobi stays Jacobi, the other mixed ones the FP32 pull, the other FP64 ones
-# the plain FP64 pull
+# refinement, 3 FP32 sync-free, 4 exact FP64 panels): both supernodal candidates become the exact
+# FP64 panels -- in the batch their products are split over CTAs and run beside the refinement,
+# which measured faster than the BF16x3 panels' three refinement steps (190 ms against 281 ms for
+# the 512-system mix with every banded system on one or the other); Jacobi stays Jacobi, the other
+# mixed ones the FP32 pull, the other FP64 ones the plain FP64 pull
 def batch_kind(cand_id):
     o = candidate(cand_id)
     if o.schedule == 6:
-        return 4 if o.precision == 0 else 2
+        return 4
     if o.precision == 0:
         return 0
     if o.schedule == 5:
