@@ -25,6 +25,7 @@
 // once per run of rows of one system, so no address sees one atomic per row.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 #include <cuda_bf16.h>
@@ -44,7 +45,7 @@ constexpr int kBRowChunk = 32;  // rows per warp task in the row kernels
 constexpr int kBatchKinds = 14;  // kernel kinds of the profiled replay
 constexpr int kP64 = 64;         // columns of G per FP64 panel work item
 constexpr int kP64Nc = 16;       // right-hand-side columns per pass of an FP64 panel work item
-constexpr int kP64CtasPerSm = 2; // FP64 panel CTAs per SM while the refinement runs beside them
+constexpr int kP64CtasPerSm = 4; // FP64 panel CTAs per SM beside the refinement (measured: 2: 190, 3: 137, 4: 135, 5: 146 ms)
 
 struct BSys {
     int n, rhs, sched, groups;  // groups: lanes per row in the row kernels (row_lanes)
@@ -957,6 +958,7 @@ struct Batch {
     cudaStream_t st = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     cudaStream_t st2 = nullptr;                // the exact FP64 panels, beside the refinement
+    int p64_ctas_per_sm = kP64CtasPerSm;       // tuning override: SPTRSV_P64_CTAS
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     int sm_count = 0;
     int count = 0;
@@ -1359,7 +1361,7 @@ int Batch::build_graph(int mode, const double* b, double* x, cudaGraphExec_t* ou
             cudaStreamWaitEvent(st2, ev_fork, 0);
             cudaMemsetAsync(cnt64.p, 0, sizeof(int) * n_chunks64, st2);
             const int grid = (int)std::min<long long>(resident((const void*)k_b_panels64, 128, sm_count, n_items64),
-                                                      (long long)sm_count * kP64CtasPerSm);
+                                                      (long long)sm_count * p64_ctas_per_sm);
             k_b_panels64<<<grid, 128, 0, st2>>>(A, items64.as<int2>(), n_items64, chunks64.as<BChunk>(),
                                                 part64.as<double>(), cnt64.as<int>());
             cudaEventRecord(ev_join, st2);
@@ -1588,10 +1590,11 @@ int Batch::sync(int64_t* kernels) {
     return 0;
 }
 
-// Default schedule from the analysis: dense row ranges (banded / skyline) -> panels; rows
-// dominated by their diagonal -> Jacobi; otherwise the FP32 sync-free pull.
+// Default schedule from the analysis: dense row ranges (banded / skyline) -> exact FP64 panels
+// (measured faster in the batch than the BF16x3 panels' refinement); rows dominated by their
+// diagonal -> Jacobi; otherwise the FP32 sync-free pull.
 static int default_schedule(const BSys& S, long long nnz, float ratio, int gapped) {
-    if (!gapped && nnz >= 8LL * S.n) return BS_PANEL;
+    if (!gapped && nnz >= 8LL * S.n) return BS_PANEL64;
     if (ratio < 1.f) return BS_JACOBI;
     return BS_SF32;
 }
@@ -1652,6 +1655,7 @@ int sptrsv_batch_create(sptrsv_batch* out, int device, int count, const int* n, 
     B->sched.assign(count, BS_PLAIN);
     B->panel_ok.assign(count, -1);
     B->have_bf16.assign(count, 0);
+    if (const char* e = getenv("SPTRSV_P64_CTAS")) B->p64_ctas_per_sm = std::max(1, atoi(e));
     B->have_f64.assign(count, 0);
     B->gidx.assign(count, -1);
     B->pchunks.resize(count);
