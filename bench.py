@@ -179,6 +179,23 @@ def jacobi_bytes(n, nnz):
 
 
 # ---------------------------------------------------------------------------------------
+def cpu_model():
+    """The host CPU as /proc/cpuinfo names it (model name, or implementer/part on Arm)."""
+    try:
+        info = open("/proc/cpuinfo").read()
+        for key in ("model name", "Model"):
+            for line in info.splitlines():
+                if line.startswith(key):
+                    return line.split(":", 1)[1].strip()
+        impl = [l.split(":")[1].strip() for l in info.splitlines() if l.startswith("CPU implementer")]
+        part = [l.split(":")[1].strip() for l in info.splitlines() if l.startswith("CPU part")]
+        if impl and part:
+            return f"{os.uname().machine} implementer {impl[0]} part {part[0]}"
+    except OSError:
+        pass
+    return os.uname().machine
+
+
 def cpu_paths(m, b, budget_s=8.0):
     """Times the reference's CPU paths on this host; returns a dict with the best."""
     from oracle import oracle
@@ -201,7 +218,14 @@ def cpu_paths(m, b, budget_s=8.0):
         else:
             oracle.barrier_upper(rpu, m.col, m.val, b, 1, num_threads=cores)
 
-    for name, fn, threads in (("serial base_gauss_upper", serial, 1), ("level-set barrier_upper", levelset, cores)):
+    def levelset1():
+        if R is not None:
+            R.ref_barrier_upper(m.n, x, b, m.val, m.col, rpu, 1, 1)
+        else:
+            oracle.barrier_upper(rpu, m.col, m.val, b, 1, num_threads=1)
+
+    for name, fn, threads in (("serial base_gauss_upper", serial, 1), ("level-set barrier_upper", levelset, cores),
+                              ("level-set barrier_upper, 1 thread", levelset1, 1)):
         fn()
         t0 = time.perf_counter()
         reps = 0
@@ -215,7 +239,7 @@ def cpu_paths(m, b, budget_s=8.0):
     best = max(res, key=lambda k: res[k]["solves_per_s"])
     return {"value": res[best]["solves_per_s"], "unit": "solves/s", "cores": res[best]["threads"], "kind": kind,
             "sample": f"{best} on the full system, {res[best]['reps']} solves timed on the host "
-                      f"({os.uname().machine}, {cores} cores); other path: "
+                      f"({cpu_model()}, {cores} cores); other paths: "
                       + "; ".join(f"{k} {v['solves_per_s']:.3g} solves/s ({v['threads']} thr)" for k, v in res.items()
                                   if k != best),
             "paths": res, "best": best, "fn": serial if best.startswith("serial") else levelset}
@@ -599,8 +623,11 @@ def run_batch(args, dist):
     res_fma = int(np.sum((l_nnz * lr)[mixed]))
     jac = sched == 1
     jac_bytes = int(np.sum((8 * (l_nnz - nn) + 4 * (nn + 1) + 16 * nn * lr)[jac]))
+    info = B.info()  # with the schedules' work lists built
+    p64 = sched == 4
+    p64_bytes = int(8 * info["g_entries_f64"] + np.sum((4 * (nn + 1) + 16 * nn * lr)[p64]))  # G once, b, x
     dom = max(prof, key=lambda k: prof[k][0])
-    dom_bytes = {"residual_f64": res_bytes, "jacobi_sweep": jac_bytes}.get(dom)
+    dom_bytes = {"residual_f64": res_bytes, "jacobi_sweep": jac_bytes, "panels_f64": p64_bytes}.get(dom)
     dom_first = prof[dom][2]
     cpu = None
     if dist.rank == 0 and not args.no_cpu_baseline:
@@ -639,17 +666,21 @@ def run_batch(args, dist):
         "refine_steps_by_schedule": {k: np.bincount(st["steps"][sched == v], minlength=4).tolist()
                                      for k, v in sp.BATCH_SCHED.items() if np.any(sched == v)},
         "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": nb, "d2h_bytes_per_step": nb},
-        "roofline": ({"bound": "hbm", "kernel": {"residual_f64": "k_b_residual", "jacobi_sweep": "k_b_jacobi"}[dom],
+        "roofline": ({"bound": "hbm", "kernel": {"residual_f64": "k_b_residual", "jacobi_sweep": "k_b_jacobi",
+                                                 "panels_f64": "k_b_panels64"}[dom],
                       "achieved": dom_bytes / (dom_first * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
                       "frac": dom_bytes / (dom_first * 1e-3) / 1e9 / peak, "peak_source": peak_src, "traffic": None,
                       "algorithmic_bytes_per_launch": dom_bytes, "launch_ms": dom_first,
-                      "note": "first launch (every mixed system active)"}
+                      "note": "first launch (every system of the kernel's schedule active)"}
                      if dom_bytes else
                      {"bound": "hbm", "kernel": dom, "achieved": fb / (ms_step * 1e-3) / 1e9, "peak": peak,
                       "unit": "GB/s", "frac": fb / (ms_step * 1e-3) / 1e9 / peak, "peak_source": peak_src,
                       "traffic": None, "algorithmic_bytes_per_launch": fb, "note": "whole solve"}),
         "fp64_residual": {"gfma_per_s": res_fma / (prof["residual_f64"][2] * 1e-3) / 1e9 if "residual_f64" in prof
                           else None, "fma_per_launch": res_fma},
+        "fp64_panels": {"gfma_per_s": info["g_fma_f64"] / (prof["panels_f64"][2] * 1e-3) / 1e9
+                        if "panels_f64" in prof else None, "fma_per_launch": info["g_fma_f64"],
+                        "g_entries": info["g_entries_f64"]},
         "kernel_profile_chosen": {k: {"ms": v[0], "launches": v[1]} for k, v in prof.items()},
         "kernel_profile_plain": {k: {"ms": v[0], "launches": v[1]} for k, v in pplain.items()},
         "gpu_launches": int(sum(ks)),
@@ -713,12 +744,16 @@ def run_supernodal(args, dist):
         t0 = time.perf_counter()
         oracle.base_gauss_upper(rpu, m.col, m.val, b, rhs)
         row["cpu_serial_ms"] = 1e3 * (time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        oracle.supernodal_upper(m.snodes, rpu, m.col, m.val, b, rhs)
+        row["cpu_supernodal_ms"] = 1e3 * (time.perf_counter() - t0)
         rows.append(row)
         L.sptrsv_device_free(h, d_b)
         L.sptrsv_device_free(h, d_x)
     info = s.info()
     print(json.dumps({"workload": "supernodal: 7-point 3D Laplacian Cholesky factor, 40^3 grid, nested dissection "
                                   "(8^3 leaves), supernodes <= 400 rows",
+                      "cpu": f"{cpu_model()}, 1 thread (serial and supernodal restatements of core.cpp)",
                       "n": m.n, "nnz": m.nnz, "supernodes": int(len(m.snodes) - 1), "max_level": info["max_level"],
                       "generation_s": t_gen, "rows": rows}), flush=True)
 

@@ -252,7 +252,8 @@ SPTRSV_API int sptrsv_batch_solve_host(sptrsv_batch b, int mode, const double* h
 SPTRSV_API int sptrsv_batch_sync(sptrsv_batch b, int64_t* kernels);
 /* Per system, of the last chosen-mode solve: status, refinement steps, relative residual, sweeps. */
 SPTRSV_API int sptrsv_batch_stats(sptrsv_batch b, int* status, int* steps, double* rel_res, int* sweeps);
-/* totals = {sum n, sum nnz, sum n*rhs, count}; ratio[s] = max row sum|off|/|diag|. */
+/* totals[6] = {sum n, sum nnz, sum n*rhs, count, G entries of the exact FP64 panels, their FMAs
+ * per solve} (the schedules' work lists are built first); ratio[s] = max row sum|off|/|diag|. */
 SPTRSV_API int sptrsv_batch_info(sptrsv_batch b, int64_t* totals, float* ratio);
 /* The selector's SPTRSV_FEATURES features of system s (with its own rhs). */
 SPTRSV_API int sptrsv_batch_features(sptrsv_batch b, int s, float* features);

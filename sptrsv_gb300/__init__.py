@@ -363,10 +363,11 @@ class Batch:
                                                    int(spin_budget_ns)), "batch_set_options")
 
     def info(self):
-        t = np.zeros(4, dtype=np.int64)
+        t = np.zeros(6, dtype=np.int64)
         r = np.zeros(self.count, dtype=np.float32)
         _check(_lib.lib().sptrsv_batch_info(self._h, t, r), "batch_info")
-        return {"rows": int(t[0]), "nnz": int(t[1]), "x_elems": int(t[2]), "count": int(t[3]), "ratio": r}
+        return {"rows": int(t[0]), "nnz": int(t[1]), "x_elems": int(t[2]), "count": int(t[3]),
+                "g_entries_f64": int(t[4]), "g_fma_f64": int(t[5]), "ratio": r}
 
     def solve(self, b, mode="chosen"):
         """Host b (all systems) -> host x, through the host-buffer entry point."""

@@ -975,6 +975,7 @@ struct Batch {
     int n_tasks_mixed = 0, n_tasks_jac = 0;
     DevBuf items64, chunks64, part64, cnt64;  // exact FP64 panels
     unsigned n_items64 = 0;
+    long long g_entries64 = 0, g_fma64 = 0;   // G entries (w x K over the chunks) and FMAs per solve
     int n_chunks64 = 0;
     unsigned n_order_all = 0, n_order_plain = 0, n_order_sf32 = 0, n_items = 0;
     DevSeg all_rows, all_el, mixed_rows, mixed_el, jac_rows, pend_el, plain_el;
@@ -1245,6 +1246,7 @@ int Batch::build_lists() {
     std::vector<BChunk> ch64;
     std::vector<std::vector<int2>> per64;
     long long poff = 0;
+    g_entries64 = g_fma64 = 0;
     for (int s = 0; s < count; ++s) {
         if (sched[s] != BS_PANEL64) continue;
         const int base = (int)ch64.size();
@@ -1256,6 +1258,8 @@ int Batch::build_lists() {
         for (BChunk b : pchunks[s]) {
             b.poff = poff;
             poff += (long long)b.nblk * b.w * sys[s].rhs;
+            g_entries64 += (long long)b.w * (b.w + b.m);
+            g_fma64 += (long long)b.w * (b.w + b.m) * sys[s].rhs;
             ch64.push_back(b);
         }
         per64.push_back(std::move(its));
@@ -1840,6 +1844,10 @@ int sptrsv_batch_info(sptrsv_batch bh, int64_t* totals, float* ratio) {
         totals[1] = B->tot_nnz;
         totals[2] = B->tot_x;
         totals[3] = B->count;
+        const int rc = B->build_lists();
+        if (rc) return rc;
+        totals[4] = B->g_entries64;
+        totals[5] = B->g_fma64;
     }
     if (ratio)
         for (int s = 0; s < B->count; ++s) ratio[s] = B->ratio[s];
