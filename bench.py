@@ -667,7 +667,7 @@ def run_batch(args, dist):
                                      for k, v in sp.BATCH_SCHED.items() if np.any(sched == v)},
         "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": nb, "d2h_bytes_per_step": nb},
         "roofline": ({"bound": "hbm", "kernel": {"residual_f64": "k_b_residual", "jacobi_sweep": "k_b_jacobi",
-                                                 "panels_f64": "k_b_panels64"}[dom],
+                                                 "panels_f64": "k_panels64"}[dom],
                       "achieved": dom_bytes / (dom_first * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
                       "frac": dom_bytes / (dom_first * 1e-3) / 1e9 / peak, "peak_source": peak_src, "traffic": None,
                       "algorithmic_bytes_per_launch": dom_bytes, "launch_ms": dom_first,

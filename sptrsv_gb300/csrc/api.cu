@@ -10,6 +10,7 @@
 #include "common.cuh"
 #include "kernels.cuh"
 #include "handle.cuh"
+#include "batch.cuh"
 
 namespace sptrsv {
 
@@ -240,26 +241,39 @@ sptrsv_opts Handle::resolve(const sptrsv_opts* o, int rhs) const {
 
 int Handle::prepare(const sptrsv_opts& o, int rhs, int layout) {
     int rc;
+    // a work buffer that grows moves: graphs captured with its old address are dropped
+    bool moved = false;
+    auto grow = [&](DevBuf& d, size_t bytes) {
+        void* old = d.p;
+        const int r = d.ensure(bytes);
+        moved |= old && d.p != old;
+        return r;
+    };
     if (o.schedule == SPTRSV_SCHED_LEVELSET || (o.precision == SPTRSV_PREC_MIXED && o.inner == SPTRSV_SCHED_LEVELSET))
         if ((rc = ensure_levels())) return rc;
     const size_t nr = (size_t)n * rhs;
     if (rhs > 1 && layout == SPTRSV_COL_MAJOR) {
-        if ((rc = bw.ensure(sizeof(double) * nr))) return rc;
-        if ((rc = xw.ensure(sizeof(double) * nr))) return rc;
+        if ((rc = grow(bw, sizeof(double) * nr))) return rc;
+        if ((rc = grow(xw, sizeof(double) * nr))) return rc;
     }
     if (o.precision == SPTRSV_PREC_MIXED) {
         if (o.inner == SPTRSV_SCHED_JACOBI && rhs == 1)
             if ((rc = ensure_offdiag())) return rc;
-        if ((rc = r32.ensure(sizeof(float) * nr))) return rc;
-        if ((rc = d32a.ensure(sizeof(float) * nr))) return rc;
-        if ((rc = d32b.ensure(sizeof(float) * nr))) return rc;
-        if ((rc = norms.ensure(sizeof(double) * 2 * (size_t)rhs))) return rc;
+        if ((rc = grow(r32, sizeof(float) * nr))) return rc;
+        if ((rc = grow(d32a, sizeof(float) * nr))) return rc;
+        if ((rc = grow(d32b, sizeof(float) * nr))) return rc;
+        if ((rc = grow(norms, sizeof(double) * 2 * (size_t)rhs))) return rc;
     }
     if (o.schedule == SPTRSV_SCHED_SYNCFREE_CSC && o.precision == SPTRSV_PREC_FP64) {
         if ((rc = build_csc())) return rc;
-        if ((rc = indeg_work.ensure(sizeof(int) * (size_t)n))) return rc;
-        if ((rc = left.ensure(sizeof(double) * nr))) return rc;
+        if ((rc = grow(indeg_work, sizeof(int) * (size_t)n))) return rc;
+        if ((rc = grow(left, sizeof(double) * nr))) return rc;
     }
+    if (o.schedule == SPTRSV_SCHED_SUPERNODAL && o.precision == SPTRSV_PREC_FP64 && have_supernodes) {
+        if ((rc = grow(sn_ppart, sizeof(double) * (size_t)sn_prows * rhs))) return rc;
+        if ((rc = grow(sn_pcnt, sizeof(int) * (size_t)sn_npan * p64_groups(rhs)))) return rc;
+    }
+    if (moved) drop_graphs();
     return 0;
 }
 
@@ -720,7 +734,7 @@ Handle::~Handle() {
                       &level_rows, &stats, &csc_ptr, &csc_row, &csc_val, &scratch, &xw, &bw, &r32, &d32a, &d32b,
                       &norms, &indeg_work, &left, &db, &dx, &flush, &offdiag, &roff, &sell, &sell_perm, &sell_len, &sell_ptr,
                       &sn_start, &sn_m, &sn_roff, &sn_rect, &sn_goff, &sn_ld, &sn_colbase, &sn_outbase, &sn_items,
-                      &sn_G, &sn_Ghi, &sn_Glo, &tune_b, &tune_x};
+                      &sn_G, &sn_Ghi, &sn_Glo, &sn_pan, &sn_pitems, &sn_pcnt, &sn_ppart, &tune_b, &tune_x};
     for (DevBuf* b : bufs) b->release();
     if (ctl) cudaFree(ctl);
     if (ev0) cudaEventDestroy(ev0);
@@ -796,6 +810,9 @@ int sptrsv_create(sptrsv_handle* out, int device) {
         if ((er = cudaEventCreate(&h->ev0)) != cudaSuccess) { rc = sptrsv::set_cuda_error(er, "event"); break; }
         if ((er = cudaEventCreate(&h->ev1)) != cudaSuccess) { rc = sptrsv::set_cuda_error(er, "event"); break; }
         if ((er = cudaMalloc(&h->ctl, sizeof(sptrsv::Ctl))) != cudaSuccess) { rc = sptrsv::set_cuda_error(er, "ctl"); break; }
+        // a new control block reports no status until a solve or analysis writes one
+        if ((er = cudaMemsetAsync(h->ctl, 0, sizeof(sptrsv::Ctl), h->st)) != cudaSuccess ||
+            (er = cudaStreamSynchronize(h->st)) != cudaSuccess) { rc = sptrsv::set_cuda_error(er, "ctl"); break; }
         if ((er = cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, device)) != cudaSuccess) { rc = sptrsv::set_cuda_error(er, "attr"); break; }
     } while (0);
     if (rc) { delete h; return rc; }

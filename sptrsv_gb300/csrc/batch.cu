@@ -33,6 +33,7 @@
 #include "kernels.cuh"
 #include "handle.cuh"
 #include "mma.cuh"
+#include "batch.cuh"
 
 namespace sptrsv {
 
@@ -43,14 +44,9 @@ constexpr int kBKc = 64;        // K rows staged per chunk (a multiple of 16: ch
 constexpr int kBNc = 32;        // right-hand-side columns per pass
 constexpr int kBRowChunk = 32;  // rows per warp task in the row kernels
 constexpr int kBatchKinds = 14;  // kernel kinds of the profiled replay
-constexpr int kP64 = 64;         // columns of G per FP64 panel work item
-constexpr int kP64Nc = 16;       // right-hand-side columns per pass of an FP64 panel work item
 constexpr int kP64CtasPerSm = 4; // FP64 panel CTAs per SM beside the refinement (measured: 2: 190, 3: 137, 4: 135, 5: 146 ms)
 
-struct BSys {
-    int n, rhs, sched, groups;  // groups: lanes per row in the row kernels (row_lanes)
-    long long rp0, nz0, row0, xb0;
-};
+
 
 struct BState {
     double bnorm2, rnorm2, rel;
@@ -76,15 +72,7 @@ struct BCtl {
     int pad;
 };
 
-struct BChunk {
-    int sys, a, w, m, ld, pad;
-    const __nv_bfloat16* ghi;  // G ~ ghi + glo (two BF16 terms)
-    const __nv_bfloat16* glo;
-    const double* g64;         // G in FP64 (the exact panel schedule)
-    const int* rect;
-    long long poff;            // FP64 schedule: first partial-sum slot of the chunk
-    int nblk;                  // FP64 schedule: 64-column blocks of G
-};
+
 
 // A list of systems with the prefix of their row (or element) counts.
 struct SegList {
@@ -488,137 +476,6 @@ __global__ void __launch_bounds__(128, 4) k_b_panels(BArgs A, const int2* __rest
     }
 }
 
-// --- exact FP64 panels, split over CTAs ---------------------------------------------------------
-
-// Column blocks of a chunk's G (w own columns, then K - w solved columns): block 0 the own part;
-// blocks 1..nnear the nearest 64 solved columns in 16-column pieces (the rows published last, so
-// only one narrow block per CTA lies on the dependency chain); then 64-column blocks.
-constexpr int kP64Near = 16;
-__host__ __device__ __forceinline__ int p64_nnear(int w, int K) {
-    const int R = K - w;
-    return R <= 0 ? 0 : min(kP64 / kP64Near, (R + kP64Near - 1) / kP64Near);
-}
-__host__ __device__ __forceinline__ int p64_nblk(int w, int K) {
-    const int R = K - w;
-    return 1 + p64_nnear(w, K) + (R > kP64 ? (R - kP64 + kP64 - 1) / kP64 : 0);
-}
-__host__ __device__ __forceinline__ void p64_block(int w, int K, int blk, int& k0, int& kc) {
-    const int nn = p64_nnear(w, K);
-    if (blk == 0) {
-        k0 = 0;
-        kc = w;
-    } else if (blk <= nn) {
-        k0 = w + (blk - 1) * kP64Near;
-        kc = min(kP64Near, K - k0);
-    } else {
-        k0 = w + kP64 + (blk - 1 - nn) * kP64;
-        kc = min(kP64, K - k0);
-    }
-}
-
-// Work item (chunk, block): the block's 64 columns of G times the matching rows of [b ; x_R]
-// (waiting on solved rows), written to the chunk's partial-sum slot for that block.  The CTA that
-// completes a chunk's last block sums the partials in block order (deterministic) and publishes
-// the chunk's rows of x.  Blocks of a chunk depend only on rows of later chunks, whose items hold
-// smaller tickets, so the ticket order guarantees progress.
-__global__ void __launch_bounds__(128) k_b_panels64(BArgs A, const int2* __restrict__ items, unsigned nitems,
-                                                    const BChunk* __restrict__ chunks, double* __restrict__ part,
-                                                    int* __restrict__ cnt) {
-    __shared__ double Gs[kBPanel][kP64 + 1];
-    __shared__ double Vs[kP64][kP64Nc + 1];
-    __shared__ unsigned s_t;
-    __shared__ int s_ok, s_last;
-    Ctl* ctl = &A.bc->c;
-    for (;;) {
-        if (threadIdx.x == 0) s_t = aborted(ctl) ? 0xFFFFFFFFu : atomicAdd(&A.bc->ticket_p64, 1u);
-        __syncthreads();
-        const unsigned t = s_t;
-        __syncthreads();
-        if (t >= nitems) break;
-        const int2 it = items[t];
-        const BChunk C = chunks[it.x];
-        const BSys S = A.sys[C.sys];
-        const int a = C.a, w = C.w, K = C.w + C.m, L = C.ld, m = S.rhs, blk = it.y;
-        int k0, kc;
-        p64_block(w, K, blk, k0, kc);
-        const double* b = A.b + S.xb0;
-        double* x = A.x + S.xb0;
-        double* pb = part + C.poff + (long long)blk * w * m;
-        // the block of G (rows of the chunk, columns k0 .. k0+kc), staged once for every RHS pass
-        for (int e = threadIdx.x; e < kBPanel * kP64; e += blockDim.x) {
-            const int r = e / kP64, kk = e - r * kP64;
-            Gs[r][kk] = (r < w && kk < kc) ? C.g64[(size_t)r * L + k0 + kk] : 0.0;
-        }
-        bool ok = true;
-        for (int c0 = 0; c0 < m; c0 += kP64Nc) {
-            const int nc = min(kP64Nc, m - c0);
-            if (threadIdx.x == 0) s_ok = 1;
-            __syncthreads();
-            // eight loads per thread in flight together, then waits only on pending values
-            constexpr int kStage = 8;
-            for (int base = 0; base < kc * nc; base += 128 * kStage) {
-                double v[kStage];
-#pragma unroll
-                for (int u = 0; u < kStage; ++u) {
-                    const int e = base + threadIdx.x + u * 128;
-                    double val = 0.0;
-                    if (e < kc * nc) {
-                        const int kk = e / nc, j = e - kk * nc, k = k0 + kk;
-                        val = k < w ? b[(size_t)(a + k) * m + c0 + j] : ld_relaxed(x + (size_t)C.rect[k - w] * m + c0 + j);
-                    }
-                    v[u] = val;
-                }
-#pragma unroll
-                for (int u = 0; u < kStage; ++u) {
-                    const int e = base + threadIdx.x + u * 128;
-                    if (e < kc * nc) {
-                        const int kk = e / nc, j = e - kk * nc, k = k0 + kk;
-                        double val = v[u];
-                        if (k >= w && Pend<double>::is(val) &&
-                            !wait_ready<double>(x + (size_t)C.rect[k - w] * m + c0 + j, val, ctl, A.budget)) {
-                            s_ok = 0;
-                            val = 0.0;
-                        }
-                        Vs[kk][j] = val;
-                    }
-                }
-            }
-            __syncthreads();
-            if (!s_ok) { ok = false; break; }
-            for (int o = threadIdx.x; o < w * nc; o += blockDim.x) {
-                const int r = o / nc, j = o - r * nc;
-                double s0 = 0.0, s1 = 0.0;
-                int kk = 0;
-                for (; kk + 1 < kc; kk += 2) {
-                    s0 = fma(Gs[r][kk], Vs[kk][j], s0);
-                    s1 = fma(Gs[r][kk + 1], Vs[kk + 1][j], s1);
-                }
-                if (kk < kc) s0 = fma(Gs[r][kk], Vs[kk][j], s0);
-                pb[(size_t)r * m + c0 + j] = s0 + s1;
-            }
-            __syncthreads();
-        }
-        __threadfence();  // this thread's partial sums visible before the chunk's count moves
-        if (__syncthreads_or(!ok)) break;
-        // the last block of the chunk sums the partials in block order and publishes the rows
-        if (threadIdx.x == 0) {
-            __threadfence();
-            s_last = atomicAdd(&cnt[it.x], 1) == C.nblk - 1;
-            if (s_last) __threadfence();
-        }
-        __syncthreads();
-        if (s_last) {
-            const double* p0 = part + C.poff;
-            for (int o = threadIdx.x; o < w * m; o += blockDim.x) {
-                double v = 0.0;
-                for (int q = 0; q < C.nblk; ++q) v += __ldcg(p0 + (long long)q * w * m + o);
-                const int r = o / m, j = o - r * m;
-                st_relaxed(x + (size_t)(a + r) * m + j, Pend<double>::fix(v));
-            }
-        }
-    }
-}
-
 // --- row tasks ---------------------------------------------------------------------------------
 
 // A row task: consecutive rows of one system (about the same number of entries x RHS columns in
@@ -976,7 +833,7 @@ struct Batch {
     DevBuf items64, chunks64, part64, cnt64;  // exact FP64 panels
     unsigned n_items64 = 0;
     long long g_entries64 = 0, g_fma64 = 0;   // G entries (w x K over the chunks) and FMAs per solve
-    int n_chunks64 = 0;
+    int n_chunks64 = 0, n_cnt64 = 0;
     unsigned n_order_all = 0, n_order_plain = 0, n_order_sf32 = 0, n_items = 0;
     DevSeg all_rows, all_el, mixed_rows, mixed_el, jac_rows, pend_el, plain_el;
     std::vector<DevBuf> gbufs;            // per panel system: hi, lo, rect
@@ -1151,6 +1008,8 @@ int Batch::build_panels(int s, bool f64) {
         ch.m = mm[c];
         ch.ld = ld[c];
         ch.nblk = p64_nblk(ch.w, ch.w + ch.m);
+        ch.r0 = 0;
+        ch.pw = ch.w;
         if (!f64) {
             ch.ghi = gbufs[k0].as<__nv_bfloat16>() + goff[c];
             ch.glo = gbufs[k0 + 1].as<__nv_bfloat16>() + goff[c];
@@ -1242,39 +1101,53 @@ int Batch::build_lists() {
     n_items = (unsigned)it.size();
     if ((rc = upload_vec(chunks, ch, st)) || (rc = upload_vec(items, it, st))) return rc;
     // exact FP64 panel items: per chunk (last first) its own right-hand-side blocks, then the solved
-    // column blocks farthest first; chunks interleaved across systems; partial-sum slots per chunk
+    // column blocks farthest first, each block once per RHS group; chunks interleaved across
+    // systems; partial-sum slots per chunk, completion counters per (chunk, group)
     std::vector<BChunk> ch64;
-    std::vector<std::vector<int2>> per64;
+    std::vector<std::vector<std::vector<int2>>> per64;  // per system, per step (chunk from the last)
     long long poff = 0;
+    int cbase = 0;
     g_entries64 = g_fma64 = 0;
     for (int s = 0; s < count; ++s) {
         if (sched[s] != BS_PANEL64) continue;
-        const int base = (int)ch64.size();
-        std::vector<int2> its;
+        const int base = (int)ch64.size(), ng = p64_groups(sys[s].rhs);
+        if (ng > 0x7FFF) return SPTRSV_ERR_TOO_LARGE;  // items carry the group in 15 bits
+        for (const BChunk& b : pchunks[s])
+            if (b.nblk > 0xFFFF) return SPTRSV_ERR_TOO_LARGE;  // and the block in 16
+        std::vector<std::vector<int2>> steps;
         for (int c = (int)pchunks[s].size() - 1; c >= 0; --c) {
             const BChunk& b = pchunks[s][c];
-            for (int q = 0; q < b.nblk; ++q) its.push_back(make_int2(base + c, q == 0 ? 0 : b.nblk - q));
+            std::vector<int2> its;
+            for (int q = 0; q < b.nblk; ++q)
+                for (int g = 0; g < ng; ++g) its.push_back(make_int2(base + c, (q == 0 ? 0 : b.nblk - q) | g << 16));
+            steps.push_back(std::move(its));
         }
         for (BChunk b : pchunks[s]) {
             b.poff = poff;
+            b.cbase = cbase;
+            cbase += ng;
             poff += (long long)b.nblk * b.w * sys[s].rhs;
             g_entries64 += (long long)b.w * (b.w + b.m);
             g_fma64 += (long long)b.w * (b.w + b.m) * sys[s].rhs;
             ch64.push_back(b);
         }
-        per64.push_back(std::move(its));
+        per64.push_back(std::move(steps));
     }
+    // queue order: step by step across the systems (every system's last chunk, then every
+    // system's second-last, ...), so a system's chunk enters the queue when its dependency chain
+    // can reach it, whatever its blocks per chunk; the longest chains then run at their own pace
     std::vector<int2> it64;
     size_t longest64 = 0;
     for (auto& v : per64) longest64 = std::max(longest64, v.size());
     for (size_t t = 0; t < longest64; ++t)
         for (auto& v : per64)
-            if (t < v.size()) it64.push_back(v[t]);
+            if (t < v.size()) it64.insert(it64.end(), v[t].begin(), v[t].end());
     n_items64 = (unsigned)it64.size();
     n_chunks64 = (int)ch64.size();
+    n_cnt64 = cbase;
     if ((rc = upload_vec(chunks64, ch64, st)) || (rc = upload_vec(items64, it64, st))) return rc;
     if (n_chunks64 && ((rc = part64.ensure(sizeof(double) * (size_t)std::max(1LL, poff))) ||
-                       (rc = cnt64.ensure(sizeof(int) * (size_t)n_chunks64))))
+                       (rc = cnt64.ensure(sizeof(int) * (size_t)n_cnt64))))
         return rc;
     lists_ready = true;
     drop_graphs();
@@ -1363,13 +1236,13 @@ int Batch::build_graph(int mode, const double* b, double* x, cudaGraphExec_t* ou
             // CTAs take a fraction of the SMs; the refinement's kernels fill the rest)
             cudaEventRecord(ev_fork, st);
             cudaStreamWaitEvent(st2, ev_fork, 0);
-            cudaMemsetAsync(cnt64.p, 0, sizeof(int) * n_chunks64, st2);
-            const int grid = (int)std::min<long long>(resident((const void*)k_b_panels64, 128, sm_count, n_items64),
-                                                      (long long)sm_count * p64_ctas_per_sm);
-            k_b_panels64<<<grid, 128, 0, st2>>>(A, items64.as<int2>(), n_items64, chunks64.as<BChunk>(),
-                                                part64.as<double>(), cnt64.as<int>());
+            int64_t l64 = 0;
+            if (launch_panels64(A.sys, 0, A.b, A.x, &A.bc->c, &A.bc->ticket_p64, A.budget, items64.as<int2>(),
+                                n_items64, chunks64.as<BChunk>(), part64.as<double>(), cnt64.as<int>(), n_cnt64,
+                                p64_ctas_per_sm, sm_count, st2, &l64))
+                rc = SPTRSV_ERR_CUDA;
             cudaEventRecord(ev_join, st2);
-            ++nk;
+            nk += (int)l64;
         }
         if (n_order_plain) launch_pull64(order_plain, n_order_plain);
         if (mixed_el.nseg) {
@@ -1519,11 +1392,11 @@ int Batch::profile(int mode, const double* b, double* x, float* kind_ms, int* ki
             goto out;
         if (n_order_plain && (rc = pull64(order_plain, n_order_plain))) goto out;
         if (n_items64) {
-            CUDA_TRY(cudaMemsetAsync(cnt64.p, 0, sizeof(int) * n_chunks64, st));
-            const int grid = resident((const void*)k_b_panels64, 128, sm_count, n_items64);
+            int64_t l64 = 0;
             if ((rc = timed(13, [&] {
-                     k_b_panels64<<<grid, 128, 0, st>>>(A, items64.as<int2>(), n_items64, chunks64.as<BChunk>(),
-                                                        part64.as<double>(), cnt64.as<int>());
+                     launch_panels64(A.sys, 0, A.b, A.x, &A.bc->c, &A.bc->ticket_p64, A.budget, items64.as<int2>(),
+                                     n_items64, chunks64.as<BChunk>(), part64.as<double>(), cnt64.as<int>(),
+                                     n_cnt64, 64, sm_count, st, &l64);
                  })))
                 goto out;
         }

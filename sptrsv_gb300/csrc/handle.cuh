@@ -73,6 +73,12 @@ struct Handle {
     // supernode partition and its dense panels (supernodal.cu)
     DevBuf sn_start, sn_m, sn_roff, sn_rect, sn_goff, sn_ld, sn_colbase, sn_outbase, sn_items, sn_G, sn_Ghi, sn_Glo;
     int sn_count = 0, sn_nitems = 0;
+    // the FP64 solve's 64-row panels split into column blocks (panels64.cu): panel records,
+    // (panel, block) items, per-panel completion counters, partial sums (sn_prows per column)
+    DevBuf sn_pan, sn_pitems, sn_pcnt, sn_ppart;
+    int sn_npan = 0;
+    unsigned sn_npitems = 0;
+    long long sn_prows = 0;
     bool have_supernodes = false;
     bool have_offdiag = false;
 

@@ -7,20 +7,22 @@
 // so once G_s is formed (in FP64, at analysis: the diagonal-block factors stay FP64) every row of
 // X_s is an independent dot product.  The solve is a sync-free walk over 64-row panels of the
 // supernodes in reverse order (a panel waits only on rows of higher supernodes, whose panels hold
-// smaller tickets), one CTA per panel:
-//   * FP64: the panel product on CUDA cores;
-//   * MIXED inner solve: BF16x3 tensor-core products (G = G_hi + G_lo and V = V_hi + V_lo in
-//     bfloat16; G V ~ G_hi V_hi + G_hi V_lo + G_lo V_hi) accumulated in FP32 with
-//     mma.sync.m16n8k16, inside the FP64 refinement of refine.cu.
+// smaller tickets):
+//   * FP64: each panel's product split into column blocks taken by different CTAs, partial sums
+//     added in block order by the CTA that completes the panel (panels64.cu);
+//   * MIXED inner solve: one CTA per panel, BF16x3 tensor-core products (G = G_hi + G_lo and
+//     V = V_hi + V_lo in bfloat16; G V ~ G_hi V_hi + G_hi V_lo + G_lo V_hi) accumulated in FP32
+//     with mma.sync.m16n8k16, inside the FP64 refinement of refine.cu.
 // Supernodes wider than kSnMaxW rows are split into chunks (a chunk of a supernode is again a
-// supernode).  The right-hand side chunk [B_s ; X_R] is staged in shared memory K-chunk by
-// K-chunk; every wait on X_R is a bounded pending-sentinel poll.
+// supernode).  The right-hand side [B_s ; X_R] is staged in shared memory block by block; every
+// wait on X_R is a bounded pending-sentinel poll.
 #include <cuda_bf16.h>
 #include <vector>
 #include "common.cuh"
 #include "kernels.cuh"
 #include "handle.cuh"
 #include "mma.cuh"
+#include "batch.cuh"
 
 namespace sptrsv {
 
@@ -176,94 +178,6 @@ __global__ void k_sn_split(long long count, const double* __restrict__ G, __nv_b
 }
 
 // --- solve ------------------------------------------------------------------------------
-
-// FP64 panel product on CUDA cores: X[rows of the panel] = G_s[rows] [B_s ; X_R].
-__global__ void __launch_bounds__(128) k_sn_solve_f64(SnArgs A, const double* __restrict__ G, int rhs,
-                                                      const double* __restrict__ b, double* x, Ctl* ctl,
-                                                      int64_t budget) {
-    __shared__ double V[kKc][kNc];
-    __shared__ unsigned s_t;
-    __shared__ int s_ok;
-    for (;;) {
-        if (threadIdx.x == 0) s_t = aborted(ctl) ? 0xFFFFFFFFu : atomicAdd(&ctl->ticket, 1u);
-        __syncthreads();
-        const unsigned t = s_t;
-        if (t >= (unsigned)A.nitems) break;
-        const int s = A.item_s[t], p = A.item_p[t];
-        const int a = A.sstart[s], w = A.sstart[s + 1] - a, m = A.mrect[s];
-        const int K = w + m, L = A.ld[s];
-        const int* rc = A.rect_cols + A.roff[s];
-        const double* g = G + A.goff[s];
-        const int r0 = p * kPanel;
-        const int nrows = min(kPanel, w - r0);
-        bool ok = true;
-        for (int c0 = 0; c0 < rhs; c0 += kNc) {
-            const int nc = min(kNc, rhs - c0);
-            // each thread owns outputs (row, col) = (threadIdx.x % 64 + 64 q...); 128 threads, 64 x nc outputs
-            double acc[16];
-#pragma unroll
-            for (int q = 0; q < 16; ++q) acc[q] = 0.0;
-            for (int k0 = 0; k0 < K; k0 += kKc) {
-                const int kc = min(kKc, K - k0);
-                if (threadIdx.x == 0) s_ok = 1;
-                __syncthreads();
-                // eight loads per thread in flight together, then waits only on pending values
-                constexpr int kStage = 8;
-                for (int base = 0; base < kc * nc; base += 128 * kStage) {
-                    double v[kStage];
-#pragma unroll
-                    for (int u = 0; u < kStage; ++u) {
-                        const int e = base + threadIdx.x + u * 128;
-                        double val = 0.0;
-                        if (e < kc * nc) {
-                            const int kk = e / nc, j = e % nc, k = k0 + kk;
-                            val = k < w ? b[(size_t)(a + k) * rhs + c0 + j] : ld_relaxed(x + (size_t)rc[k - w] * rhs + c0 + j);
-                        }
-                        v[u] = val;
-                    }
-#pragma unroll
-                    for (int u = 0; u < kStage; ++u) {
-                        const int e = base + threadIdx.x + u * 128;
-                        if (e < kc * nc) {
-                            const int kk = e / nc, j = e % nc, k = k0 + kk;
-                            double val = v[u];
-                            if (k >= w && Pend<double>::is(val) &&
-                                !wait_ready<double>(x + (size_t)rc[k - w] * rhs + c0 + j, val, ctl, budget)) {
-                                s_ok = 0;
-                                val = 0.0;
-                            }
-                            V[kk][j] = val;
-                        }
-                    }
-                }
-                __syncthreads();
-                if (!s_ok) { ok = false; break; }
-                // outputs: o = threadIdx.x + 128 q, row = o % 64, col = o / 64
-#pragma unroll
-                for (int q = 0; q < 16; ++q) {
-                    const int o = threadIdx.x + 128 * q;
-                    const int row = o & 63, cj = o >> 6;
-                    if (row < nrows && cj < nc) {
-                        const double* gr = g + (size_t)(r0 + row) * L + k0;
-                        double sacc = acc[q];
-                        for (int kk = 0; kk < kc; ++kk) sacc = fma(gr[kk], V[kk][cj], sacc);
-                        acc[q] = sacc;
-                    }
-                }
-                __syncthreads();
-            }
-            if (!ok) break;
-#pragma unroll
-            for (int q = 0; q < 16; ++q) {
-                const int o = threadIdx.x + 128 * q;
-                const int row = o & 63, cj = o >> 6;
-                if (row < nrows && cj < nc)
-                    st_relaxed(x + (size_t)(a + r0 + row) * rhs + c0 + cj, Pend<double>::fix(acc[q]));
-            }
-        }
-        if (__syncthreads_or(!ok)) break;
-    }
-}
 
 // BF16x3 tensor-core panel product, FP32 output (the mixed path's inner solve).
 __global__ void __launch_bounds__(128) k_sn_solve_bf16x3(SnArgs A, const __nv_bfloat16* __restrict__ Ghi,
@@ -454,7 +368,46 @@ int Handle::set_supernodes(int sn, const int* snodes_host) {
                                               sn_Glo.as<__nv_bfloat16>());
     ++launches;
     CUDA_TRY(cudaGetLastError());
+    // FP64 panel records: every 64-row panel of every chunk, its G split into column blocks
+    // (panels64.cu).  Items run chunk by chunk from the last; within a chunk, every panel's own
+    // right-hand-side blocks first (no waits), then the solved-row blocks farthest first.
+    std::vector<BChunk> pan;
+    std::vector<int2> pit;
+    long long prows = 0;
+    for (int s = S - 1; s >= 0; --s) {
+        const int w = ss[s + 1] - ss[s], K = w + m[s], nb = p64_nblk(w, K), no = p64_nown(w);
+        const int first = (int)pan.size();
+        for (int r0 = 0; r0 < w; r0 += kP64) {
+            BChunk c{};
+            c.sys = 0;
+            c.a = ss[s];
+            c.w = w;
+            c.m = m[s];
+            c.ld = ldh[s];
+            c.g64 = sn_G.as<double>() + goffh[s];
+            c.rect = sn_rect.as<int>() + roffh[s];
+            c.nblk = nb;
+            c.r0 = r0;
+            c.pw = std::min(kP64, w - r0);
+            c.poff = prows;
+            c.cbase = (int)pan.size();
+            prows += (long long)nb * c.pw;
+            pan.push_back(c);
+        }
+        const int np = (int)pan.size() - first;
+        for (int q = 0; q < no; ++q)
+            for (int p = 0; p < np; ++p) pit.push_back(make_int2(first + p, q));
+        for (int q = nb - 1; q >= no; --q)
+            for (int p = 0; p < np; ++p) pit.push_back(make_int2(first + p, q));
+    }
+    if ((rc = sn_pan.ensure(sizeof(BChunk) * pan.size())) || (rc = sn_pitems.ensure(sizeof(int2) * pit.size())))
+        return rc;
+    CUDA_TRY(cudaMemcpyAsync(sn_pan.p, pan.data(), sizeof(BChunk) * pan.size(), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(sn_pitems.p, pit.data(), sizeof(int2) * pit.size(), cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaStreamSynchronize(st));
+    sn_npan = (int)pan.size();
+    sn_npitems = (unsigned)pit.size();
+    sn_prows = prows;
     sn_count = S;
     sn_nitems = (int)item_s.size();
     have_supernodes = true;
@@ -477,13 +430,18 @@ SnArgs Handle::sn_args() const {
 }
 
 int launch_sn_solve(const Handle& h, bool mixed, const void* b, void* x, int rhs, int64_t budget, int64_t* launches) {
-    const SnArgs A = h.sn_args();
     if (!mixed) {
-        int per_sm = 0;
-        CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sn_solve_f64, 128, 0));
-        int grid = std::max(1, std::min(per_sm * h.sm_count, A.nitems));
-        k_sn_solve_f64<<<grid, 128, 0, h.st>>>(A, h.sn_G.as<double>(), rhs, (const double*)b, (double*)x, h.ctl, budget);
-    } else {
+        // the partial sums (sn_prows x rhs doubles) and the counters (one per panel and RHS group)
+        // are sized by Handle::prepare
+        const int ncnt = h.sn_npan * p64_groups(rhs);
+        if (h.sn_ppart.cap < sizeof(double) * (size_t)h.sn_prows * rhs || h.sn_pcnt.cap < sizeof(int) * (size_t)ncnt)
+            return SPTRSV_ERR_INVALID_ARG;
+        return launch_panels64(nullptr, rhs, (const double*)b, (double*)x, h.ctl, &h.ctl->ticket, budget,
+                               h.sn_pitems.as<int2>(), h.sn_npitems, h.sn_pan.as<BChunk>(), h.sn_ppart.as<double>(),
+                               h.sn_pcnt.as<int>(), ncnt, 64, h.sm_count, h.st, launches);
+    }
+    const SnArgs A = h.sn_args();
+    {
         int per_sm = 0;
         CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sn_solve_bf16x3, 128, 0));
         int grid = std::max(1, std::min(per_sm * h.sm_count, A.nitems));

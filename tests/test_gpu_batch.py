@@ -267,3 +267,15 @@ def test_profile_replay_matches_graph(orc, mixsys):
         assert set(pp) == {"fill_x", "pull_f64"}
         L.sptrsv_device_free(s.handle, d_b)
         L.sptrsv_device_free(s.handle, d_x)
+
+
+def test_new_handles_report_no_status_after_batches_free_memory(mixsys):
+    """Building panel schedules allocates and frees per-system work buffers with nonzero contents;
+    control blocks of handles created afterwards (which may reuse that memory) start cleared."""
+    with mixsys.batch() as B:
+        sched = B.schedule.copy()
+        sched[0::2] = 4
+        B.schedule = sched
+    for _ in range(8):
+        with sp.Solver(0) as s:
+            assert s.sync() == 0

@@ -104,3 +104,33 @@ def test_band_factor_skyline_panels(orc, solver, width, rhs):
     x = solver.solve(b, rhs=rhs, schedule="supernodal", precision="mixed", max_refine=20)
     assert solver.last_refine()[1] <= RES_TOL
     assert elem_err(x, ref) <= MIXED_ELEM_TOL
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_graph_replay_after_work_buffers_grow(orc, solver, nd12, prec):
+    """The same device b and x solved at 1, then 8, then 1 right-hand side: the 8-column solve
+    grows the handle's work buffers, and the second 1-column solve must not replay a graph
+    captured with their old addresses."""
+    import ctypes
+    m = nd12
+    L = sp._lib.lib()
+    solver.analyse(m.row_ptr, m.col, m.val).set_supernodes(m.snodes)
+    rpu = m.row_ptr.astype(np.uint64)
+    nb = 8 * m.n * 8
+    d_b, d_x = ctypes.c_void_p(), ctypes.c_void_p()
+    assert L.sptrsv_device_alloc(solver.handle, nb, ctypes.byref(d_b)) == 0
+    assert L.sptrsv_device_alloc(solver.handle, nb, ctypes.byref(d_x)) == 0
+    o = sp.make_opts(schedule="supernodal", precision=prec, max_refine=20)
+    try:
+        for rhs in (1, 8, 1):
+            b = gen.uniform(300 + rhs, m.n * rhs)
+            L.sptrsv_copy_h2d(solver.handle, d_b, b.ctypes.data, 8 * m.n * rhs)
+            solver.solve_device(d_b, d_x, rhs=rhs, opts=o)
+            x = np.empty(m.n * rhs)
+            L.sptrsv_copy_d2h(solver.handle, x.ctypes.data, d_x, 8 * m.n * rhs)
+            assert solver.sync() == 0
+            ref = orc.base_gauss_upper(rpu, m.col, m.val, b, rhs)
+            assert elem_err(x, ref) <= (ELEM_TOL if prec == "fp64" else MIXED_ELEM_TOL)
+    finally:
+        L.sptrsv_device_free(solver.handle, d_b)
+        L.sptrsv_device_free(solver.handle, d_x)
