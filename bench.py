@@ -531,6 +531,21 @@ def batch_cpu_sample(M, budget_s=12.0, seed=0):
                       f"projected to all {M.count} by nnz x rhs ({os.uname().machine} host)"}
 
 
+# FP64 FMA rate of a dependency-free FMA loop over every SM of a GB300 (2,070 MHz), the ceiling of
+# the FP64-pipe-bound kernels (the residual, the exact FP64 panels)
+FP64_GFMA_MEASURED = 502.0
+
+
+def fp64_rate(fma, prof_kind):
+    """FMAs per launch and the rate of the kind's first launch (every system active), also as a
+    fraction of the measured FP64 rate."""
+    if not prof_kind:
+        return {"fma_per_launch": fma, "gfma_per_s": None}
+    g = fma / (prof_kind[2] * 1e-3) / 1e9
+    return {"fma_per_launch": fma, "gfma_per_s": g, "frac_of_measured_fp64": g / FP64_GFMA_MEASURED,
+            "measured_fp64_gfma_per_s": FP64_GFMA_MEASURED}
+
+
 def run_batch(args, dist):
     import ctypes
     import sptrsv_gb300 as sp
@@ -676,11 +691,8 @@ def run_batch(args, dist):
                      {"bound": "hbm", "kernel": dom, "achieved": fb / (ms_step * 1e-3) / 1e9, "peak": peak,
                       "unit": "GB/s", "frac": fb / (ms_step * 1e-3) / 1e9 / peak, "peak_source": peak_src,
                       "traffic": None, "algorithmic_bytes_per_launch": fb, "note": "whole solve"}),
-        "fp64_residual": {"gfma_per_s": res_fma / (prof["residual_f64"][2] * 1e-3) / 1e9 if "residual_f64" in prof
-                          else None, "fma_per_launch": res_fma},
-        "fp64_panels": {"gfma_per_s": info["g_fma_f64"] / (prof["panels_f64"][2] * 1e-3) / 1e9
-                        if "panels_f64" in prof else None, "fma_per_launch": info["g_fma_f64"],
-                        "g_entries": info["g_entries_f64"]},
+        "fp64_residual": fp64_rate(res_fma, prof.get("residual_f64")),
+        "fp64_panels": dict(fp64_rate(info["g_fma_f64"], prof.get("panels_f64")), g_entries=info["g_entries_f64"]),
         "kernel_profile_chosen": {k: {"ms": v[0], "launches": v[1]} for k, v in prof.items()},
         "kernel_profile_plain": {k: {"ms": v[0], "launches": v[1]} for k, v in pplain.items()},
         "gpu_launches": int(sum(ks)),

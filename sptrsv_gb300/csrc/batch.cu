@@ -597,6 +597,98 @@ __global__ void __launch_bounds__(256) k_b_jacobi(BArgs A, const int4* __restric
     }
 }
 
+// The same sweep with one thread per ROW holding all of the row's right-hand-side columns in
+// registers (M >= rhs, columns c >= rhs predicated off): each lane walks its own row, so a warp has
+// 32 rows' column/value loads in flight per round trip instead of 32 / rhs rows' (the element
+// layout above shares one row's loads among rhs lanes), and each entry's rhs gathers are contiguous.
+// Entries go min(8, 16 / M) at a time (at least one): their column/value loads, then their
+// gathers (at most 16 values in flight, which keeps the kernel at 64 registers), then their FMAs
+// in entry order.
+template <int M>
+__device__ __forceinline__ void b_jacobi_rows(const BArgs& A, const int4 T, int k, int c0, const float* src,
+                                              float* dst, float& mx, float& ch) {
+    constexpr int kB = (16 / M) < 1 ? 1 : ((16 / M) < 8 ? (16 / M) : 8);
+    const int s = T.x, lane = threadIdx.x & 31;
+    const BSys S = A.sys[s];
+    const int m = S.rhs, mc = m - c0;  // this call's columns: c0 .. c0 + min(M, mc)
+    const int* rp = A.rp + S.rp0;
+    const int* cl = A.col + S.nz0;
+    const float* vl = A.val32 + S.nz0;
+    const float* invd = A.invd32 + S.row0;
+    const float* rr = A.r32 + S.xb0 + c0;
+    const float* so = src + S.xb0 + c0;
+    float* dd = dst + S.xb0 + c0;
+    for (int i0 = T.y; i0 < T.y + T.z; i0 += 32) {
+        const int i = i0 + lane;
+        if (i >= T.y + T.z) break;
+        float acc[M];
+#pragma unroll
+        for (int c = 0; c < M; ++c) acc[c] = 0.f;
+        if (k > 0) {
+            const int beg = __ldg(rp + i) + 1, end = __ldg(rp + i + 1);
+            for (int q0 = beg; q0 < end; q0 += kB) {
+                int jj[kB];
+                float vv[kB];
+#pragma unroll
+                for (int u = 0; u < kB; ++u) {
+                    const bool in = q0 + u < end;
+                    jj[u] = in ? __ldg(cl + q0 + u) : i;
+                    vv[u] = in ? __ldg(vl + q0 + u) : 0.f;
+                }
+                float g[kB][M];
+#pragma unroll
+                for (int u = 0; u < kB; ++u)
+#pragma unroll
+                    for (int c = 0; c < M; ++c) g[u][c] = (c < mc) ? so[(size_t)jj[u] * m + c] : 0.f;
+#pragma unroll
+                for (int u = 0; u < kB; ++u)
+#pragma unroll
+                    for (int c = 0; c < M; ++c) acc[c] = fmaf(vv[u], g[u][c], acc[c]);
+            }
+        }
+        const float di = __ldg(invd + i);
+#pragma unroll
+        for (int c = 0; c < M; ++c) {
+            if (c < mc) {
+                const size_t e = (size_t)i * m + c;
+                const float dn = (rr[e] - acc[c]) * di;
+                const float old = k > 0 ? so[e] : 0.f;
+                dd[e] = dn;
+                mx = fmaxf(mx, fabsf(dn));
+                ch = fmaxf(ch, fabsf(dn - old));
+            }
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_b_jacobi_rows(BArgs A, const int4* __restrict__ tasks, int ntasks) {
+    const int k = *(volatile const int*)&A.bc->sweep_k;
+    const float* src = (k & 1) ? A.d1 : A.d0;
+    float* dst = (k & 1) ? A.d0 : A.d1;
+    const int lane = threadIdx.x & 31;
+    const long long gw = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+    const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long t = gw; t < ntasks; t += nw) {
+        const int4 T = tasks[t];
+        const int s = T.x;
+        const BState& St = A.st[s];
+        if (St.done || St.inner_done) continue;
+        const int m = A.sys[s].rhs;
+        float mx = 0.f, ch = 0.f;
+        if (m == 1) b_jacobi_rows<1>(A, T, k, 0, src, dst, mx, ch);
+        else if (m == 2) b_jacobi_rows<2>(A, T, k, 0, src, dst, mx, ch);
+        else if (m <= 4) b_jacobi_rows<4>(A, T, k, 0, src, dst, mx, ch);
+        else if (m <= 8) b_jacobi_rows<8>(A, T, k, 0, src, dst, mx, ch);
+        else
+            for (int c0 = 0; c0 < m; c0 += 16) b_jacobi_rows<16>(A, T, k, c0, src, dst, mx, ch);
+        const float m1 = warp_max(mx), m2 = warp_max(ch);
+        if (lane == 0 && (m1 > 0.f || m2 > 0.f)) {
+            atomicMax(&A.st[s].dmax_bits, __float_as_uint(m1));
+            atomicMax(&A.st[s].dchg_bits, __float_as_uint(m2));
+        }
+    }
+}
+
 // --- FP64 residual ----------------------------------------------------------------------------
 
 // r = b - U x in FP64 for the systems still refining; r32 = (float) r; ||r||^2 per system
@@ -862,6 +954,8 @@ struct Batch {
     BArgs args(const double* b, double* x) const;
     int build_lists();
     int build_panels(int s, bool f64);
+    bool jacobi_elem = false;  // tuning override (SPTRSV_BJAC=elem): the thread-per-element sweep
+    void launch_jacobi(const BArgs& A);
     int build_graph(int mode, const double* b, double* x, cudaGraphExec_t* out, int64_t* fixed);
     int solve(int mode, const double* b, double* x);
     int sync(int64_t* kernels);
@@ -1064,7 +1158,8 @@ int Batch::build_lists() {
         rows = std::max(rpw, rows / rpw * rpw);
         for (int r0 = 0; r0 < sys[s].n; r0 += rows) tm.push_back(make_int4(s, r0, std::min(rows, sys[s].n - r0), 0));
         if (sched[s] == BS_JACOBI) {
-            const int jrows = std::max(1, 1024 / sys[s].rhs);  // about 1,024 (row, column) elements per task
+            // about 1,024 (row, column) elements per task, whole warps of rows
+            const int jrows = std::max(32, (1024 / sys[s].rhs + 31) / 32 * 32);
             for (int r0 = 0; r0 < sys[s].n; r0 += jrows)
                 tj.push_back(make_int4(s, r0, std::min(jrows, sys[s].n - r0), 0));
         }
@@ -1167,6 +1262,13 @@ static int elem_grid(int sm_count, long long total) {
 
 static int task_grid(int sm_count, long long tasks) {
     return (int)std::max(1LL, std::min((long long)sm_count * 8, (tasks + 7) / 8));
+}
+
+void Batch::launch_jacobi(const BArgs& A) {
+    if (jacobi_elem)
+        k_b_jacobi<<<task_grid(sm_count, n_tasks_jac), 256, 0, st>>>(A, tasks_jac.as<int4>(), n_tasks_jac);
+    else
+        k_b_jacobi_rows<<<task_grid(sm_count, n_tasks_jac), 256, 0, st>>>(A, tasks_jac.as<int4>(), n_tasks_jac);
 }
 
 static int row_grid(int sm_count, long long rows) {
@@ -1293,7 +1395,7 @@ int Batch::build_graph(int mode, const double* b, double* x, cudaGraphExec_t* ou
     if (!rc && ibody) {
         e = cudaStreamBeginCaptureToGraph(st, ibody, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
         if (e == cudaSuccess) {
-            k_b_jacobi<<<task_grid(sm_count, n_tasks_jac), 256, 0, st>>>(A, tasks_jac.as<int4>(), n_tasks_jac);
+            launch_jacobi(A);
             k_b_jcheck<<<1, 512, 0, st>>>(A, count, hi, true);
             e = cudaStreamEndCapture(st, &g2);
             if (!rc && e != cudaSuccess) rc = set_cuda_error(e, "batch capture inner");
@@ -1425,7 +1527,7 @@ int Batch::profile(int mode, const double* b, double* x, float* kind_ms, int* ki
                 if (jac_rows.nseg) {
                     if ((rc = read_ctl(&c))) goto out;
                     for (int sw = 0; sw < 100000 && c.jac_active > 0 && !c.c.status; ++sw) {
-                        if ((rc = timed(8, [&] { k_b_jacobi<<<task_grid(sm_count, n_tasks_jac), 256, 0, st>>>(A, tasks_jac.as<int4>(), n_tasks_jac); })) ||
+                        if ((rc = timed(8, [&] { launch_jacobi(A); })) ||
                             (rc = timed(9, [&] { k_b_jcheck<<<1, 512, 0, st>>>(A, count, none, false); })) ||
                             (rc = read_ctl(&c)))
                             goto out;
@@ -1533,6 +1635,7 @@ int sptrsv_batch_create(sptrsv_batch* out, int device, int count, const int* n, 
     B->panel_ok.assign(count, -1);
     B->have_bf16.assign(count, 0);
     if (const char* e = getenv("SPTRSV_P64_CTAS")) B->p64_ctas_per_sm = std::max(1, atoi(e));
+    if (const char* e = getenv("SPTRSV_BJAC")) B->jacobi_elem = strcmp(e, "elem") == 0;
     B->have_f64.assign(count, 0);
     B->gidx.assign(count, -1);
     B->pchunks.resize(count);

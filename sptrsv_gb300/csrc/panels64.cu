@@ -6,6 +6,14 @@
 
 namespace sptrsv {
 
+// 8-byte global -> shared copies that complete asynchronously (no register staging), so a tile's
+// loads are all in flight together and overlap the waits on the right-hand side.
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+    const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
 // Work item (panel, block, RHS group): the block's columns of G times the matching rows of
 // [b ; x_R] for one group of right-hand-side columns (waiting on solved rows), written to the
 // panel's partial-sum slot for that block.  The CTA that completes the last block of a (panel,
@@ -53,10 +61,11 @@ __global__ void __launch_bounds__(128) k_panels64(const BSys* __restrict__ sys, 
         const double* b = bbase + xb0;
         double* x = xbase + xb0;
         double* pb = part + poff + (long long)blk * pw * m;
-        // the block of G (the panel's rows, columns k0 .. k0+kc)
+        // the block of G (the panel's rows, columns k0 .. k0+kc), copied asynchronously while the
+        // right-hand side below is gathered and waited on
         for (int e = threadIdx.x; e < pw * kc; e += blockDim.x) {
             const int r = e / kc, kk = e - r * kc;
-            Gs[r][kk] = C.g64[(size_t)(r0 + r) * L + k0 + kk];
+            cp_async8(&Gs[r][kk], C.g64 + (size_t)(r0 + r) * L + k0 + kk);
         }
         if (threadIdx.x == 0) s_ok = 1;
         __syncthreads();
@@ -89,6 +98,7 @@ __global__ void __launch_bounds__(128) k_panels64(const BSys* __restrict__ sys, 
                 }
             }
         }
+        cp_async_wait_all();
         __syncthreads();
         const bool ok = s_ok;
         if (ok) {
