@@ -403,7 +403,7 @@ def run_ours(args, dist):
     dom_times = [t for t in per_kind[dom_kind] if t > 0]
     dom_avg_ms = sum(dom_times) / len(dom_times)
     if dom_kind == 9:
-        dom_bytes, dom_name = jacobi_bytes(n, nnz), "k_jacobi_batched"
+        dom_bytes, dom_name = jacobi_bytes(n, nnz), "k_jacobi_pairs"
     elif dom_kind == 7:
         dom_bytes, dom_name = fp64_bytes(n, nnz) - 8 * n, "k_residual_tile"
     else:

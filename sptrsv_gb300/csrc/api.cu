@@ -446,8 +446,29 @@ int Handle::ensure_offdiag() {
         return 0;
     }
     const int kRoffPad = 64;
-    if ((rc = offdiag.ensure(sizeof(int2) * ((size_t)(nnz - n) + 4)))) return rc;
     if ((rc = roff.ensure(sizeof(int) * ((size_t)n + 1 + kRoffPad)))) return rc;
+    if (sweep_kernel == 0) {
+        // the paired layout of the default sweep: rows padded to an even slot count
+        if ((rc = scratch.ensure(sizeof(int) * ((size_t)n + scan_partials_needed(n) + 64)))) return rc;
+        int* len2 = scratch.as<int>();
+        int* part = len2 + n + 32;
+        if ((rc = launch_pair_offsets(n, rp, len2, roff.as<int>(), kRoffPad, part, sm_count, st, &launches)))
+            return rc;
+        int total = 0;
+        CUDA_TRY(cudaMemcpyAsync(&total, roff.as<int>() + n, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaStreamSynchronize(st));
+        if ((rc = offdiag.ensure(sizeof(int2) * ((size_t)total + 4)))) return rc;
+        CUDA_TRY(cudaMemsetAsync(offdiag.p, 0, sizeof(int2) * ((size_t)total + 4), st));
+        if ((rc = launch_build_offdiag_pairs(n, rp, col, val, roff.as<int>(), offdiag.as<int2>(), sm_count, st,
+                                             &launches)))
+            return rc;
+        CUDA_TRY(cudaStreamSynchronize(st));
+        off_pairs = true;
+        have_offdiag = true;
+        return 0;
+    }
+    off_pairs = false;
+    if ((rc = offdiag.ensure(sizeof(int2) * ((size_t)(nnz - n) + 4)))) return rc;
     CUDA_TRY(cudaMemsetAsync(offdiag.p, 0, sizeof(int2) * ((size_t)(nnz - n) + 4), st));
     if ((rc = launch_build_offdiag(n, rp, col, val, offdiag.as<int2>(), roff.as<int>(), kRoffPad, sm_count, st,
                                    &launches)))
@@ -472,6 +493,7 @@ int Handle::refine_args(const sptrsv_opts& o, const double* b, double* x, int rh
     const bool sl = have_offdiag && rhs == 1 && sweep_kernel == 6;
     r.off = (have_offdiag && rhs == 1 && !sl) ? offdiag.as<int2>() : nullptr;
     r.roff = (have_offdiag && rhs == 1 && !sl) ? roff.as<int>() : nullptr;
+    r.pairs = off_pairs ? 1 : 0;
     r.sweep_kernel = sweep_kernel;
     r.nslices = sl ? sell_nslices : 0;
     r.sell_perm = sl ? sell_perm.as<int>() : nullptr;
@@ -818,8 +840,8 @@ int sptrsv_create(sptrsv_handle* out, int device) {
     if (rc) { delete h; return rc; }
     const char* g = getenv("SPTRSV_NO_GRAPH");
     h->use_graphs = !(g && g[0] == '1');
-    // tuning override of the Jacobi sweep kernel: batch8 (default), batch4, direct, tile, tile8, direct2, tma,
-    // sell
+    // tuning override of the Jacobi sweep kernel (default: lane per row over entry pairs): batch8,
+    // batch4, direct, tile, tile8, direct2, tma, sell
     const char* sk = getenv("SPTRSV_SWEEP_KERNEL");
     h->sweep_kernel = 0;
     if (sk && strcmp(sk, "sell") == 0) h->sweep_kernel = 6;

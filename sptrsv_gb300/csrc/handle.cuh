@@ -68,6 +68,7 @@ struct Handle {
     bool have_csc = false;
     DevBuf offdiag;        // interleaved FP32 off-diagonals for the Jacobi sweeps
     DevBuf roff;           // per-row first off-diagonal slot, padded by kRoffPad
+    bool off_pairs = false;  // offdiag/roff in the paired layout (rows padded to an even count)
     DevBuf sell, sell_perm, sell_len, sell_ptr;  // SELL-32-256 copy of the off-diagonals
     int sell_nslices = 0;
     // supernode partition and its dense panels (supernodal.cu)

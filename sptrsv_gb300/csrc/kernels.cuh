@@ -96,8 +96,10 @@ struct RefineArgs {
     const float* invd32;
     const int2* off;   // interleaved (column, FP32 value) off-diagonals, or nullptr
     const int* roff;   // first off-diagonal slot of every row (rp[i] - i), padded, or nullptr
-    int sweep_kernel;  // 0/2 lane per row (default), 1 warp tiles, 3 tiles at 8 blocks/SM,
-                       // 4 two rows per lane, 5 bulk-copy pipeline, 6 SELL slices
+    int pairs;         // off/roff in the paired layout: every row's slots padded to an even count
+    int sweep_kernel;  // 0 lane per row over entry pairs (default), 1 warp tiles, 2 lane per row,
+                       // 3 tiles at 8 blocks/SM, 4 two rows per lane, 5 bulk-copy pipeline,
+                       // 6 SELL slices, 7/8 lane per row with 4/8-entry batches
     int nslices;       // SELL: slices of 32 rows
     const int* sell_perm;  // SELL: row of every slice lane (-1 = padding)
     const int* sell_len;   // SELL: entries per lane of every slice
@@ -118,6 +120,14 @@ struct RefineArgs {
 };
 int launch_build_offdiag(int n, const int* rp, const int* col, const double* val, int2* off, int* roff,
                          int roff_pad, int sm_count, cudaStream_t st, int64_t* launches);
+// Paired layout: roff[i] = sum over rows j < i of their off-diagonal count rounded up to even
+// (roff[n .. n + roff_pad] = the total); launch_pair_offsets fills roff (len2 and part are
+// scratch of n and scan_partials_needed(n) ints), launch_build_offdiag_pairs the entries: a row of
+// odd length ends with the pad entry (its own column, value 0).
+int launch_pair_offsets(int n, const int* rp, int* len2, int* roff, int roff_pad, int* part, int sm_count,
+                        cudaStream_t st, int64_t* launches);
+int launch_build_offdiag_pairs(int n, const int* rp, const int* col, const double* val, const int* roff, int2* off,
+                               int sm_count, cudaStream_t st, int64_t* launches);
 int sell_prepare(int n, const int* rp, int* perm, int* slen, int* sptr, int* part, int sm_count, cudaStream_t st,
                  int64_t* launches, int* total);
 int sell_fill(int n, const int* rp, const int* col, const double* val, const int* perm, const int* slen,

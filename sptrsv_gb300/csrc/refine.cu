@@ -84,6 +84,30 @@ __global__ void k_build_roff(int n, int pad, const int* __restrict__ rp, int* __
         roff[i] = (i <= n) ? rp[i] - i : rp[n] - n;
 }
 
+__global__ void k_pair_len(int n, const int* __restrict__ rp, int* __restrict__ len2) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int len = rp[i + 1] - rp[i] - 1;
+        len2[i] = len + (len & 1);
+    }
+}
+
+__global__ void k_pad_roff(int n, int pad, int* __restrict__ roff) {
+    const int total = roff[n];
+    for (int i = n + 1 + blockIdx.x * blockDim.x + threadIdx.x; i <= n + pad; i += gridDim.x * blockDim.x)
+        roff[i] = total;
+}
+
+__global__ void k_build_offdiag_pairs(int n, const int* __restrict__ rp, const int* __restrict__ col,
+                                      const double* __restrict__ val, const int* __restrict__ roff,
+                                      int2* __restrict__ off) {
+    const int lane = threadIdx.x & 31;
+    for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += (gridDim.x * blockDim.x) >> 5) {
+        const int b = rp[i] + 1, len = rp[i + 1] - b, o = roff[i];
+        for (int k = lane; k < len; k += 32) off[o + k] = make_int2(col[b + k], __float_as_int((float)val[b + k]));
+        if (lane == 0 && (len & 1)) off[o + len] = make_int2(i, __float_as_int(0.f));
+    }
+}
+
 // Jacobi seed d0 = D^-1 r from the FP32 residual and FP32 reciprocal (FP32 pipe; the FP64 pipe
 // is the residual kernels' bottleneck on this GPU), or the pending fill for an exact inner solve.
 __device__ __forceinline__ void seed_out(int seed, float* d0, size_t p, float r32, float invd32) {
@@ -439,6 +463,64 @@ __global__ void __launch_bounds__(256, MINB) k_jacobi_batched(int n, const int* 
             for (int j = 0; j < B; ++j) g[j] = (k0 + j < e) ? __ldg(src + p[j].x) : 0.f;
 #pragma unroll
             for (int j = 0; j < B; ++j) sum = fmaf(__int_as_float(p[j].y), g[j], sum);
+        }
+        const float d = (ri - sum) * di;
+        if (stats) {
+            dmax = fmaxf(dmax, fabsf(d));
+            dchg = fmaxf(dchg, fabsf(d - src[i]));
+        }
+        if (last) x[i] += (double)d;
+        else dst[i] = d;
+        i = inext;
+        s = sn;
+        e = en;
+    }
+    if (stats) reduce_stats(dmax, dchg, ctl, s_max);
+}
+
+// The lane-per-row sweep over the paired layout: every row's slots start on a 16-byte boundary and
+// come in pairs, so one 16-byte load brings two entries (half the load instructions, and the L1
+// wavefronts, of 8-byte entry loads).  B entries (B/2 pair loads, then B gathers, then B FMAs in
+// entry order) per batch; the next row's offsets are fetched while the current row is summed.  The
+// pad entry of an odd row adds 0 * d_i.
+template <int B, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_jacobi_pairs(int n, const int* __restrict__ roff,
+                                                           const int4* __restrict__ off2,
+                                                           const float* __restrict__ invd,
+                                                           const float* __restrict__ r,
+                                                           const float* __restrict__ src, float* __restrict__ dst,
+                                                           double* __restrict__ x, int last, int stats, Ctl* ctl) {
+    static_assert(B % 2 == 0, "entries come in pairs");
+    __shared__ unsigned s_max[2];
+    if (is_done(ctl)) return;
+    if (threadIdx.x < 2) s_max[threadIdx.x] = 0u;
+    __syncthreads();
+    float dmax = 0.f, dchg = 0.f;
+    const int stride = gridDim.x * blockDim.x;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int s = 0, e = 0;
+    if (i < n) { s = __ldg(roff + i); e = __ldg(roff + i + 1); }
+    while (i < n) {
+        const int inext = i + stride;
+        int sn = 0, en = 0;
+        if (inext < n) { sn = __ldg(roff + inext); en = __ldg(roff + inext + 1); }
+        const float ri = r[i], di = invd[i];
+        float sum = 0.f;
+        for (int k0 = s; k0 < e; k0 += B) {
+            int4 p[B / 2];
+            float g[B];
+#pragma unroll
+            for (int j = 0; j < B / 2; ++j) p[j] = (k0 + 2 * j < e) ? __ldg(off2 + (k0 >> 1) + j) : make_int4(i, 0, i, 0);
+#pragma unroll
+            for (int j = 0; j < B / 2; ++j) {
+                g[2 * j] = (k0 + 2 * j < e) ? __ldg(src + p[j].x) : 0.f;
+                g[2 * j + 1] = (k0 + 2 * j < e) ? __ldg(src + p[j].z) : 0.f;
+            }
+#pragma unroll
+            for (int j = 0; j < B / 2; ++j) {
+                sum = fmaf(__int_as_float(p[j].y), g[2 * j], sum);
+                sum = fmaf(__int_as_float(p[j].w), g[2 * j + 1], sum);
+            }
         }
         const float d = (ri - sum) * di;
         if (stats) {
@@ -898,6 +980,27 @@ static int resident_grid(const void* fn, int block, int sm_count) {
 
 static size_t tma_smem_bytes() { return sizeof(TmaStage) * kStages * kTmaWarps; }
 
+int launch_pair_offsets(int n, const int* rp, int* len2, int* roff, int roff_pad, int* part, int sm_count,
+                        cudaStream_t st, int64_t* launches) {
+    k_pair_len<<<sm_count * 4, 256, 0, st>>>(n, rp, len2);
+    ++*launches;
+    CUDA_TRY(cudaGetLastError());
+    int rc = scan_exclusive(len2, roff, n, part, st, launches);
+    if (rc) return rc;
+    k_pad_roff<<<1, 64, 0, st>>>(n, roff_pad, roff);
+    ++*launches;
+    CUDA_TRY(cudaGetLastError());
+    return 0;
+}
+
+int launch_build_offdiag_pairs(int n, const int* rp, const int* col, const double* val, const int* roff, int2* off,
+                               int sm_count, cudaStream_t st, int64_t* launches) {
+    k_build_offdiag_pairs<<<sm_count * 8, 256, 0, st>>>(n, rp, col, val, roff, off);
+    ++*launches;
+    CUDA_TRY(cudaGetLastError());
+    return 0;
+}
+
 int launch_build_offdiag(int n, const int* rp, const int* col, const double* val, int2* off, int* roff,
                          int roff_pad, int sm_count, cudaStream_t st, int64_t* launches) {
     k_build_offdiag<<<sm_count * 8, 256, 0, st>>>(n, rp, col, val, off);
@@ -981,7 +1084,12 @@ int launch_jacobi_sweep(const RefineArgs& a, int src, bool last, bool stats) {
     const float* s = a.d32[src];
     float* d = a.d32[src ^ 1];
     const int st_flag = stats ? 1 : 0;
-    if (use_tiles(a) && a.roff && (a.sweep_kernel == 7)) {
+    if (use_tiles(a) && a.roff && a.pairs) {
+        static int grid_p8 = 0;
+        if (!grid_p8) grid_p8 = resident_grid((const void*)k_jacobi_pairs<8, 6>, 256, a.sm_count);
+        k_jacobi_pairs<8, 6><<<grid_p8, 256, 0, a.st>>>(a.n, a.roff, reinterpret_cast<const int4*>(a.off), a.invd32,
+                                                       a.r32, s, d, a.x, last, st_flag, a.ctl);
+    } else if (use_tiles(a) && a.roff && (a.sweep_kernel == 7)) {
         static int grid_b4 = 0;
         if (!grid_b4) grid_b4 = resident_grid((const void*)k_jacobi_batched<4, 8>, 256, a.sm_count);
         k_jacobi_batched<4, 8><<<grid_b4, 256, 0, a.st>>>(a.n, a.roff, a.off, a.invd32, a.r32, s, d, a.x, last,
