@@ -25,7 +25,7 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 // Batched (sys != nullptr): items[t] = {panel, block | group << 16}, one per ticket; the panel's
 // poff and cbase are absolute.  One system (sys == nullptr, `rhs` columns at offset 0): ticket t is
 // group t % ncg of item t / ncg, and poff and cbase count per column and per group.
-__global__ void __launch_bounds__(128) k_panels64(const BSys* __restrict__ sys, int rhs, int ncg,
+__global__ void __launch_bounds__(128, 8) k_panels64(const BSys* __restrict__ sys, int rhs, int ncg,
                                                   const double* __restrict__ bbase, double* xbase, Ctl* ctl,
                                                   unsigned* ticket, int64_t budget, const int2* __restrict__ items,
                                                   unsigned ntickets, const BChunk* __restrict__ panels,
