@@ -245,6 +245,23 @@ def cpu_paths(m, b, budget_s=8.0):
             "paths": res, "best": best, "fn": serial if best.startswith("serial") else levelset}
 
 
+def errors_vs_serial(m, b, solutions):
+    """Error of each GPU solution against the reference's serial FP64 solve of the same system
+    (the oracle's C restatement, whose outputs the golden tests pin to the compiled reference):
+    relative residual
+    ||b - U x|| / ||b|| and max_i |x_i - x_ref_i| / |x_ref_i| (components with |x_ref_i| < 1e-12
+    are measured against 1e-12), plus the reference-style relative 2-norm error (utils.cpp:355-380)."""
+    from oracle import oracle
+    rpu = m.row_ptr.astype(np.uint64)
+    x_ref = oracle.base_gauss_upper(rpu, m.col, m.val, b, 1)
+    out = {"oracle": "serial base_gauss_upper (core.cpp:18-32), FP64"}
+    for name, xg in solutions.items():
+        out[name] = {"rel_residual": oracle.rel_residual(rpu, m.col, m.val, xg, b, 1),
+                     "max_elem_rel_error": oracle.max_elem_rel_error(x_ref, xg, 1e-12),
+                     "rel_error_2norm": oracle.rel_error(x_ref, xg)}
+    return out
+
+
 def run_reference_batch(args):
     """The reference's serial solve over the batched mix: each step solves a bounded random
     sample of the systems (about 10 s) and is projected to the whole mix by nnz x rhs."""
@@ -344,11 +361,13 @@ def run_ours(args, dist):
 
     # correctness of both forms before timing
     x = np.empty(n)
+    x_plain = np.empty(n)
     for o in (chosen, plain):
         dev_solve(o)
         rc = s.sync()
         if rc:
             raise sp.SptrsvError(rc, "check solve")
+    L.sptrsv_copy_d2h(h, x_plain.ctypes.data, d_x, nbytes)
     dev_solve(chosen)
     assert s.sync() == 0
     steps_ref, rel_res = s.last_refine()
@@ -434,6 +453,7 @@ def run_ours(args, dist):
     e2e_value = dist.ws * args.steps / e2e_total
 
     cpu = None
+    vs_oracle = None
     if dist.rank == 0 and dist.ws >= 1 and not args.no_cpu_baseline:
         try:
             cb = cpu_paths(m, b)
@@ -441,6 +461,7 @@ def run_ours(args, dist):
             cb.pop("paths")
             cb.pop("best")
             cpu = cb
+            vs_oracle = errors_vs_serial(m, b, {"chosen": x, "plain_fp64_syncfree": x_plain})
         except Exception as e:  # the baseline is reported, never required
             cpu = {"value": None, "unit": "solves/s", "error": str(e)[:200]}
 
@@ -468,6 +489,7 @@ def run_ours(args, dist):
         "gflops": (2 * (nnz - n) + n) * value / 1e9,
         "rel_residual": rel_res, "refine_steps": steps_ref, "inner_sweeps": sweeps_ref,
         "max_abs_err_vs_xstar": err_xstar,
+        "vs_oracle": vs_oracle,
         "plain_fp64_syncfree": {"solves_per_s": plain_sps, "ms_per_solve": 1e3 / plain_sps,
                                 "hbm_gbs": fb * plain_sps / 1e9},
         "speedup_vs_plain": value / dist.ws / plain_sps,

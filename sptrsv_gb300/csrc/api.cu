@@ -445,9 +445,38 @@ int Handle::ensure_offdiag() {
         have_offdiag = true;
         return 0;
     }
+    if (sweep_kernel == 9) {
+        // the group-jagged layout (32-row groups, jagged diagonals)
+        const int ngroups = (n + 31) / 32;
+        if ((rc = jbase.ensure(sizeof(int) * ((size_t)ngroups + 2)))) return rc;
+        if ((rc = jmeta.ensure(sizeof(int) * (size_t)ngroups * 32))) return rc;
+        if ((rc = scratch.ensure(sizeof(int) * ((size_t)ngroups + scan_partials_needed(ngroups) + 64)))) return rc;
+        int* gsize = scratch.as<int>();
+        int* part = gsize + ngroups + 32;
+        int* overflow = jbase.as<int>() + ngroups + 1;
+        CUDA_TRY(cudaMemsetAsync(overflow, 0, sizeof(int), st));
+        if ((rc = launch_jds_sizes(n, rp, gsize, overflow, sm_count, st, &launches))) return rc;
+        if ((rc = scan_exclusive(gsize, jbase.as<int>(), ngroups, part, st, &launches))) return rc;
+        int tail[2] = {0, 0};
+        CUDA_TRY(cudaMemcpyAsync(tail, jbase.as<int>() + ngroups, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaStreamSynchronize(st));
+        if (tail[1] == 0) {
+            if ((rc = offdiag.ensure(sizeof(int2) * ((size_t)tail[0] + 4)))) return rc;
+            if ((rc = launch_jds_fill(n, rp, col, val, jbase.as<int>(), jmeta.as<int>(), offdiag.as<int2>(), sm_count,
+                                      st, &launches)))
+                return rc;
+            CUDA_TRY(cudaStreamSynchronize(st));
+            off_jds = true;
+            off_pairs = false;
+            have_offdiag = true;
+            return 0;
+        }
+        // a row too long for the group metadata: the paired layout instead
+    }
+    off_jds = false;
     const int kRoffPad = 64;
     if ((rc = roff.ensure(sizeof(int) * ((size_t)n + 1 + kRoffPad)))) return rc;
-    if (sweep_kernel == 0) {
+    if (sweep_kernel == 0 || sweep_kernel == 9) {
         // the paired layout of the default sweep: rows padded to an even slot count
         if ((rc = scratch.ensure(sizeof(int) * ((size_t)n + scan_partials_needed(n) + 64)))) return rc;
         int* len2 = scratch.as<int>();
@@ -494,6 +523,8 @@ int Handle::refine_args(const sptrsv_opts& o, const double* b, double* x, int rh
     r.off = (have_offdiag && rhs == 1 && !sl) ? offdiag.as<int2>() : nullptr;
     r.roff = (have_offdiag && rhs == 1 && !sl) ? roff.as<int>() : nullptr;
     r.pairs = off_pairs ? 1 : 0;
+    r.jmeta = (have_offdiag && rhs == 1 && off_jds) ? jmeta.as<int>() : nullptr;
+    r.jbase = (have_offdiag && rhs == 1 && off_jds) ? jbase.as<int>() : nullptr;
     r.sweep_kernel = sweep_kernel;
     r.nslices = sl ? sell_nslices : 0;
     r.sell_perm = sl ? sell_perm.as<int>() : nullptr;
@@ -754,7 +785,7 @@ Handle::~Handle() {
     if (prof0) cudaEventDestroy(prof0);
     DevBuf* bufs[] = {&own_rp, &own_col, &own_val, &val32, &invd, &invd32, &in_degree, &levels, &level_ptr,
                       &level_rows, &stats, &csc_ptr, &csc_row, &csc_val, &scratch, &xw, &bw, &r32, &d32a, &d32b,
-                      &norms, &indeg_work, &left, &db, &dx, &flush, &offdiag, &roff, &sell, &sell_perm, &sell_len, &sell_ptr,
+                      &norms, &indeg_work, &left, &db, &dx, &flush, &offdiag, &roff, &jmeta, &jbase, &sell, &sell_perm, &sell_len, &sell_ptr,
                       &sn_start, &sn_m, &sn_roff, &sn_rect, &sn_goff, &sn_ld, &sn_colbase, &sn_outbase, &sn_items,
                       &sn_G, &sn_Ghi, &sn_Glo, &sn_pan, &sn_pitems, &sn_pcnt, &sn_ppart, &tune_b, &tune_x};
     for (DevBuf* b : bufs) b->release();
@@ -840,11 +871,12 @@ int sptrsv_create(sptrsv_handle* out, int device) {
     if (rc) { delete h; return rc; }
     const char* g = getenv("SPTRSV_NO_GRAPH");
     h->use_graphs = !(g && g[0] == '1');
-    // tuning override of the Jacobi sweep kernel (default: lane per row over entry pairs): batch8,
-    // batch4, direct, tile, tile8, direct2, tma, sell
+    // tuning override of the Jacobi sweep kernel (default: lane per row over entry pairs): jds,
+    // batch8, batch4, direct, tile, tile8, direct2, tma, sell
     const char* sk = getenv("SPTRSV_SWEEP_KERNEL");
     h->sweep_kernel = 0;
     if (sk && strcmp(sk, "sell") == 0) h->sweep_kernel = 6;
+    if (sk && strcmp(sk, "jds") == 0) h->sweep_kernel = 9;
     if (sk && strcmp(sk, "batch4") == 0) h->sweep_kernel = 7;
     if (sk && strcmp(sk, "batch8") == 0) h->sweep_kernel = 8;
     if (sk && strcmp(sk, "tile") == 0) h->sweep_kernel = 1;

@@ -69,6 +69,9 @@ struct Handle {
     DevBuf offdiag;        // interleaved FP32 off-diagonals for the Jacobi sweeps
     DevBuf roff;           // per-row first off-diagonal slot, padded by kRoffPad
     bool off_pairs = false;  // offdiag/roff in the paired layout (rows padded to an even count)
+    DevBuf jmeta;          // group-jagged layout: per 32-row group, lane R -> (row << 27) | count
+    DevBuf jbase;          // group-jagged layout: first entry of every group (+ total, overflow flag)
+    bool off_jds = false;  // offdiag holds the group-jagged entries
     DevBuf sell, sell_perm, sell_len, sell_ptr;  // SELL-32-256 copy of the off-diagonals
     int sell_nslices = 0;
     // supernode partition and its dense panels (supernodal.cu)

@@ -97,9 +97,12 @@ struct RefineArgs {
     const int2* off;   // interleaved (column, FP32 value) off-diagonals, or nullptr
     const int* roff;   // first off-diagonal slot of every row (rp[i] - i), padded, or nullptr
     int pairs;         // off/roff in the paired layout: every row's slots padded to an even count
+    const int* jmeta;  // group-jagged layout (off holds its entries): per group lane (row << 27) | count
+    const int* jbase;  // group-jagged layout: first entry of every 32-row group
     int sweep_kernel;  // 0 lane per row over entry pairs (default), 1 warp tiles, 2 lane per row,
                        // 3 tiles at 8 blocks/SM, 4 two rows per lane, 5 bulk-copy pipeline,
-                       // 6 SELL slices, 7/8 lane per row with 4/8-entry batches
+                       // 6 SELL slices, 7/8 lane per row with 4/8-entry batches, 9 warp per
+                       // 32-row group over the group-jagged layout
     int nslices;       // SELL: slices of 32 rows
     const int* sell_perm;  // SELL: row of every slice lane (-1 = padding)
     const int* sell_len;   // SELL: entries per lane of every slice
@@ -124,6 +127,14 @@ int launch_build_offdiag(int n, const int* rp, const int* col, const double* val
 // (roff[n .. n + roff_pad] = the total); launch_pair_offsets fills roff (len2 and part are
 // scratch of n and scan_partials_needed(n) ints), launch_build_offdiag_pairs the entries: a row of
 // odd length ends with the pad entry (its own column, value 0).
+// Group-jagged layout of the `jds` sweep (32-row groups, rows ranked longest first, jagged
+// diagonals contiguous): launch_jds_sizes writes every group's entry count into gsize (n/32
+// rounded up ints) and sets *overflow when a row has 2^27 or more entries; after an exclusive scan
+// of gsize into jbase, launch_jds_fill writes jmeta (32 ints per group) and the entries.
+int launch_jds_sizes(int n, const int* rp, int* gsize, int* overflow, int sm_count, cudaStream_t st,
+                     int64_t* launches);
+int launch_jds_fill(int n, const int* rp, const int* col, const double* val, const int* jbase, int* jmeta, int2* jent,
+                    int sm_count, cudaStream_t st, int64_t* launches);
 int launch_pair_offsets(int n, const int* rp, int* len2, int* roff, int roff_pad, int* part, int sm_count,
                         cudaStream_t st, int64_t* launches);
 int launch_build_offdiag_pairs(int n, const int* rp, const int* col, const double* val, const int* roff, int2* off,

@@ -134,6 +134,28 @@ def test_mixed_refinement_reaches_1e12(golden, orc, solver, inner, tag):
     assert elem_err(x, golden[tag + "/base"][: len(x)]) <= MIXED_ELEM_TOL
 
 
+@pytest.mark.parametrize("layout", ["jds", "batch8", "sell"])
+def test_mixed_sweep_layouts(golden, orc, monkeypatch, layout):
+    """The selectable layouts of the Jacobi sweep (SPTRSV_SWEEP_KERNEL, read when a handle is
+    created) reach the same tolerances as the default paired layout: rows of every length, groups
+    and slices cut by n, and the 2-8-row tails of the golden systems."""
+    monkeypatch.setenv("SPTRSV_SWEEP_KERNEL", layout)
+    m = gen.random_upper(50_003, 8.0, 0.9, 64, 5)
+    xs, b = gen.system(m, 11)
+    cases = [(m.row_ptr, m.col, m.val, b)]
+    for t in ("rand3000", "snr800", "csr_5_upper"):
+        rp, col, val, bt, _ = _case(golden, t)
+        cases.append((rp, col, val, bt[: len(rp) - 1]))
+    with sp.Solver(0) as s:
+        for rp, col, val, bb in cases:
+            s.analyse(rp, col, val)
+            x = s.solve(bb, precision="mixed", schedule="jacobi", max_refine=20)
+            assert s.last_refine()[1] <= RES_TOL, layout
+            ref = orc.base_gauss_upper(np.asarray(rp).astype(np.uint64), col, val, bb, 1)
+            assert orc.rel_residual(np.asarray(rp).astype(np.uint64), col, val, x, bb, 1) <= 2 * RES_TOL
+            assert elem_err(x, ref) <= MIXED_ELEM_TOL, layout
+
+
 def test_device_pointer_api(orc, solver):
     torch = pytest.importorskip("torch")
     m = gen.random_upper(20_000, 8.0, 0.9, 64, 41)
