@@ -101,7 +101,8 @@ typedef struct sptrsv_opts {
     double tol;             /* MIXED: target ||b - U x||_2 / ||b||_2 */
     int64_t spin_budget_ns; /* per-wait limit of every device spin (0 = 2 s) */
     int resident_warps;     /* sync-free kernels: warps launched (0 = chosen from the level width) */
-    int inner_tol_exp;      /* MIXED + JACOBI: inner sweeps stop when max|change| <= 10^-e max|d| (0 = 6) */
+    int inner_tol_exp;      /* MIXED + JACOBI: inner sweeps stop when max|change| <= eps max|d|, eps =
+                               max(10^-e, 0.1 tol / last relative residual) (0: e = 6) */
 } sptrsv_opts;
 
 typedef struct sptrsv_ctx* sptrsv_handle;

@@ -230,6 +230,8 @@ sptrsv_opts Handle::resolve(const sptrsv_opts* o, int rhs) const {
         if (r.inner == SPTRSV_SCHED_JACOBI && !(max_ratio < 1.0)) r.inner = SPTRSV_SCHED_SYNCFREE_WARP;
         // flat (unlooped) graphs run a fixed number of sweeps per correction
         if (r.inner_sweeps <= 0) r.inner_sweeps = 16;
+        // the floor of the inner change test; a correction that needs less (its residual is
+        // already near the tolerance) stops earlier, see k_check_outer
         if (r.inner_tol_exp <= 0) r.inner_tol_exp = 6;
     }
     if (r.rows_per_warp <= 0) {

@@ -804,7 +804,7 @@ __global__ void k_b_inner_begin(BArgs A, int count, cudaGraphConditionalHandle i
 }
 
 // After a Jacobi sweep: per-system change test |d_new - d_old| <= eps |d_new| (max norms) or the
-// sweep cap.
+// sweep cap; eps = max(10^-inner_tol_exp, 0.1 tol / the system's last relative residual).
 __global__ void k_b_jcheck(BArgs A, int count, cudaGraphConditionalHandle inner, bool set_cond) {
     const int k = A.bc->sweep_k;
     int still = 0, swept = 0;
@@ -818,7 +818,12 @@ __global__ void k_b_jcheck(BArgs A, int count, cudaGraphConditionalHandle inner,
                 ++T.inner_count;
                 ++T.sweeps;
                 const float mx = __uint_as_float(T.dmax_bits), ch = __uint_as_float(T.dchg_bits);
-                const bool conv = k > 0 ? ch <= A.inner_eps * mx : mx == 0.f;
+                // a correction (after the first residual) only needs a tenth of what takes this
+                // system's residual to the tolerance, never tighter than the FP32 floor
+                const float eps = (T.steps > 0 && T.rel > 0.0)
+                                      ? fmaxf(A.inner_eps, (float)fmin(1.0, 0.1 * A.tol / T.rel))
+                                      : A.inner_eps;
+                const bool conv = k > 0 ? ch <= eps * mx : mx == 0.f;
                 if (conv || T.inner_count >= A.max_sweeps || !(ch == ch)) {
                     T.inner_done = 1;
                     T.final_idx = (k + 1) & 1;

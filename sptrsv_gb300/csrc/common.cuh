@@ -42,6 +42,7 @@ struct Ctl {
     int inner_count;       // MIXED + JACOBI: sweeps of the current inner solve
     int inner_total;       // MIXED + JACOBI: sweeps over the whole solve
     int x_zero;            // MIXED: x is still the zero start vector (the residual is b)
+    float inner_eps;       // MIXED + JACOBI: change test of the next inner solve, from the last residual
 };
 
 template <typename T> struct Pend;

@@ -331,6 +331,9 @@ __global__ void k_check(int rhs, double* rn2, const double* bn2, Ctl* ctl, doubl
 
 // Conditional graphs: the test at the top of every outer iteration.  Continues (and arms the
 // inner loop) while rel > tol and fewer than max_refine corrections were applied.
+// Relative accuracy asked of a correction: a tenth of what would just reach the tolerance.
+constexpr double kInnerTarget = 0.1;
+
 __global__ void k_check_outer(int rhs, double* rn2, const double* bn2, Ctl* ctl, double tol, int max_refine,
                               cudaGraphConditionalHandle h_outer, cudaGraphConditionalHandle h_inner) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
@@ -348,14 +351,19 @@ __global__ void k_check_outer(int rhs, double* rn2, const double* bn2, Ctl* ctl,
         cudaGraphSetConditional(h_inner, 0);
     } else {
         ctl->steps = step + 1;
+        // inexact correction: x + d has residual ~ rel * (relative error of d), so the next inner
+        // solve only needs kInnerTarget * tol / rel (never tighter than its own floor, below)
+        ctl->inner_eps = (float)fmin(1.0, kInnerTarget * tol / rel);
         cudaGraphSetConditional(h_inner, 1);
     }
 }
 
 // Conditional graphs: after each pair of sweeps.  Stops the inner loop once the largest
-// change is at most eps times the largest |d|, or after max_sweeps sweeps.
-__global__ void k_check_inner(Ctl* ctl, float eps, int max_sweeps, cudaGraphConditionalHandle h_inner) {
+// change is at most max(eps, ctl->inner_eps) times the largest |d|, or after max_sweeps sweeps:
+// eps is the FP32 floor of the sweeps, ctl->inner_eps what the outer residual still asks for.
+__global__ void k_check_inner(Ctl* ctl, float eps_floor, int max_sweeps, cudaGraphConditionalHandle h_inner) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const float eps = fmaxf(eps_floor, ctl->inner_eps);
     const float dmax = __uint_as_float(ctl->dmax_bits), dchg = __uint_as_float(ctl->dchg_bits);
     const int cnt = ctl->inner_count + 2;
     ctl->inner_count = cnt;
