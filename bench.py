@@ -59,7 +59,7 @@ RES_TOL = 1e-12
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=2_000_000)
@@ -114,12 +114,21 @@ class Clocks:
         self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
 
     def start(self):
+        """Starts sampling every 50 ms and returns once the first sample is written (at most 5 s),
+        so that the timed region that follows is covered from its start."""
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=self.f, stderr=subprocess.DEVNULL)
         except OSError:
             self.proc = None
+            return
+        t0 = time.time()
+        while time.time() - t0 < 5.0 and self.proc.poll() is None:
+            self.f.flush()
+            if os.path.getsize(self.f.name) > 0:
+                break
+            time.sleep(0.01)
 
     def stop(self):
         if not self.proc:
@@ -381,9 +390,9 @@ def run_ours(args, dist):
     # warm-up + timed region (chosen form)
     timed_steps(chosen, args.warmup)
     clocks = Clocks(dist.local)
+    clocks.start()
     dist.barrier()
     assert s.sync() == 0
-    clocks.start()
     l0 = s.launches()
     ms = timed_steps(chosen, args.steps)
     l1 = s.launches()
@@ -625,8 +634,8 @@ def run_batch(args, dist):
         raise SystemExit("batched chosen form missed the tolerance")
     run("chosen", args.warmup)
     clocks = Clocks(dist.local)
-    dist.barrier()
     clocks.start()
+    dist.barrier()
     ms, ks = run("chosen", args.steps)
     ck = clocks.stop()
     dist.barrier()
