@@ -273,15 +273,17 @@ def errors_vs_serial(m, b, solutions):
 
 def run_reference_batch(args):
     """The reference's serial solve over the batched mix: each step solves a bounded random
-    sample of the systems (about 10 s) and is projected to the whole mix by nnz x rhs."""
+    sample of the systems (10 s, less when there are more than 12 steps, so that the run stays
+    near two minutes) and is projected to the whole mix by nnz x rhs."""
     from sptrsv_gb300 import gen
     M = gen.mix(count=args.count, seed=2, nmin=1000, nmax=args.nmax)
     for k in range(args.warmup):
         batch_cpu_sample(M, budget_s=2.0, seed=100 + k)
     vals, t_all = [], time.perf_counter()
     cb = None
+    budget = min(10.0, max(0.5, 120.0 / max(1, args.steps)))  # the whole run stays near two minutes
     for k in range(args.steps):
-        cb = batch_cpu_sample(M, budget_s=10.0, seed=k)
+        cb = batch_cpu_sample(M, budget_s=budget, seed=k)
         vals.append(cb["value"])
     el = time.perf_counter() - t_all
     v = float(len(vals) / np.sum(1.0 / np.array(vals)))  # harmonic mean of the projected rates
