@@ -156,6 +156,57 @@ def test_mixed_sweep_layouts(golden, orc, monkeypatch, layout):
             assert elem_err(x, ref) <= MIXED_ELEM_TOL, layout
 
 
+def _tiny_cases():
+    rng = np.random.default_rng(21)
+    out = [("n1", np.array([0, 1]), np.array([0], dtype=np.int32), np.array([2.0]))]
+    for n in (2, 31, 32, 33, 65):
+        m = gen.random_upper(n, 3.0, 0.9, 8, n)
+        out.append((f"rand{n}", m.row_ptr, m.col, m.val))
+    n = 1000  # diagonal only: no off-diagonal anywhere
+    out.append(("diag1000", np.arange(n + 1), np.arange(n, dtype=np.int32), rng.uniform(1.0, 2.0, n)))
+    n = 96  # dense upper triangle: rows far longer than the short-row sweeps take
+    rp = np.concatenate([[0], np.cumsum(np.arange(n, 0, -1))])
+    col = np.concatenate([np.arange(i, n) for i in range(n)]).astype(np.int32)
+    val = rng.uniform(-1.0, 1.0, len(col))
+    for i in range(n):
+        val[rp[i]] = 1.0 + np.abs(val[rp[i] + 1:rp[i + 1]]).sum()
+    out.append(("dense96", rp, col, val))
+    return out
+
+
+@pytest.mark.parametrize("case", _tiny_cases(), ids=lambda c: c[0])
+def test_tiny_and_degenerate_systems(orc, solver, case):
+    """One-row, diagonal-only, warp-boundary sizes and a dense triangle through every FP64
+    schedule, the mixed path and several right-hand sides, against the serial solve."""
+    _, rp, col, val = case
+    n = len(rp) - 1
+    rpu = np.asarray(rp).astype(np.uint64)
+    solver.analyse(rp, col, val)
+    lv, ml = orc.levels(rpu, col)
+    assert solver.info()["max_level"] == ml and np.array_equal(solver.levels(), lv)
+    b = gen.uniform(n + 5, n * 3)
+    ref1 = orc.base_gauss_upper(rpu, col, val, b[:n], 1)
+    for sched, rpw in FP64_SCHEDULES:
+        x = solver.solve(b[:n], schedule=sched, rows_per_warp=rpw)
+        assert elem_err(x, ref1) <= ELEM_TOL, sched
+    x = solver.solve(b[:n], precision="mixed", max_refine=20)
+    assert solver.last_refine()[1] <= RES_TOL
+    assert elem_err(x, ref1) <= MIXED_ELEM_TOL
+    ref3 = orc.base_gauss_upper(rpu, col, val, b, 3)
+    for sched in ("syncfree_warp", "syncfree_csc", "levelset"):
+        x = solver.solve(b, rhs=3, schedule=sched)
+        assert elem_err(x, ref3) <= ELEM_TOL, sched
+
+
+def test_empty_system_is_an_error(solver):
+    with pytest.raises(sp.SptrsvError) as e:
+        solver.analyse(np.array([0]), np.zeros(0, dtype=np.int32), np.zeros(0))
+    assert e.value.status == -2  # SPTRSV_ERR_INVALID_ARG
+    # the handle stays usable
+    solver.analyse(np.array([0, 1]), np.array([0], dtype=np.int32), np.array([4.0]))
+    assert solver.solve(np.array([2.0]))[0] == 0.5
+
+
 def test_device_pointer_api(orc, solver):
     torch = pytest.importorskip("torch")
     m = gen.random_upper(20_000, 8.0, 0.9, 64, 41)
