@@ -10,8 +10,10 @@ Reported (one JSON line on rank 0):
   value        solves/s of the chosen form (FP32 bulk solve + FP64 iterative refinement,
                schedule from the matrix features), inputs resident in HBM, device time of
                each step with CUDA events on the solver's stream, L2 flushed between steps;
-  e2e          the same through the public C ABI with pinned host b / x (H2D + solve + D2H
-               inside the timed region of every step);
+  e2e          the same through the public C ABI with pinned host b / x: every step copies b
+               to the device and brings x back inside its timed region (x is written to the
+               pinned host buffer by the FP64 residual kernels over the C2C link, the converged
+               one last, so no copy follows the solve);
   plain_fp64_syncfree  the plain FP64 sync-free GPU solve on the same system (the baseline the
                chosen form is compared with);
   roofline     the dominant kernel of the chosen form: its algorithmic bytes per launch over

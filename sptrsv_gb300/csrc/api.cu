@@ -556,7 +556,7 @@ bool Handle::cond_eligible(const sptrsv_opts& o, int rhs) const {
     return use_graphs && !profiling && o.precision == SPTRSV_PREC_MIXED && o.inner == SPTRSV_SCHED_JACOBI;
 }
 
-int Handle::build_cond_graph(const sptrsv_opts& o, const double* b, double* x, int rhs, int layout,
+int Handle::build_cond_graph(const sptrsv_opts& o, const double* b, double* x, double* x_out, int rhs, int layout,
                              cudaGraphExec_t* out, int64_t* fixed_kernels) {
     *out = nullptr;
     const bool conv = rhs > 1 && layout == SPTRSV_COL_MAJOR;
@@ -565,6 +565,7 @@ int Handle::build_cond_graph(const sptrsv_opts& o, const double* b, double* x, i
     RefineArgs ra{};
     int rc = refine_args(o, brm, xrm, rhs, &ra);
     if (rc) return rc;
+    ra.x_out = rhs == 1 ? x_out : nullptr;
     int64_t scratch_launches = 0;
     ra.launches = &scratch_launches;
     cudaGraph_t g = nullptr;
@@ -660,6 +661,7 @@ int Handle::solve(const sptrsv_opts* o_in, const double* b, double* x, int rhs, 
     if ((rc = prepare(o, rhs, layout))) return rc;
     last_mixed = o.precision == SPTRSV_PREC_MIXED;
     last_cond = false;
+    last_mirrored = false;
     // profiled solves launch directly: their per-step events are timed from the host stream
     if (!use_graphs || profiling) return enqueue(o, b, x, rhs, layout);
     const bool cond = cond_eligible(o, rhs);
@@ -667,6 +669,7 @@ int Handle::solve(const sptrsv_opts* o_in, const double* b, double* x, int rhs, 
     key.o = o;
     key.b = b;
     key.x = x;
+    key.xo = (cond && rhs == 1) ? x_mirror : nullptr;
     key.rhs = rhs;
     key.layout = layout;
     key.warps = warps_override;
@@ -676,6 +679,7 @@ int Handle::solve(const sptrsv_opts* o_in, const double* b, double* x, int rhs, 
             CUDA_TRY(cudaGraphLaunch(g.exec, st));
             launches += g.kernels;
             last_cond = cond;
+            last_mirrored = key.xo != nullptr;
             cond_fixed_kernels = g.kernels;
             return 0;
         }
@@ -683,7 +687,7 @@ int Handle::solve(const sptrsv_opts* o_in, const double* b, double* x, int rhs, 
     if (cond) {
         cudaGraphExec_t exec = nullptr;
         int64_t fixed = 0;
-        rc = build_cond_graph(o, b, x, rhs, layout, &exec, &fixed);
+        rc = build_cond_graph(o, b, x, key.xo, rhs, layout, &exec, &fixed);
         if (!rc && exec) {
             GraphEntry ge;
             ge.key = key;
@@ -697,11 +701,13 @@ int Handle::solve(const sptrsv_opts* o_in, const double* b, double* x, int rhs, 
             CUDA_TRY(cudaGraphLaunch(exec, st));
             launches += fixed;
             last_cond = true;
+            last_mirrored = key.xo != nullptr;
             cond_fixed_kernels = fixed;
             return 0;
         }
-        // conditional nodes unavailable: fall through to the flat graph
+        // conditional nodes unavailable: fall through to the flat graph (which writes no mirror)
         (void)cudaGetLastError();
+        key.xo = nullptr;
     }
     const int64_t before = launches;
     CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
@@ -1011,7 +1017,30 @@ int sptrsv_solve_host(sptrsv_handle hh, const sptrsv_opts* o, const double* b, d
     if ((rc = h->db.ensure(bytes))) return rc;
     if ((rc = h->dx.ensure(bytes))) return rc;
     CUDA_TRY(cudaMemcpyAsync(h->db.p, b, bytes, cudaMemcpyHostToDevice, h->st));
-    if ((rc = h->solve(o, h->db.as<double>(), h->dx.as<double>(), rhs, layout))) return rc;
+    // Pinned (or registered) host x with one right-hand side: the refinement's FP64 residual
+    // kernels, which read all of x anyway, write it straight to the host over the C2C link, so
+    // the converged x needs no device-to-host copy after the last residual.
+    h->x_mirror = nullptr;
+    if (rhs == 1) {
+        cudaPointerAttributes pa{};
+        if (cudaPointerGetAttributes(&pa, x) == cudaSuccess && pa.type == cudaMemoryTypeHost && pa.devicePointer)
+            h->x_mirror = static_cast<double*>(pa.devicePointer);
+        else
+            (void)cudaGetLastError();
+    }
+    rc = h->solve(o, h->db.as<double>(), h->dx.as<double>(), rhs, layout);
+    h->x_mirror = nullptr;
+    if (rc) return rc;
+    if (h->last_mirrored) {
+        rc = h->sync();
+        // complete when the solve converged after at least one residual of a nonzero x; a zero
+        // right-hand side (x = 0 from the start) or an unconverged solve takes the copy below
+        if (rc == 0 && h->last_steps >= 1) return 0;
+        if (rc != 0 && rc != SPTRSV_ERR_NOT_CONVERGED) return rc;
+        CUDA_TRY(cudaMemcpyAsync(x, h->dx.p, bytes, cudaMemcpyDeviceToHost, h->st));
+        CUDA_TRY(cudaStreamSynchronize(h->st));
+        return rc;
+    }
     CUDA_TRY(cudaMemcpyAsync(x, h->dx.p, bytes, cudaMemcpyDeviceToHost, h->st));
     return h->sync();
 }

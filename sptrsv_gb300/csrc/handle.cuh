@@ -21,6 +21,7 @@ struct GraphKey {
     sptrsv_opts o;
     const double* b;
     double* x;
+    double* xo;  // host mirror of x written by the residual kernels (RefineArgs::x_out), or nullptr
     int rhs;
     int layout;
     int warps;
@@ -30,7 +31,7 @@ struct GraphKey {
                o.rhs_tile == k.o.rhs_tile && o.inner == k.o.inner && o.inner_sweeps == k.o.inner_sweeps &&
                o.max_refine == k.o.max_refine && o.tol == k.o.tol && o.spin_budget_ns == k.o.spin_budget_ns &&
                o.resident_warps == k.o.resident_warps && o.inner_tol_exp == k.o.inner_tol_exp &&
-               b == k.b && x == k.x && rhs == k.rhs && layout == k.layout && warps == k.warps && prof == k.prof;
+               b == k.b && x == k.x && xo == k.xo && rhs == k.rhs && layout == k.layout && warps == k.warps && prof == k.prof;
     }
 };
 
@@ -91,6 +92,8 @@ struct Handle {
     unsigned flush_byte = 1;
     bool last_mixed = false;
     bool last_cond = false;       // the last solve ran the conditional (device-looped) graph
+    double* x_mirror = nullptr;   // set by sptrsv_solve_host around solve(): pinned host x for the residuals
+    bool last_mirrored = false;   // the last solve's residual kernels wrote x_mirror
     int64_t cond_fixed_kernels = 0;
     int last_steps = 0;
     int last_sweeps = 0;
@@ -121,7 +124,7 @@ struct Handle {
     int ensure_offdiag();
     bool cond_eligible(const sptrsv_opts& o, int rhs) const;
     int refine_args(const sptrsv_opts& o, const double* b, double* x, int rhs, RefineArgs* ra);
-    int build_cond_graph(const sptrsv_opts& o, const double* b, double* x, int rhs, int layout,
+    int build_cond_graph(const sptrsv_opts& o, const double* b, double* x, double* x_out, int rhs, int layout,
                          cudaGraphExec_t* out, int64_t* fixed_kernels);
     int resident_warps(const sptrsv_opts& o) const;
     int set_supernodes(int sn, const int* snodes_host);

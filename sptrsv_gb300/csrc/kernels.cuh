@@ -110,6 +110,8 @@ struct RefineArgs {
     const int2* sell;      // SELL: column-major slice entries
     const double* b;   // row-major n x rhs
     double* x;         // row-major n x rhs
+    double* x_out;     // rhs == 1: device-accessible host copy of x that every matrix residual
+                       // rewrites (so the converged x is on the host when the graph ends), or nullptr
     float* r32;        // n x rhs
     float* d32[2];     // n x rhs ping-pong
     double* rn2;       // rhs  (||r_c||^2)

@@ -185,7 +185,8 @@ __global__ void __launch_bounds__(kResWarps * 32) k_residual_tile(int n, const i
                                                                   const double* __restrict__ val,
                                                                   const float* __restrict__ invd,
                                                                   const double* __restrict__ b,
-                                                                  const double* __restrict__ x, float* __restrict__ r32,
+                                                                  const double* __restrict__ x,
+                                                                  double* __restrict__ x_out, float* __restrict__ r32,
                                                                   float* __restrict__ d0, int seed,
                                                                   double* __restrict__ rn2, const Ctl* ctl) {
     __shared__ int s_col[kResWarps][kTileMax];
@@ -229,6 +230,7 @@ __global__ void __launch_bounds__(kResWarps * 32) k_residual_tile(int n, const i
             r32[i] = rf;
             seed_out(seed, d0, i, rf, invd[i]);
             acc = fma(r, r, acc);
+            if (x_out) x_out[i] = x[i];
         }
     }
     acc = warp_sum(acc);
@@ -242,9 +244,11 @@ template <int LPR>
 __global__ void __launch_bounds__(256) k_residual_v(int n, const int* __restrict__ rp, const int* __restrict__ col,
                                                     const double* __restrict__ val, const float* __restrict__ invd,
                                                     const double* __restrict__ b, const double* __restrict__ x,
-                                                    float* __restrict__ r32, float* __restrict__ d0, int seed,
-                                                    double* __restrict__ rn2, const Ctl* ctl) {
+                                                    double* __restrict__ x_out, float* __restrict__ r32,
+                                                    float* __restrict__ d0, int seed, double* __restrict__ rn2,
+                                                    const Ctl* ctl) {
     if (is_done(ctl)) return;
+    if (*(volatile const int*)&ctl->x_zero) x_out = nullptr;  // x is still the zero start vector
     __shared__ double s_acc;
     if (threadIdx.x == 0) s_acc = 0.0;
     __syncthreads();
@@ -266,6 +270,7 @@ __global__ void __launch_bounds__(256) k_residual_v(int n, const int* __restrict
             r32[i] = rf;
             seed_out(seed, d0, i, rf, invd[i]);
             acc = fma(r, r, acc);
+            if (x_out) x_out[i] = x[i];
         }
     }
     acc = warp_sum(acc);
@@ -1180,13 +1185,13 @@ int launch_residual(const RefineArgs& a, bool jacobi_seed, int final_check) {
         static int grid_rt = 0;
         if (!grid_rt) grid_rt = resident_grid((const void*)k_residual_tile, kResWarps * 32, a.sm_count);
         k_residual_tile<<<grid_rt, kResWarps * 32, 0, a.st>>>(a.n, a.rp, a.col, a.val, a.invd32, a.b, a.x,
-                                                                      a.r32, a.d32[0], seed, a.rn2, a.ctl);
+                                                                      a.x_out, a.r32, a.d32[0], seed, a.rn2, a.ctl);
     } else if (a.rhs == 1) {
         switch (lpr_for(a.n, a.nnz)) {
-            case 4: k_residual_v<4><<<grid, 256, 0, a.st>>>(a.n, a.rp, a.col, a.val, a.invd32, a.b, a.x, a.r32, a.d32[0], seed, a.rn2, a.ctl); break;
-            case 8: k_residual_v<8><<<grid, 256, 0, a.st>>>(a.n, a.rp, a.col, a.val, a.invd32, a.b, a.x, a.r32, a.d32[0], seed, a.rn2, a.ctl); break;
-            case 16: k_residual_v<16><<<grid, 256, 0, a.st>>>(a.n, a.rp, a.col, a.val, a.invd32, a.b, a.x, a.r32, a.d32[0], seed, a.rn2, a.ctl); break;
-            default: k_residual_v<32><<<grid, 256, 0, a.st>>>(a.n, a.rp, a.col, a.val, a.invd32, a.b, a.x, a.r32, a.d32[0], seed, a.rn2, a.ctl); break;
+            case 4: k_residual_v<4><<<grid, 256, 0, a.st>>>(a.n, a.rp, a.col, a.val, a.invd32, a.b, a.x, a.x_out, a.r32, a.d32[0], seed, a.rn2, a.ctl); break;
+            case 8: k_residual_v<8><<<grid, 256, 0, a.st>>>(a.n, a.rp, a.col, a.val, a.invd32, a.b, a.x, a.x_out, a.r32, a.d32[0], seed, a.rn2, a.ctl); break;
+            case 16: k_residual_v<16><<<grid, 256, 0, a.st>>>(a.n, a.rp, a.col, a.val, a.invd32, a.b, a.x, a.x_out, a.r32, a.d32[0], seed, a.rn2, a.ctl); break;
+            default: k_residual_v<32><<<grid, 256, 0, a.st>>>(a.n, a.rp, a.col, a.val, a.invd32, a.b, a.x, a.x_out, a.r32, a.d32[0], seed, a.rn2, a.ctl); break;
         }
     } else {
         k_residual_m<<<grid, 256, sizeof(double) * a.rhs, a.st>>>(a.n, a.rhs, a.rp, a.col, a.val, a.invd32, a.b, a.x,

@@ -226,6 +226,70 @@ def test_device_pointer_api(orc, solver):
     assert elem_err(x.cpu().numpy().T.reshape(-1), ref) <= ELEM_TOL
 
 
+def test_host_buffers_pinned_and_pageable(orc):
+    """sptrsv_solve_host with pinned host x: the refinement's residual kernels write x to the host
+    directly (no copy after the solve).  Same solution as the device-pointer solve and the oracle
+    tolerances; a zero right-hand side, an unconverged solve (its status, and the same x as the
+    device path) and pageable numpy buffers (the copy path) behave as before."""
+    L = sp._lib.lib()
+    m = gen.random_upper(50_000, 8.0, 0.9, 64, 43)
+    xs, b = gen.system(m, 44)
+    n, nb = m.n, 8 * m.n
+    rpu = m.row_ptr.astype(np.uint64)
+    ref = orc.base_gauss_upper(rpu, m.col, m.val, b, 1)
+    with sp.Solver(0) as s:
+        s.analyse(m.row_ptr, m.col, m.val)
+        h = s.handle
+        hb, hx, db, dx = (ctypes.c_void_p() for _ in range(4))
+        assert L.sptrsv_host_alloc(h, nb, ctypes.byref(hb)) == 0 and L.sptrsv_host_alloc(h, nb, ctypes.byref(hx)) == 0
+        assert L.sptrsv_device_alloc(h, nb, ctypes.byref(db)) == 0 and L.sptrsv_device_alloc(h, nb, ctypes.byref(dx)) == 0
+        hb_np = np.ctypeslib.as_array(ctypes.cast(hb, ctypes.POINTER(ctypes.c_double)), shape=(n,))
+        hx_np = np.ctypeslib.as_array(ctypes.cast(hx, ctypes.POINTER(ctypes.c_double)), shape=(n,))
+
+        def device_x(o, bb):
+            L.sptrsv_copy_h2d(h, db, bb.ctypes.data, nb)
+            rc = L.sptrsv_solve(h, ctypes.byref(o), db, dx, 1, sp.COL_MAJOR)
+            rc = rc or s.sync()
+            out = np.empty(n)
+            L.sptrsv_copy_d2h(h, out.ctypes.data, dx, nb)
+            assert s.sync() in (0, -10)
+            return rc, out
+
+        try:
+            o = sp.make_opts(precision="mixed", schedule="jacobi")
+            rc_d, x_dev = device_x(o, b)
+            assert rc_d == 0
+            for _ in range(2):  # the second call replays the cached graph
+                hb_np[:] = b
+                hx_np[:] = np.nan
+                assert L.sptrsv_solve_host(h, ctypes.byref(o), hb, hx, 1, sp.COL_MAJOR) == 0
+                x = hx_np.copy()
+                assert s.last_refine()[1] <= RES_TOL
+                assert orc.rel_residual(rpu, m.col, m.val, x, b, 1) <= 2 * RES_TOL
+                assert elem_err(x, ref) <= MIXED_ELEM_TOL
+                assert np.max(np.abs(x - x_dev)) <= 1e-13 * np.max(np.abs(x_dev))
+            # zero right-hand side: converged on x = 0 before any residual of a nonzero x
+            hb_np[:] = 0.0
+            hx_np[:] = np.nan
+            assert L.sptrsv_solve_host(h, ctypes.byref(o), hb, hx, 1, sp.COL_MAJOR) == 0
+            assert np.all(hx_np == 0.0)
+            # unconverged: one correction of a loose inner solve
+            o1 = sp.make_opts(precision="mixed", schedule="jacobi", max_refine=1, inner_tol_exp=1)
+            rc_d, x_dev1 = device_x(o1, b)
+            hb_np[:] = b
+            hx_np[:] = np.nan
+            assert L.sptrsv_solve_host(h, ctypes.byref(o1), hb, hx, 1, sp.COL_MAJOR) == rc_d == -10
+            assert np.array_equal(hx_np, x_dev1)
+        finally:
+            L.sptrsv_host_free(h, hb)
+            L.sptrsv_host_free(h, hx)
+            L.sptrsv_device_free(h, db)
+            L.sptrsv_device_free(h, dx)
+        # pageable numpy buffers take the copy path
+        x = s.solve(b, precision="mixed", schedule="jacobi")
+        assert elem_err(x, ref) <= MIXED_ELEM_TOL
+
+
 # ---------------------------------------------------------------------------------------
 # The reference-signature entry points
 
