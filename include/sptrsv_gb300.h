@@ -56,7 +56,9 @@ enum sptrsv_schedule {
     SPTRSV_SCHED_SYNCFREE_THREAD = 2, /* CSR pull, one lane per row (kernel_full3.cl family) */
     SPTRSV_SCHED_SYNCFREE_CSC = 3,  /* CSC push with per-row in-degree counters (kernel_full.cl family) */
     SPTRSV_SCHED_LEVELSET = 4,      /* persistent kernel, one grid barrier per level */
-    SPTRSV_SCHED_JACOBI = 5,        /* iterative sweeps x <- D^-1 (b - N x); mixed precision only */
+    SPTRSV_SCHED_JACOBI = 5,        /* iterative FP32 sweeps x <- D^-1 (b - N x) inside FP64 refinement; with
+                                       SPTRSV_PREC_FP64 the refinement runs to a relative residual of
+                                       min(tol, 1e-15), the accuracy of the exact FP64 schedules */
     SPTRSV_SCHED_SUPERNODAL = 6,    /* dense supernode blocks on tensor cores */
     SPTRSV_SCHED_SYNCFREE_BLOCK = 7 /* CSR pull, 512-row blocks per CTA with their x in shared memory */
 };

@@ -101,7 +101,7 @@ int Handle::analyse() {
     if ((rc = invd32.ensure(sizeof(float) * (size_t)n))) return rc;
     if ((rc = val32.ensure(sizeof(float) * (size_t)nnz))) return rc;
     if ((rc = levels.ensure(sizeof(int) * (size_t)n))) return rc;
-    if ((rc = stats.ensure(2 * sizeof(unsigned long long)))) return rc;
+    if ((rc = stats.ensure(3 * sizeof(unsigned long long)))) return rc;
     const int sgrid = sm_count * 4;
     k_validate<<<sgrid, 256, 0, st>>>(n, nnz, rp, col, val, in_degree.as<int>(), invd.as<double>(),
                                       invd32.as<float>(), ctl);
@@ -110,16 +110,19 @@ int Handle::analyse() {
     if ((rc = read_ctl(&c))) return rc;
     if (c.status) return c.status;
     k_to_f32<<<sgrid, 256, 0, st>>>((size_t)nnz, val, val32.as<float>());
-    CUDA_TRY(cudaMemsetAsync(stats.p, 0, 2 * sizeof(unsigned long long), st));
-    k_row_stats<<<sgrid, 256, 0, st>>>(n, rp, val, stats.as<unsigned long long>(), stats.as<unsigned long long>() + 1);
+    CUDA_TRY(cudaMemsetAsync(stats.p, 0, 3 * sizeof(unsigned long long), st));
+    k_row_stats<<<sgrid, 256, 0, st>>>(n, rp, col, val, stats.as<unsigned long long>(),
+                                       stats.as<unsigned long long>() + 1,
+                                       reinterpret_cast<double*>(stats.as<unsigned long long>() + 2));
     launches += 2;
     CUDA_TRY(cudaGetLastError());
-    unsigned long long hs[2];
+    unsigned long long hs[3];
     CUDA_TRY(cudaMemcpyAsync(hs, stats.p, sizeof(hs), cudaMemcpyDeviceToHost, st));
     CUDA_TRY(cudaStreamSynchronize(st));
     double mr;
     memcpy(&mr, &hs[0], sizeof(double));
     max_ratio = mr;
+    memcpy(&depth_est, &hs[2], sizeof(double));
     mean_len = (double)nnz / n;
     const double ex2 = (double)hs[1] / n;
     std_len = std::sqrt(std::fmax(0.0, ex2 - mean_len * mean_len));
@@ -210,6 +213,12 @@ sptrsv_opts Handle::resolve(const sptrsv_opts* o, int rhs) const {
     if (r.spin_budget_ns <= 0) r.spin_budget_ns = kDefaultBudgetNs;
     if (r.tol <= 0) r.tol = 1e-12;
     if (r.max_refine <= 0) r.max_refine = 8;
+    // FP64 accuracy through refinement: FP32 Jacobi sweeps with FP64 residuals and updates, run
+    // until the relative residual is at the level of an exact FP64 solve
+    if (r.precision == SPTRSV_PREC_FP64 && r.schedule == SPTRSV_SCHED_JACOBI) {
+        r.precision = SPTRSV_PREC_MIXED;
+        r.tol = std::min(r.tol, kFp64RefineTol);
+    }
     const double width = (double)n / (max_level > 0 ? max_level : 1);
     if (r.schedule == SPTRSV_SCHED_AUTO) {
         if (have_supernodes) {

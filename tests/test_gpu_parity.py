@@ -23,7 +23,8 @@ RES_TOL = 1e-12
 MIXED_ELEM_TOL = 1e-8
 GOLDEN_CASES = ["csr_5_upper", "csr_6_upper", "rand3000", "lap12", "chain500", "snr800"]
 FP64_SCHEDULES = [("syncfree_warp", 1), ("syncfree_warp", 2), ("syncfree_warp", 4), ("syncfree_warp", 8),
-                  ("syncfree_thread", 0), ("syncfree_block", 0), ("syncfree_csc", 0), ("levelset", 0)]
+                  ("syncfree_thread", 0), ("syncfree_block", 0), ("syncfree_csc", 0), ("levelset", 0),
+                  ("jacobi", 0)]  # FP64 accuracy through refinement (FP32 sweeps, FP64 residuals)
 
 
 def _case(g, tag):
@@ -458,6 +459,16 @@ def test_irregular_2m_full(orc, solver):
     assert elem_err(x, ref) <= MIXED_ELEM_TOL
     # property at full size: the solution of U x = U x* is x*
     assert np.max(np.abs(x - xs)) <= 1e-9
+    # FP64 accuracy through refinement, explicitly and through the drop-in (348,506 levels: the
+    # drop-in's cost model takes the refinement here)
+    x = solver.solve(b, schedule="jacobi")
+    assert solver.last_refine()[1] <= 1e-15
+    assert elem_err(x, ref) <= ELEM_TOL
+    xd = np.zeros(m.n)
+    secs = sp.base_gauss_upper(m.n, m.val, m.row_ptr.astype(np.uint64), m.col, xd, b, 1)
+    assert secs > 0 and sp.last_status() == 0
+    assert elem_err(xd, ref) <= ELEM_TOL
+    assert orc.rel_residual(m.row_ptr.astype(np.uint64), m.col, m.val, xd, b, 1) <= RES_TOL
 
 
 @pytest.mark.parametrize("tag", ["csr_6_lower", "lower3000"])
