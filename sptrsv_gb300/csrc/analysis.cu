@@ -53,36 +53,43 @@ __global__ void k_to_f32(size_t count, const double* __restrict__ a, float* __re
 
 // Per-row dominance ratio sum_j |U_ij| / |U_ii| (reduced to its maximum) and the sum of
 // squared row lengths, used to choose schedules.
-// Per-matrix statistics: max_i sum|off| / |diag|, sum of squared row lengths, and the sum over
-// rows of 1 / (distance to the row's nearest dependency), which is about the depth of the DAG when
-// dependencies chain through their nearest columns (the levels themselves take a DAG traversal).
+// Per-matrix statistics: max_i sum|off| / |diag|, sum of squared row lengths, the sum over rows
+// of 1 / (distance to the row's nearest dependency), which is about the depth of the DAG when
+// dependencies chain through their nearest columns (the levels themselves take a DAG traversal),
+// and the number of rows that are not one contiguous column range from the diagonal (zero for a
+// banded factor stored with its explicit zeros: a skyline matrix).
 __global__ void k_row_stats(int n, const int* __restrict__ rp, const int* __restrict__ col,
                             const double* __restrict__ val, unsigned long long* max_ratio_bits,
-                            unsigned long long* sum_len2, double* depth_sum) {
+                            unsigned long long* sum_len2, double* depth_sum, unsigned long long* gapped_rows) {
     double mr = 0.0, dep = 0.0;
-    unsigned long long l2 = 0;
+    unsigned long long l2 = 0, gapped = 0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const int s = rp[i], e = rp[i + 1];
         double off = 0.0;
         int near = n;
+        bool contiguous = true;
         for (int k = s + 1; k < e; ++k) {
             off += fabs(val[k]);
             near = min(near, col[k] - i);
+            contiguous &= col[k] == i + (k - s);
         }
         const double r = off / fabs(val[s]);
         mr = fmax(mr, r);
         if (e > s + 1) dep += 1.0 / (double)near;
+        gapped += contiguous ? 0ull : 1ull;
         l2 += (unsigned long long)(e - s) * (unsigned long long)(e - s);
     }
     for (int o = 16; o > 0; o >>= 1) {
         mr = fmax(mr, __shfl_xor_sync(0xffffffffu, mr, o));
         dep += __shfl_xor_sync(0xffffffffu, dep, o);
         l2 += __shfl_xor_sync(0xffffffffu, l2, o);
+        gapped += __shfl_xor_sync(0xffffffffu, gapped, o);
     }
     if ((threadIdx.x & 31) == 0) {
         atomicMax(max_ratio_bits, (unsigned long long)__double_as_longlong(mr));  // mr >= 0: bit order = value order
         atomicAdd(sum_len2, l2);
         atomicAdd(depth_sum, dep);
+        atomicAdd(gapped_rows, gapped);
     }
 }
 

@@ -85,6 +85,8 @@ void Handle::drop_matrix() {
     have_csc = false;
     have_offdiag = false;
     have_supernodes = false;
+    auto_supernodes = false;
+    skyline = false;
     for (bool& v : tuned_valid) v = false;
     n = nnz = max_level = 0;
     rp = col = nullptr;
@@ -101,7 +103,7 @@ int Handle::analyse() {
     if ((rc = invd32.ensure(sizeof(float) * (size_t)n))) return rc;
     if ((rc = val32.ensure(sizeof(float) * (size_t)nnz))) return rc;
     if ((rc = levels.ensure(sizeof(int) * (size_t)n))) return rc;
-    if ((rc = stats.ensure(3 * sizeof(unsigned long long)))) return rc;
+    if ((rc = stats.ensure(4 * sizeof(unsigned long long)))) return rc;
     const int sgrid = sm_count * 4;
     k_validate<<<sgrid, 256, 0, st>>>(n, nnz, rp, col, val, in_degree.as<int>(), invd.as<double>(),
                                       invd32.as<float>(), ctl);
@@ -110,19 +112,21 @@ int Handle::analyse() {
     if ((rc = read_ctl(&c))) return rc;
     if (c.status) return c.status;
     k_to_f32<<<sgrid, 256, 0, st>>>((size_t)nnz, val, val32.as<float>());
-    CUDA_TRY(cudaMemsetAsync(stats.p, 0, 3 * sizeof(unsigned long long), st));
+    CUDA_TRY(cudaMemsetAsync(stats.p, 0, 4 * sizeof(unsigned long long), st));
     k_row_stats<<<sgrid, 256, 0, st>>>(n, rp, col, val, stats.as<unsigned long long>(),
                                        stats.as<unsigned long long>() + 1,
-                                       reinterpret_cast<double*>(stats.as<unsigned long long>() + 2));
+                                       reinterpret_cast<double*>(stats.as<unsigned long long>() + 2),
+                                       stats.as<unsigned long long>() + 3);
     launches += 2;
     CUDA_TRY(cudaGetLastError());
-    unsigned long long hs[3];
+    unsigned long long hs[4];
     CUDA_TRY(cudaMemcpyAsync(hs, stats.p, sizeof(hs), cudaMemcpyDeviceToHost, st));
     CUDA_TRY(cudaStreamSynchronize(st));
     double mr;
     memcpy(&mr, &hs[0], sizeof(double));
     max_ratio = mr;
     memcpy(&depth_est, &hs[2], sizeof(double));
+    skyline = hs[3] == 0;
     mean_len = (double)nnz / n;
     const double ex2 = (double)hs[1] / n;
     std_len = std::sqrt(std::fmax(0.0, ex2 - mean_len * mean_len));
@@ -221,7 +225,8 @@ sptrsv_opts Handle::resolve(const sptrsv_opts* o, int rhs) const {
     }
     const double width = (double)n / (max_level > 0 ? max_level : 1);
     if (r.schedule == SPTRSV_SCHED_AUTO) {
-        if (have_supernodes) {
+        if (have_supernodes || (r.precision == SPTRSV_PREC_FP64 && dense_skyline())) {
+            // banded / skyline rows without a partition: uniform chunks are built on first use
             r.schedule = SPTRSV_SCHED_SUPERNODAL;
         } else if (r.precision == SPTRSV_PREC_MIXED) {
             r.schedule = SPTRSV_SCHED_JACOBI;
@@ -252,6 +257,15 @@ sptrsv_opts Handle::resolve(const sptrsv_opts* o, int rhs) const {
 
 int Handle::prepare(const sptrsv_opts& o, int rhs, int layout) {
     int rc;
+    if (o.schedule == SPTRSV_SCHED_SUPERNODAL && !have_supernodes && skyline) {
+        // exact FP64 panels over uniform chunks of a skyline matrix (every row contiguous from its
+        // diagonal): 64-row chunks, the panel height of the supernodal kernels
+        std::vector<int> part;
+        for (int a = 0; a < n; a += kAutoChunkRows) part.push_back(a);
+        part.push_back(n);
+        if ((rc = set_supernodes((int)part.size() - 1, part.data()))) return rc;
+        auto_supernodes = true;
+    }
     // a work buffer that grows moves: graphs captured with its old address are dropped
     bool moved = false;
     auto grow = [&](DevBuf& d, size_t bytes) {

@@ -148,7 +148,8 @@ static int solve_host_timed(Handle* h, const sptrsv_opts& o, const double* b, do
 // been computed); the refinement makes about 40 bandwidth-bound sweeps and 4 FP64 residual
 // passes, and needs sweeps that contract (every row strictly dominant).
 static bool refinement_pays(const Handle* h, int rhs) {
-    if (!(h->max_ratio < 1.0) || rhs > 1024) return false;
+    // dense skyline rows go to the exact FP64 panels instead
+    if (!(h->max_ratio < 1.0) || rhs > 1024 || h->dense_skyline()) return false;
     const double depth = h->levels_ready ? (double)h->max_level : h->depth_est;
     const double n = h->n, nnz = h->nnz;
     const double sweep_s = (8.0 * (nnz - n) + 16.0 * n * rhs) / 4.0e12 + 4.0e-6;

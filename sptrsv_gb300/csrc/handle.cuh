@@ -20,6 +20,8 @@ struct DevBuf {
 // Relative residual the FP64 + JACOBI form refines to: an exact FP64 solve of the measured
 // systems lands at 1e-16 - 2e-16.
 constexpr double kFp64RefineTol = 1e-15;
+// Rows per chunk of the partition prepare() builds for a skyline matrix.
+constexpr int kAutoChunkRows = 64;
 
 struct GraphKey {
     sptrsv_opts o;
@@ -70,6 +72,11 @@ struct Handle {
     int max_level = 0;
     double max_ratio = 0.0, mean_len = 0.0, std_len = 0.0;
     double depth_est = 0.0;  // analysis: sum over rows of 1 / (distance to the nearest dependency)
+    bool skyline = false;    // analysis: every row is one contiguous column range from its diagonal
+    bool auto_supernodes = false;  // the supernode partition was built by prepare(), not the caller
+    // FP64 AUTO solves dense skyline matrices (rows of similar length, so the dense panels stay
+    // about the size of the matrix) on exact FP64 panels over uniform chunks
+    bool dense_skyline() const { return skyline && mean_len >= 16.0 && std_len <= 0.5 * mean_len; }
     DevBuf csc_ptr, csc_row, csc_val;
     bool have_csc = false;
     DevBuf offdiag;        // interleaved FP32 off-diagonals for the Jacobi sweeps

@@ -30,7 +30,8 @@ __global__ void k_validate(int n, int nnz, const int* rp, const int* col, const 
                            double* invd, float* invd32, Ctl* ctl);
 __global__ void k_to_f32(size_t count, const double* a, float* b);
 __global__ void k_row_stats(int n, const int* rp, const int* col, const double* val,
-                            unsigned long long* max_ratio_bits, unsigned long long* sum_len2, double* depth_sum);
+                            unsigned long long* max_ratio_bits, unsigned long long* sum_len2, double* depth_sum,
+                            unsigned long long* gapped_rows);
 __global__ void k_levels(int n, const int* rp, const int* col, int* level, Ctl* ctl, int64_t budget);
 __global__ void k_level_hist(int n, const int* level, int* cnt);
 __global__ void k_level_tasks(int max_level, const int* lptr, const int* lrows, const int* rp, int T, int* tasks);

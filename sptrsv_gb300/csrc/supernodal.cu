@@ -294,6 +294,7 @@ __global__ void __launch_bounds__(128) k_sn_solve_bf16x3(SnArgs A, const __nv_bf
 
 int Handle::set_supernodes(int sn, const int* snodes_host) {
     if (!analysed) return SPTRSV_ERR_NO_ANALYSIS;
+    auto_supernodes = false;
     if (sn < 1 || !snodes_host) return SPTRSV_ERR_INVALID_ARG;
     // validate the partition and split wide supernodes (metadata only, O(sn))
     if (snodes_host[0] != 0 || snodes_host[sn] != n) return SPTRSV_ERR_SUPERNODES;

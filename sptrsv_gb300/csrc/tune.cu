@@ -217,7 +217,8 @@ int Handle::features(float* f, int rhs) {
     for (int b = 0; b < 8; ++b) f[k++] = (float)(hist[b] / L);  // level-width histogram (fractions)
     // supernode-width histogram: <=8, <=32, <=128, wider (fractions of rows), and their count
     float sw[4] = {0.f, 0.f, 0.f, 0.f};
-    if (have_supernodes) {
+    const bool user_sn = have_supernodes && !auto_supernodes;  // the caller's partition, not uniform chunks
+    if (user_sn) {
         std::vector<int> ss(sn_count + 1);
         CUDA_TRY(cudaMemcpy(ss.data(), sn_start.p, sizeof(int) * (sn_count + 1), cudaMemcpyDeviceToHost));
         for (int s = 0; s < sn_count; ++s) {
@@ -226,8 +227,8 @@ int Handle::features(float* f, int rhs) {
         }
     }
     for (int b = 0; b < 4; ++b) f[k++] = sw[b];
-    f[k++] = have_supernodes ? (float)std::log2(1.0 + sn_count) : 0.f;
-    f[k++] = have_supernodes ? 1.f : 0.f;
+    f[k++] = user_sn ? (float)std::log2(1.0 + sn_count) : 0.f;
+    f[k++] = user_sn ? 1.f : 0.f;
     f[k++] = (float)std::log2(1.0 + (double)nnz / n * (double)n / L);  // work per level
     f[k++] = (float)std::log2((double)std::max(1, rhs));                 // right-hand sides
     return 0;

@@ -444,6 +444,16 @@ def test_band_laplace_full(orc, solver):
     x = solver.solve(b, precision="mixed")
     assert solver.last_refine()[1] <= RES_TOL
     assert elem_err(x, ref) <= MIXED_ELEM_TOL
+    # FP64 AUTO on this skyline matrix (every row one contiguous band): exact FP64 panels over
+    # uniform 64-row chunks, one and three right-hand sides, and the drop-in
+    x = solver.solve(b)
+    assert elem_err(x, ref) <= ELEM_TOL
+    b3 = gen.uniform(77, m.n * 3)
+    ref3 = orc.base_gauss_upper(m.row_ptr.astype(np.uint64), m.col, m.val, b3, 3)
+    assert elem_err(solver.solve(b3, rhs=3), ref3) <= ELEM_TOL
+    xd = np.zeros(m.n)
+    assert sp.base_gauss_upper(m.n, m.val, m.row_ptr.astype(np.uint64), m.col, xd, b, 1) > 0
+    assert sp.last_status() == 0 and elem_err(xd, ref) <= ELEM_TOL
 
 
 def test_irregular_2m_full(orc, solver):
