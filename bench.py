@@ -352,7 +352,8 @@ def run_ours(args, dist):
     assert s.sync() == 0
 
     chosen = sp.make_opts(precision="mixed", schedule="auto")
-    plain = sp.make_opts(schedule="auto")  # the best plain FP64 sync-free schedule for this matrix
+    # the plain FP64 sync-free baseline: 512-row blocks (the fastest sync-free kernel for one RHS)
+    plain = sp.make_opts(schedule="syncfree_block")
     fp64r = sp.make_opts(schedule="jacobi")  # FP64 accuracy through refinement (residual 1e-15)
 
     def dev_solve(o):
