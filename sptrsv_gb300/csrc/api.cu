@@ -259,7 +259,7 @@ int Handle::prepare(const sptrsv_opts& o, int rhs, int layout) {
     int rc;
     if (o.schedule == SPTRSV_SCHED_SUPERNODAL && !have_supernodes && skyline) {
         // exact FP64 panels over uniform chunks of a skyline matrix (every row contiguous from its
-        // diagonal): 64-row chunks, the panel height of the supernodal kernels
+        // diagonal)
         std::vector<int> part;
         for (int a = 0; a < n; a += kAutoChunkRows) part.push_back(a);
         part.push_back(n);

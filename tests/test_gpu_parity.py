@@ -445,7 +445,7 @@ def test_band_laplace_full(orc, solver):
     assert solver.last_refine()[1] <= RES_TOL
     assert elem_err(x, ref) <= MIXED_ELEM_TOL
     # FP64 AUTO on this skyline matrix (every row one contiguous band): exact FP64 panels over
-    # uniform 64-row chunks, one and three right-hand sides, and the drop-in
+    # uniform 256-row chunks, one and three right-hand sides, and the drop-in
     x = solver.solve(b)
     assert elem_err(x, ref) <= ELEM_TOL
     b3 = gen.uniform(77, m.n * 3)
