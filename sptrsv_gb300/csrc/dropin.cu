@@ -166,6 +166,25 @@ static sptrsv_opts fp64(int schedule) {
     return o;
 }
 
+// The FP64 solve of the serial-substitution entry points (any schedule whose result meets the
+// serial solve's accuracy): for deep DAGs with dominant rows, FP64 accuracy through refinement
+// with the exact AUTO solve if it stalls; otherwise the exact AUTO solve.  *secs: device time of
+// the solves made.
+static int solve_fp64_host(Handle* h, const double* b, double* x, int rhs, double* secs) {
+    *secs = 0.0;
+    int rc;
+    if (refinement_pays(h, rhs)) {
+        sptrsv_opts o = fp64(SPTRSV_SCHED_JACOBI);
+        o.max_refine = 6;
+        rc = solve_host_timed(h, o, b, x, rhs, SPTRSV_COL_MAJOR, secs);
+        if (rc != SPTRSV_ERR_NOT_CONVERGED) return rc;
+    }
+    double exact = 0.0;
+    rc = solve_host_timed(h, fp64(SPTRSV_SCHED_AUTO), b, x, rhs, SPTRSV_COL_MAJOR, &exact);
+    *secs += exact;
+    return rc;
+}
+
 static double gauss_upper(int n, double* val, uint64_t* row_index, int* col, double* x, double* b, int rhs) {
     std::lock_guard<std::mutex> lk(g_mu);
     Handle* h;
@@ -175,21 +194,9 @@ static double gauss_upper(int n, double* val, uint64_t* row_index, int* col, dou
     if ((rc = h->set_matrix_host(n, (int64_t)row_index[n], (const int64_t*)row_index, col, val))) return fail(rc);
     if ((rc = h->analyse())) return fail(rc);
     double secs = 0;
-    if (refinement_pays(h, rhs)) {
-        // deep DAG, dominant rows: FP64 accuracy through refinement, the exact solve if it stalls
-        sptrsv_opts o = fp64(SPTRSV_SCHED_JACOBI);
-        o.max_refine = 6;
-        rc = solve_host_timed(h, o, b, x, rhs, SPTRSV_COL_MAJOR, &secs);
-        if (rc == 0) {
-            set_last_status(0);
-            return secs;
-        }
-        if (rc != SPTRSV_ERR_NOT_CONVERGED) return fail(rc);
-    }
-    double exact = 0;
-    if ((rc = solve_host_timed(h, fp64(SPTRSV_SCHED_AUTO), b, x, rhs, SPTRSV_COL_MAJOR, &exact))) return fail(rc);
+    if ((rc = solve_fp64_host(h, b, x, rhs, &secs))) return fail(rc);
     set_last_status(0);
-    return secs + exact;
+    return secs;
 }
 
 // Lower-triangular CSR (diagonal last in every row) -> the upper-triangular CSR of the same
@@ -232,8 +239,7 @@ static double gauss_lower(int n, double* val, uint64_t* row_index, int* col, dou
     std::vector<double> br(b, b + n), xr(n);
     std::reverse(br.begin(), br.end());
     double secs = 0;
-    if ((rc = solve_host_timed(h, fp64(SPTRSV_SCHED_AUTO), br.data(), xr.data(), 1, SPTRSV_COL_MAJOR, &secs)))
-        return fail(rc);
+    if ((rc = solve_fp64_host(h, br.data(), xr.data(), 1, &secs))) return fail(rc);
     std::reverse_copy(xr.begin(), xr.end(), x);
     set_last_status(0);
     return secs;

@@ -493,6 +493,22 @@ def test_dropin_base_gauss_lower(golden, tag):
     assert elem_err(x, golden[tag + "/lower"]) <= ELEM_TOL
 
 
+def test_dropin_base_gauss_lower_deep(orc):
+    """A deep lower system with dominant rows (the reversal of a 200k-row dominant upper factor,
+    ~60k levels): the drop-in takes FP64 accuracy through refinement on the reversed system."""
+    m = gen.random_upper(200_000, 8.0, 0.9, 64, 17)
+    n, nnz = m.n, m.nnz
+    lrp = (nnz - m.row_ptr[::-1]).astype(np.uint64)
+    lcol = (n - 1 - m.col[::-1]).astype(np.int32)
+    lval = m.val[::-1].copy()
+    b = gen.uniform(18, n)
+    ref = orc.base_gauss_lower(lrp, lcol, lval, b)
+    x = np.zeros(n)
+    assert sp.base_gauss_lower(n, lval.copy(), lrp.copy(), lcol.copy(), x, b.copy()) > 0
+    assert sp.last_status() == 0
+    assert elem_err(x, ref) <= ELEM_TOL
+
+
 def test_dropin_base_gauss_lower_rejects_upper(golden):
     rp = golden["csr_6_upper/row_ptr"].astype(np.uint64)
     col, val = golden["csr_6_upper/col"], golden["csr_6_upper/val"]
