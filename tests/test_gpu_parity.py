@@ -509,6 +509,19 @@ def test_dropin_base_gauss_lower_deep(orc):
     assert elem_err(x, ref) <= ELEM_TOL
 
 
+def test_dropin_base_gauss_upper_deep_multi_rhs(orc):
+    """Three column-major right-hand sides of a deep dominant system through the drop-in (the
+    refinement path with rhs > 1), against the serial solve."""
+    m = gen.random_upper(200_000, 8.0, 0.9, 64, 19)
+    rpu = m.row_ptr.astype(np.uint64)
+    b = gen.uniform(20, m.n * 3)
+    ref = orc.base_gauss_upper(rpu, m.col, m.val, b, 3)
+    x = np.zeros(m.n * 3)
+    assert sp.base_gauss_upper(m.n, m.val, rpu, m.col, x, b, 3) > 0 and sp.last_status() == 0
+    assert elem_err(x, ref) <= ELEM_TOL
+    assert orc.rel_residual(rpu, m.col, m.val, x, b, 3) <= RES_TOL
+
+
 def test_dropin_base_gauss_lower_rejects_upper(golden):
     rp = golden["csr_6_upper/row_ptr"].astype(np.uint64)
     col, val = golden["csr_6_upper/col"], golden["csr_6_upper/val"]
