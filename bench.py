@@ -37,6 +37,8 @@ Other workloads (their own JSON line, same keys where they apply):
   --workload supernodal  the 40^3 nested-dissection factor at 1, 8, 32 and 128 right-hand sides:
                          FP64 supernodal, BF16x3 supernodal + FP64 refinement, plain FP64
                          sync-free, serial CPU.
+  --workload dropin      the reference-signature base_gauss_upper on the 64 x 64 and 256 x 256
+                         grid Laplacian factors and the 2M-row system, against the serial CPU solve.
 """
 import argparse
 import csv
@@ -68,9 +70,10 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=2_000_000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="irregular2m", choices=["irregular2m", "batch", "supernodal"],
+    ap.add_argument("--workload", default="irregular2m", choices=["irregular2m", "batch", "supernodal", "dropin"],
                     help="irregular2m: the 2M-row single solve (default); batch: the 512-system uneven mix; "
-                         "supernodal: the 40^3 nested-dissection factor at 1/8/32/128 right-hand sides")
+                         "supernodal: the 40^3 nested-dissection factor at 1/8/32/128 right-hand sides; "
+                         "dropin: the reference-signature base_gauss_upper on three systems")
     ap.add_argument("--count", type=int, default=512, help="batch: number of systems")
     ap.add_argument("--nmax", type=int, default=200_000, help="batch: largest n")
     return ap.parse_args()
@@ -829,6 +832,53 @@ def run_supernodal(args, dist):
                       "generation_s": t_gen, "rows": rows}), flush=True)
 
 
+def run_dropin(args, dist):
+    """The reference-signature entry point base_gauss_upper (core.h:10) on three systems: the
+    64 x 64 grid Laplacian factor (n = 4,096, the reference's own CPU-runnable case), the
+    256 x 256 one and the 2M-row irregular system.  Per system: the solve time the call returns
+    (device events around the solve, as the reference reports its kernel time), the wall time of
+    the whole call (upload, analysis, solve, copies), the serial CPU solve, and the elementwise
+    error against it."""
+    if dist.rank != 0:
+        return
+    import sptrsv_gb300 as sp
+    from sptrsv_gb300 import gen
+    from oracle import oracle
+    cases = [("band 64x64 grid factor (n=4,096)", lambda: gen.band_laplace_case()),
+             ("band 256x256 grid factor (n=65,536)", lambda: (lambda mm: (mm,) + gen.system(mm, 0))(
+                 gen.laplace2d_cholesky(256))),
+             ("irregular 2M", lambda: gen.irregular_case(args.n))]
+    rows = []
+    for name, make in cases:
+        m, xs, b = make()
+        rpu = m.row_ptr.astype(np.uint64)
+        cpu_s = None
+        for _ in range(3):  # best of three, warm
+            t0 = time.perf_counter()
+            ref = oracle.base_gauss_upper(rpu, m.col, m.val, b, 1)
+            el = time.perf_counter() - t0
+            cpu_s = el if cpu_s is None else min(cpu_s, el)
+        best, wall = None, None
+        x = np.zeros(m.n)
+        for k in range(max(2, min(args.steps, 5)) + 1):
+            x = np.zeros(m.n)
+            t0 = time.perf_counter()
+            secs = sp.base_gauss_upper(m.n, m.val, rpu, m.col, x, b, 1)
+            w = time.perf_counter() - t0
+            if secs < 0:
+                raise SystemExit(f"base_gauss_upper failed on {name}: {secs}")
+            if k > 0:
+                best = secs if best is None else min(best, secs)
+                wall = w if wall is None else min(wall, w)
+        rows.append({"system": name, "n": m.n, "nnz": m.nnz, "solve_ms": 1e3 * best, "call_wall_ms": 1e3 * wall,
+                     "cpu_serial_ms": 1e3 * cpu_s, "solve_speedup_vs_cpu": cpu_s / best,
+                     "max_elem_rel_error": oracle.max_elem_rel_error(ref, x, 1e-12),
+                     "rel_residual": oracle.rel_residual(rpu, m.col, m.val, x, b, 1)})
+    print(json.dumps({"workload": "drop-in base_gauss_upper (core.h:10) against the serial CPU solve",
+                      "cpu": f"{cpu_model()}, 1 thread (oracle restatement of base_gauss_upper)",
+                      "rows": rows}), flush=True)
+
+
 def main():
     args = parse()
     dist = Dist()
@@ -839,6 +889,8 @@ def main():
             run_batch(args, dist)
         elif args.workload == "supernodal":
             run_supernodal(args, dist)
+        elif args.workload == "dropin":
+            run_dropin(args, dist)
         else:
             run_ours(args, dist)
     finally:
