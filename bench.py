@@ -791,8 +791,9 @@ def run_supernodal(args, dist):
         for name, o, reps in (("fp64_supernodal", sp.make_opts(schedule="supernodal"), args.steps),
                               ("mixed_supernodal_bf16x3", sp.make_opts(schedule="supernodal", precision="mixed"),
                                args.steps),
-                              ("plain_fp64_syncfree", sp.make_opts(schedule="syncfree_block" if rhs == 1 else
-                                                                   "syncfree_warp"), 1 if rhs > 1 else 3)):
+                              # the block sync-free kernel, once per column for several RHS (this
+                              # factor's rows are long: faster than the RHS-tiled warp kernel)
+                              ("plain_fp64_syncfree", sp.make_opts(schedule="syncfree_block"), 1 if rhs > 1 else 3)):
             x = np.empty(m.n * rhs)
             best = None
             for k in range(1 + reps):

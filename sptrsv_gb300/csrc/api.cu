@@ -232,9 +232,11 @@ sptrsv_opts Handle::resolve(const sptrsv_opts* o, int rhs) const {
             r.schedule = SPTRSV_SCHED_JACOBI;
         } else {
             // wide, shallow DAGs: one grid barrier per level is cheap; otherwise the block
-            // sync-free kernel for one RHS and the RHS-tiled warp kernel for several
+            // sync-free kernel for one RHS (and, once per column, for several RHS on long rows)
+            // and the RHS-tiled warp kernel for several RHS on short rows
             if (levels_ready && width >= 2048.0 && max_level <= 2000) r.schedule = SPTRSV_SCHED_LEVELSET;
-            else r.schedule = rhs == 1 ? SPTRSV_SCHED_SYNCFREE_BLOCK : SPTRSV_SCHED_SYNCFREE_WARP;
+            else if (rhs == 1 || mean_len >= kBlockPerColumnLen) r.schedule = SPTRSV_SCHED_SYNCFREE_BLOCK;
+            else r.schedule = SPTRSV_SCHED_SYNCFREE_WARP;
         }
     }
     if (r.precision == SPTRSV_PREC_MIXED) {
@@ -307,7 +309,8 @@ int Handle::enqueue(const sptrsv_opts& o, const double* b, double* x, int rhs, i
     int rc;
     const double* brm = b;
     double* xrm = x;
-    const bool conv = rhs > 1 && layout == SPTRSV_COL_MAJOR;
+    const bool percol = block_per_column(o, rhs, layout);
+    const bool conv = rhs > 1 && layout == SPTRSV_COL_MAJOR && !percol;
     prof_n = 0;
     if (profiling) {
         if (!prof0) CUDA_TRY(cudaEventCreate(&prof0));
@@ -353,11 +356,19 @@ int Handle::enqueue(const sptrsv_opts& o, const double* b, double* x, int rhs, i
                 if ((rc = mark(SPTRSV_K_PULL_WARP))) return rc;
                 break;
             case SPTRSV_SCHED_SYNCFREE_BLOCK:
-                if (rhs == 1) {
-                    if ((rc = launch_fill_pending(false, xrm, (size_t)n * rhs, st, &launches))) return rc;
-                    if ((rc = mark(SPTRSV_K_FILL))) return rc;
-                    if ((rc = launch_bsf(false, a))) return rc;
-                    if ((rc = mark(SPTRSV_K_PULL_BLOCK))) return rc;
+                if (rhs == 1 || percol) {
+                    // one column at a time (column-major b / x), each from a fresh row ticket
+                    for (int c = 0; c < rhs; ++c) {
+                        SolveArgs ac = a;
+                        ac.b = brm + (size_t)c * n;
+                        ac.x = xrm + (size_t)c * n;
+                        ac.rhs = 1;
+                        if (c > 0) CUDA_TRY(cudaMemsetAsync(&ctl->ticket, 0, sizeof(ctl->ticket), st));
+                        if ((rc = launch_fill_pending(false, xrm + (size_t)c * n, (size_t)n, st, &launches))) return rc;
+                        if ((rc = mark(SPTRSV_K_FILL))) return rc;
+                        if ((rc = launch_bsf(false, ac))) return rc;
+                        if ((rc = mark(SPTRSV_K_PULL_BLOCK))) return rc;
+                    }
                     break;
                 }
                 if ((rc = launch_fill_pending(false, xrm, (size_t)n * rhs, st, &launches))) return rc;

@@ -20,6 +20,12 @@ struct DevBuf {
 // Relative residual the FP64 + JACOBI form refines to: an exact FP64 solve of the measured
 // systems lands at 1e-16 - 2e-16.
 constexpr double kFp64RefineTol = 1e-15;
+// Mean row length from which FP64 solves of several column-major right-hand sides run the block
+// sync-free kernel once per column rather than the RHS-tiled warp kernel (whose lanes walk a long
+// row's entries one after another): on the 40^3 nested-dissection factor (385 entries per row)
+// 114 ms against 1,558 ms at 8 RHS; on 8.6-entry rows the warp kernel stays 3.5x faster.
+constexpr double kBlockPerColumnLen = 64.0;
+
 // Rows per chunk of the partition prepare() builds for a skyline matrix: the widest chunk the
 // supernodal solve takes.  A banded matrix's chunks form one dependency chain, and G = T^-1 [..]
 // leaves no dependency inside a chunk, so wider chunks mean fewer hops (64 x 64 grid factor:
@@ -80,6 +86,11 @@ struct Handle {
     // FP64 AUTO solves dense skyline matrices (rows of similar length, so the dense panels stay
     // about the size of the matrix) on exact FP64 panels over uniform chunks
     bool dense_skyline() const { return skyline && mean_len >= 16.0 && std_len <= 0.5 * mean_len; }
+    // FP64 block sync-free solve of several column-major right-hand sides, one column at a time
+    bool block_per_column(const sptrsv_opts& o, int rhs, int layout) const {
+        return o.precision == SPTRSV_PREC_FP64 && o.schedule == SPTRSV_SCHED_SYNCFREE_BLOCK && rhs > 1 &&
+               layout == SPTRSV_COL_MAJOR && mean_len >= kBlockPerColumnLen;
+    }
     DevBuf csc_ptr, csc_row, csc_val;
     bool have_csc = false;
     DevBuf offdiag;        // interleaved FP32 off-diagonals for the Jacobi sweeps

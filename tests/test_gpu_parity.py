@@ -101,6 +101,30 @@ def test_fp64_schedules_match_reference(golden, orc, solver, tag, sched, rpw):
     assert orc.rel_residual(rp.astype(np.uint64), col, val, x, bb, rhs_run) <= RES_TOL
 
 
+@pytest.fixture(scope="module")
+def nd16():
+    return gen.laplace3d_nd_cholesky(16, leaf=4)  # n = 4,096, 119 entries per row
+
+
+@pytest.mark.parametrize("rhs", [3, 8])
+@pytest.mark.parametrize("layout", [sp.COL_MAJOR, sp.ROW_MAJOR])
+@pytest.mark.parametrize("sched", ["auto", "syncfree_block"])
+def test_multi_rhs_long_rows(orc, solver, nd16, rhs, layout, sched):
+    """Several right-hand sides of a factor with long rows and no supernode partition: the block
+    sync-free kernel once per column (column-major), the RHS-tiled warp kernel (row-major)."""
+    m = nd16
+    solver.analyse(m.row_ptr, m.col, m.val)
+    b_cm = gen.uniform(31 + rhs, m.n * rhs)
+    ref = orc.base_gauss_upper(m.row_ptr.astype(np.uint64), m.col, m.val, b_cm, rhs)
+    if layout == sp.COL_MAJOR:
+        x = solver.solve(b_cm, rhs=rhs, layout=layout, schedule=sched)
+    else:
+        x_rm = solver.solve(b_cm.reshape(rhs, m.n).T.copy().reshape(-1), rhs=rhs, layout=layout, schedule=sched)
+        x = x_rm.reshape(m.n, rhs).T.reshape(-1)
+    assert elem_err(x, ref) <= ELEM_TOL
+    assert orc.rel_residual(m.row_ptr.astype(np.uint64), m.col, m.val, x, b_cm, rhs) <= RES_TOL
+
+
 @pytest.mark.parametrize("rhs", [2, 5, 8, 33])
 @pytest.mark.parametrize("layout", [sp.COL_MAJOR, sp.ROW_MAJOR])
 @pytest.mark.parametrize("sched", ["syncfree_warp", "syncfree_csc", "levelset"])
