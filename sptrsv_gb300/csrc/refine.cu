@@ -11,19 +11,19 @@
 //   d  ~= U^{-1} r              FP32 inner solve, either
 //                                 JACOBI: d <- D^-1 (r - N d) sweeps over an interleaved
 //                                 (column, FP32 value) copy of the off-diagonals, until the
-//                                 largest change is below 10^-e of the largest |d| (the inner
-//                                 WHILE node) -- fully parallel; it converges for any
-//                                 triangular U because N is nilpotent, and fast when U is
-//                                 diagonally dominant -- or
+//                                 largest change is below max(10^-e, 0.1 tol / rel) of the
+//                                 largest |d| (the inner WHILE node) -- fully parallel; it
+//                                 converges for any triangular U because N is nilpotent, and
+//                                 fast when U is diagonally dominant -- or
 //                                 an exact FP32 sync-free / level-set solve (solve.cu);
 //   x  += d                     FP64 update.
 // x starts at 0, so the first residual is b itself.
 //
-// Row-streaming kernels for short rows use warp tiles of 32 consecutive rows: the warp copies
-// the tile's entries into shared memory with independent coalesced loads (16-byte vectors for
-// the interleaved FP32 copy), then each lane sums its own row sequentially (deterministic).
-// Tiles with more than kTileMax entries read straight from global memory; long-row matrices
-// use the warp-per-row kernels (LPR lanes per row).
+// Short rows: the FP64 residual uses warp tiles of 32 consecutive rows (the warp copies the
+// tile's entries into shared memory with coalesced loads, then each lane sums its own row in
+// order: deterministic; tiles with more than kTileMax entries read straight from global memory);
+// the default Jacobi sweep gives each lane a row of the paired layout (16-byte loads of two
+// entries).  Long-row matrices use the warp-per-row kernels (LPR lanes per row).
 #include "common.cuh"
 #include "kernels.cuh"
 
