@@ -166,6 +166,9 @@ SPTRSV_API int sptrsv_get_levels(sptrsv_handle h, uint64_t* levels);       /* co
 SPTRSV_API int sptrsv_get_in_degree(sptrsv_handle h, int* in_degree);      /* kernel_full.cl:40-52 values */
 SPTRSV_API int sptrsv_get_level_buckets(sptrsv_handle h, int* level_ptr, int* level_rows); /* core.cpp:282-288 */
 SPTRSV_API int sptrsv_get_level_tasks(sptrsv_handle h, int num_threads, int* tasks);      /* core.cpp:289-332 */
+/* CSR -> CSC of U as utils.cpp:128-159 lays it out (column pointer, rows ascending within a column so
+ * the diagonal is last, values), built on the device; host arrays of n+1 / nnz / nnz, any may be NULL. */
+SPTRSV_API int sptrsv_get_csc(sptrsv_handle h, int* col_ptr, int* row_idx, double* val);
 
 /* Solve U X = B with device-resident B and X (rhs columns, layout enum sptrsv_layout),
  * enqueued on the handle's stream.  Returns after the enqueue; the device status is read by
@@ -206,8 +209,10 @@ SPTRSV_API int sptrsv_device_sm_count(sptrsv_handle h);
  * The first call on a device looks up that device's array address (cudaGetSymbolAddress), so
  * make the first call before any stream capture starts.  The matrix is checked first (same
  * statuses as sptrsv_analyse_*).  The call is synchronous: it returns the solve's status after
- * the stream has drained.  All calls share the array and each rewrites it, so calls that
- * overlap on the GPU race: order them on one stream or one host thread. */
+ * the stream has drained.  All calls in a process share the array and each rewrites it: the
+ * library holds one lock for the whole of each call, so calls made from several host threads
+ * run one after another whatever stream they name.  The array keeps the last call's contents;
+ * each call clears what must start at zero. */
 SPTRSV_API int sptrsv_solve_noalloc(int n, int nnz, const int* d_row_ptr, const int* d_col, const double* d_val,
                                     const double* d_b, double* d_x, void* stream);
 

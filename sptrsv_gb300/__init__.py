@@ -238,6 +238,15 @@ class Solver:
         _check(_lib.lib().sptrsv_get_in_degree(self._h, out), "in_degree")
         return out
 
+    def csc(self):
+        """(col_ptr, row_idx, val) of the device CSR -> CSC transpose (utils.cpp:128-159 layout)."""
+        info = self.info()
+        cp = np.zeros(self.n + 1, dtype=np.int32)
+        ri = np.zeros(info["nnz"], dtype=np.int32)
+        cv = np.zeros(info["nnz"], dtype=np.float64)
+        _check(_lib.lib().sptrsv_get_csc(self._h, cp, ri, cv), "csc")
+        return cp, ri, cv
+
     def level_buckets(self):
         ml = self.info()["max_level"]
         ptr = np.zeros(ml + 2, dtype=np.int32)

@@ -89,6 +89,7 @@ C_API = {
     "sptrsv_info": ([c_vp, _c_int_p, _c_int_p, _c_int_p], c_int),
     "sptrsv_get_levels": ([c_vp, u64], c_int),
     "sptrsv_get_in_degree": ([c_vp, i32], c_int),
+    "sptrsv_get_csc": ([c_vp, i32, i32, f64], c_int),
     "sptrsv_get_level_buckets": ([c_vp, i32, i32], c_int),
     "sptrsv_get_level_tasks": ([c_vp, c_int, i32], c_int),
     "sptrsv_solve": ([c_vp, ctypes.POINTER(Opts), c_vp, c_vp, c_int, c_int], c_int),

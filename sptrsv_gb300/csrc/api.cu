@@ -1007,6 +1007,21 @@ int sptrsv_get_in_degree(sptrsv_handle hh, int* in_degree) {
     return 0;
 }
 
+// The device CSC of U (utils.cpp:128-159 layout), built on first need, copied to host arrays
+// of n+1, nnz and nnz entries; any of them may be NULL.
+int sptrsv_get_csc(sptrsv_handle hh, int* col_ptr, int* row_idx, double* val) {
+    H();
+    if (!h->analysed) return SPTRSV_ERR_NO_ANALYSIS;
+    if (int rc0 = h->build_csc()) return rc0;
+    if (col_ptr)
+        CUDA_TRY(cudaMemcpyAsync(col_ptr, h->csc_ptr.p, sizeof(int) * (size_t)(h->n + 1), cudaMemcpyDeviceToHost, h->st));
+    if (row_idx)
+        CUDA_TRY(cudaMemcpyAsync(row_idx, h->csc_row.p, sizeof(int) * (size_t)h->nnz, cudaMemcpyDeviceToHost, h->st));
+    if (val) CUDA_TRY(cudaMemcpyAsync(val, h->csc_val.p, sizeof(double) * (size_t)h->nnz, cudaMemcpyDeviceToHost, h->st));
+    CUDA_TRY(cudaStreamSynchronize(h->st));
+    return 0;
+}
+
 int sptrsv_get_level_buckets(sptrsv_handle hh, int* level_ptr, int* level_rows) {
     H();
     if (!h->analysed) return SPTRSV_ERR_NO_ANALYSIS;

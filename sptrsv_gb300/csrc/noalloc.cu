@@ -13,10 +13,15 @@
 // Host code must not pass `g_noalloc_scratch` itself to a kernel -- on the host that name is
 // only a stand-in, not a device address.  The device address is looked up once per device,
 // with that device current, by cudaGetSymbolAddress on the first call made on that device, so
-// that first call should come before any stream capture begins.  All calls share the one
-// array and it keeps the previous call's contents: each call clears the control block and
-// rewrites the reciprocal diagonal for its rows before the solve, and two calls that overlap
-// on the GPU (different streams or threads without ordering between them) race on it.
+// that first call should come before any stream capture begins (after cudaDeviceReset the
+// cached address is stale, as is every other device object of the library).  All calls share
+// the one array and it keeps the previous call's contents: each call clears the control block
+// and rewrites the reciprocal diagonal for its rows before the solve.  A call runs in two
+// phases on its stream (checks, then the solve), so every call in the process holds one lock
+// from its first enqueue to its return: calls from several host threads run one after another,
+// whatever streams they use.  Work the caller enqueues itself cannot be ordered by that lock,
+// so calls that overlap on the GPU with another use of the array (another process's calls
+// never do: each process has its own copy) must not be made.
 #include <mutex>
 #include "common.cuh"
 #include "kernels.cuh"
@@ -55,9 +60,9 @@ __global__ void k_noalloc_prepare(int n, int nnz, const int* __restrict__ rp, co
 static std::mutex g_noalloc_mu;
 static NoallocScratch* g_noalloc_addr[64];  // device address of the array, per device
 
+// Caller holds g_noalloc_mu.
 static int noalloc_scratch(int device, NoallocScratch** out) {
     if (device < 0 || device >= 64) return SPTRSV_ERR_INVALID_ARG;
-    std::lock_guard<std::mutex> lk(g_noalloc_mu);
     if (!g_noalloc_addr[device]) {
         void* p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
@@ -77,6 +82,8 @@ extern "C" int sptrsv_solve_noalloc(int n, int nnz, const int* d_row_ptr, const 
     if (n > SPTRSV_NOALLOC_MAX_ROWS) return SPTRSV_ERR_TOO_LARGE;
     int device = 0;
     CUDA_TRY(cudaGetDevice(&device));
+    // one call at a time in this process: the checks and the solve both use the shared array
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
     NoallocScratch* s = nullptr;
     int rc = noalloc_scratch(device, &s);
     if (rc) return rc;

@@ -73,7 +73,9 @@ def ref_supernodal(R, tag, rp, col, val, sn, b, rhs, out):
 
 
 def main():
-    refdir = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("SPTRSV_REFERENCE", "/root/reference")
+    refdir = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("SPTRSV_REFERENCE", "")
+    if not refdir:
+        raise SystemExit("usage: make_golden.py REFERENCE_CHECKOUT (or set SPTRSV_REFERENCE)")
     os.environ["SPTRSV_REFERENCE"] = refdir
     oracle.build(force=True)
     R = oracle.ref()

@@ -78,6 +78,28 @@ def test_analysis_bit_exact(golden, orc, solver, tag):
         assert np.array_equal(solver.level_tasks(T), orc.level_tasks(ml, ptr_o, rows_o, rp.astype(np.uint64), T))
 
 
+def _csc_matches_oracle(orc, solver, rp, col, val):
+    """The device CSR -> CSC transpose against utils.cpp:128-159 restated: integer arrays bit for
+    bit, values moved exactly (a permutation, no arithmetic)."""
+    solver.analyse(rp, col, val)
+    cp, ri, cv = solver.csc()
+    cp_o, ri_o, cv_o = orc.transpose(np.asarray(rp, dtype=np.uint64), col, val)
+    assert np.array_equal(cp, cp_o)
+    assert np.array_equal(ri.astype(np.uint64), ri_o)
+    assert np.array_equal(cv.view(np.uint64), cv_o.view(np.uint64))
+
+
+@pytest.mark.parametrize("tag", GOLDEN_CASES)
+def test_device_csc_bit_exact(golden, orc, solver, tag):
+    rp, col, val, _, _ = _case(golden, tag)
+    _csc_matches_oracle(orc, solver, rp, col, val)
+
+
+def test_device_csc_bit_exact_2m(orc, solver):
+    m, _, _ = gen.irregular_case()
+    _csc_matches_oracle(orc, solver, m.row_ptr, m.col, m.val)
+
+
 def test_levels_200k_digest(golden, solver):
     m = gen.random_upper(200_000, 8.0, 0.9, 64, 1)
     solver.analyse(m.row_ptr, m.col, m.val)
