@@ -60,6 +60,9 @@ METRIC = "solves/sec & HBM GB/s: chosen vs plain FP64 sync-free, at rel. resid <
 WORKLOAD = ("irregular-2M: n=2,000,000 upper CSR, Poisson(8) off-diagonals/row, 90% at offset U{1..64}, "
             "10% uniform to the right, FP64, diag=1+sum|off|, b=U x*, seed 1, single RHS")
 RES_TOL = 1e-12
+# the plain FP64 sync-free baseline of the single-system workload: the fastest exact sync-free
+# kernel for one RHS
+PLAIN_SCHEDULE = "syncfree_window"
 
 
 def parse():
@@ -76,6 +79,9 @@ def parse():
                          "dropin: the reference-signature base_gauss_upper on three systems")
     ap.add_argument("--count", type=int, default=512, help="batch: number of systems")
     ap.add_argument("--nmax", type=int, default=200_000, help="batch: largest n")
+    ap.add_argument("--batch-steps", type=int, default=10,
+                    help="default workload: timed steps of the batched mix measured after the 2M-row system")
+    ap.add_argument("--no-batch", action="store_true", help="default workload: skip the nested batched-mix record")
     return ap.parse_args()
 
 
@@ -355,8 +361,7 @@ def run_ours(args, dist):
     assert s.sync() == 0
 
     chosen = sp.make_opts(precision="mixed", schedule="auto")
-    # the plain FP64 sync-free baseline: 512-row blocks (the fastest sync-free kernel for one RHS)
-    plain = sp.make_opts(schedule="syncfree_block")
+    plain = sp.make_opts(schedule=PLAIN_SCHEDULE)
     fp64r = sp.make_opts(schedule="jacobi")  # FP64 accuracy through refinement (residual 1e-15)
 
     def dev_solve(o):
@@ -502,9 +507,15 @@ def run_ours(args, dist):
     L.sptrsv_device_free(h, d_x)
 
     if dist.rank != 0:
+        s.close()
+        if not args.no_batch:
+            batch_record(args, dist, max(1, args.batch_steps), max(3, min(args.warmup, 5)), with_cpu=False)
         return
     ms_step = 1e3 * total_s / args.steps
     fb = fp64_bytes(n, nnz)
+    pipe = fp64_pipe(dist.local)
+    sm_mhz = (ck or {}).get("sm_mhz") or 2070.0
+    levels = int(info["max_level"])
     line = {
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": dist.ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
@@ -522,8 +533,18 @@ def run_ours(args, dist):
         "max_abs_err_vs_xstar": err_xstar,
         "vs_oracle": vs_oracle,
         "plain_fp64_syncfree": {"solves_per_s": plain_sps, "ms_per_solve": 1e3 / plain_sps,
-                                "hbm_gbs": fb * plain_sps / 1e9},
+                                "hbm_gbs": fb * plain_sps / 1e9, "schedule": PLAIN_SCHEDULE,
+                                "ns_per_level": 1e9 / plain_sps / levels},
         "speedup_vs_plain": value / dist.ws / plain_sps,
+        # the single-solve target of >= 40 % of the HBM-bytes roofline, stated over the whole solve
+        # (one FP64 solve's algorithmic bytes per chosen-form solve), and the exact solve's
+        # critical-path bound: one dependent FP64 FMA per level
+        "single_solve_roofline": {"hbm_frac_whole_solve": fb * value / dist.ws / 1e9 / peak, "target": 0.40,
+                                  "met": fb * value / dist.ws / 1e9 / peak >= 0.40,
+                                  "dominant_kernel_frac": achieved / peak},
+        "critical_path": {"levels": levels, "dep_fma_cycles": pipe["dep_fma_cycles"], "sm_mhz": sm_mhz,
+                          "bound_ms_one_fma_per_level": levels * pipe["dep_fma_cycles"] / (sm_mhz * 1e3),
+                          "plain_ms": 1e3 / plain_sps, "fp64_pipe_gfma_per_s": pipe["gfma_per_s"]},
         "fp64_refined": {"solves_per_s": fp64r_sps, "ms_per_solve": 1e3 / fp64r_sps, "rel_residual": fp64r_res,
                          "form": "FP64 accuracy through refinement: FP32 Jacobi sweeps, FP64 residuals to 1e-15"},
         "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes},
@@ -535,6 +556,15 @@ def run_ours(args, dist):
         "clocks": ck,
         "cpu_baseline": cpu,
     }
+    s.close()
+    if not args.no_batch:
+        # the batched mix (the configuration of the >= 2x chosen-vs-plain target), same run
+        rec = batch_record(args, dist, max(1, args.batch_steps), max(3, min(args.warmup, 5)),
+                           with_cpu=not args.no_cpu_baseline)
+        if rec is not None:
+            for k in ("metric", "n_gpus", "higher_is_better", "vs_baseline", "data"):
+                rec.pop(k, None)
+            line["batch"] = rec
     print(json.dumps(line), flush=True)
 
 
@@ -586,22 +616,77 @@ def batch_cpu_sample(M, budget_s=12.0, seed=0):
                       f"projected to all {M.count} by nnz x rhs ({os.uname().machine} host)"}
 
 
-# FP64 FMA rate of a dependency-free FMA loop over every SM of a GB300 (2,070 MHz), the ceiling of
-# the FP64-pipe-bound kernels (the residual, the exact FP64 panels)
-FP64_GFMA_MEASURED = 502.0
+_FP64 = {}
 
 
-def fp64_rate(fma, prof_kind):
+def fp64_pipe(device=0):
+    """The FP64 pipe of this GPU, measured by the library (sptrsv_measure_fp64): G FMA/s of
+    independent FMA chains over every SM (the ceiling of the FP64-pipe-bound kernels: the residual,
+    the exact FP64 panels) and SM cycles per dependent FMA (the floor of one dependency hop of an
+    exact FP64 solve)."""
+    if device not in _FP64:
+        import sptrsv_gb300 as sp
+        g, c = sp.measure_fp64(device)
+        _FP64[device] = {"gfma_per_s": g, "dep_fma_cycles": c, "source": "sptrsv_measure_fp64 in this run"}
+    return _FP64[device]
+
+
+def fp64_rate(fma, prof_kind, device=0):
     """FMAs per launch and the rate of the kind's first launch (every system active), also as a
     fraction of the measured FP64 rate."""
     if not prof_kind:
         return {"fma_per_launch": fma, "gfma_per_s": None}
     g = fma / (prof_kind[2] * 1e-3) / 1e9
-    return {"fma_per_launch": fma, "gfma_per_s": g, "frac_of_measured_fp64": g / FP64_GFMA_MEASURED,
-            "measured_fp64_gfma_per_s": FP64_GFMA_MEASURED}
+    ref = fp64_pipe(device)["gfma_per_s"]
+    return {"fma_per_launch": fma, "gfma_per_s": g, "frac_of_measured_fp64": g / ref,
+            "measured_fp64_gfma_per_s": ref}
 
 
-def run_batch(args, dist):
+def batch_errors_vs_serial(M, mine, B, xs_mode, sched, count=16, seed=7):
+    """Errors of both modes against the reference's serial FP64 solve (the oracle's restatement of
+    core.cpp:18-32) on a seeded sample of `count` of this rank's systems that always holds the
+    largest banded and the largest random system: relative residual ||B - U X||_F / ||B||_F, max
+    elementwise relative error (components below 1e-12 measured against 1e-12) and the
+    term-relative error (against max(|x_i|, (|b_i| + sum_j |U_ij x_j|) / |U_ii|), the size of what
+    component i is summed from).  Maxima over the sample per mode and per schedule kind."""
+    from oracle import oracle
+    idx = np.asarray(mine)
+    kind = M.kind[idx]
+    big = [int(idx[np.flatnonzero(kind == k)[np.argmax(M.n[idx][kind == k])]]) for k in (0, 1) if np.any(kind == k)]
+    rest = [int(v) for v in np.random.default_rng(seed).permutation(idx) if int(v) not in big]
+    pick = big + rest[:max(0, count - len(big))]
+    where = {int(g): k for k, g in enumerate(idx)}
+    parts = {mode: B.split(x) for mode, x in xs_mode.items()}
+    worst = {}
+    per = []
+    for g in pick:
+        m, _, b = M.system(g)
+        r = int(M.rhs[g])
+        rpu = m.row_ptr.astype(np.uint64)
+        col, val = np.ascontiguousarray(m.col), np.ascontiguousarray(m.val)
+        bcm = np.ascontiguousarray(np.asarray(b).reshape(m.n, r).T).reshape(-1)
+        ref = oracle.base_gauss_upper(rpu, col, val, bcm, r)
+        rec = {"system": g, "n": int(m.n), "rhs": r, "kind": "banded" if M.kind[g] == 0 else "random",
+               "schedule": int(sched[where[g]])}
+        for mode, pl in parts.items():
+            xcm = np.ascontiguousarray(np.asarray(pl[where[g]]).T).reshape(-1)
+            e = {"rel_residual": oracle.rel_residual(rpu, col, val, xcm, bcm, r),
+                 "max_elem_rel_error": oracle.max_elem_rel_error(ref, xcm, 1e-12),
+                 "term_rel_error": oracle.term_rel_error(rpu, col, val, ref, xcm, bcm, r)}
+            rec[mode] = e
+            names = {v: k for k, v in __import__("sptrsv_gb300").BATCH_SCHED.items()}
+            key = mode if mode == "plain" else "chosen_" + names.get(int(sched[where[g]]), str(int(sched[where[g]])))
+            w = worst.setdefault(key, {k: 0.0 for k in e})
+            for k, v in e.items():
+                w[k] = max(w[k], v)
+        per.append(rec)
+    return {"oracle": "serial base_gauss_upper (core.cpp:18-32), FP64", "sampled": len(pick),
+            "includes": "the largest banded and the largest random system", "max_by_form": worst, "systems": per}
+
+
+def batch_record(args, dist, steps, warmup, with_cpu=True, sample_errors=True):
+    """Measures the batched mix (the 512-system uneven workload) and returns its JSON record on rank 0
+    (None elsewhere)."""
     import ctypes
     import sptrsv_gb300 as sp
     from sptrsv_gb300 import gen
@@ -646,27 +731,29 @@ def run_batch(args, dist):
         return ms, ks
 
     # correctness of both modes before timing
-    x = np.empty(int(info["x_elems"]))
+    xs_mode = {}
     worst = {}
     for mode in ("plain", "chosen"):
         run(mode, 1)
+        x = np.empty(int(info["x_elems"]))
         L.sptrsv_copy_d2h(h, x.ctypes.data, d_x, nb)
         assert s.sync() == 0
         worst[mode] = float(np.max(np.abs(x - l_xs)))
+        xs_mode[mode] = x
     st = B.stats()
     if np.any(st["status"] != 0) or not np.all(st["rel"][(sched != 0) & (sched != 4)] <= RES_TOL):
         raise SystemExit("batched chosen form missed the tolerance")
-    run("chosen", args.warmup)
+    run("chosen", warmup)
     clocks = Clocks(dist.local)
     clocks.start()
     dist.barrier()
-    ms, ks = run("chosen", args.steps)
+    ms, ks = run("chosen", steps)
     ck = clocks.stop()
     dist.barrier()
     total_s = dist.max(sum(ms) / 1e3)
-    value = args.count * args.steps / total_s  # every system of the mix, over the slowest rank
+    value = args.count * steps / total_s  # every system of the mix, over the slowest rank
     run("plain", 1)
-    psteps = max(2, min(args.steps, 3))
+    psteps = max(2, min(steps, 3))
     pms, _ = run("plain", psteps)
     plain_sps = args.count * psteps / dist.max(sum(pms) / 1e3)
     # e2e: host b -> device, solve, x -> host, per step (pinned host buffers)
@@ -675,14 +762,14 @@ def run_batch(args, dist):
     assert L.sptrsv_host_alloc(h, nb, ctypes.byref(hx)) == 0
     ctypes.memmove(hb, l_b.ctypes.data, nb)
     e2e_ms = []
-    for k in range(args.warmup + args.steps):
+    for k in range(warmup + steps):
         B.timer_begin()
         B.solve_host(hb.value, hx.value, "chosen")
         t = B.timer_end()
         B.sync()
-        if k >= args.warmup:
+        if k >= warmup:
             e2e_ms.append(t)
-    e2e_value = args.count * args.steps / dist.max(sum(e2e_ms) / 1e3)
+    e2e_value = args.count * steps / dist.max(sum(e2e_ms) / 1e3)
     # per-kernel device times: the same solve replayed from the host with events around every kernel
     prof = B.profile(d_b.value, d_x.value, "chosen")
     pplain = B.profile(d_b.value, d_x.value, "plain")
@@ -700,24 +787,34 @@ def run_batch(args, dist):
     dom_bytes = {"residual_f64": res_bytes, "jacobi_sweep": jac_bytes, "panels_f64": p64_bytes}.get(dom)
     dom_first = prof[dom][2]
     cpu = None
-    if dist.rank == 0 and not args.no_cpu_baseline:
+    if dist.rank == 0 and with_cpu:
         try:
             cpu = batch_cpu_sample(M)
         except Exception as e:
             cpu = {"value": None, "unit": "solves/s", "error": str(e)[:200]}
+    errs = None
+    if dist.rank == 0 and sample_errors:
+        try:
+            errs = batch_errors_vs_serial(M, mine, B, xs_mode, sched)
+        except Exception as e:  # reported, never required
+            errs = {"error": str(e)[:200]}
+    del xs_mode
     L.sptrsv_host_free(h, hb)
     L.sptrsv_host_free(h, hx)
     L.sptrsv_device_free(h, d_b)
     L.sptrsv_device_free(h, d_x)
+    B.close()
+    s.close()
     if dist.rank != 0:
-        return
+        M.close()
+        return None
     fb = batch_fp64_bytes(M)
     peak, peak_src = measured_peak()
-    ms_step = 1e3 * total_s / args.steps
+    ms_step = 1e3 * total_s / steps
     counts = {k: int(np.sum(sched == v)) for k, v in sp.BATCH_SCHED.items()}
     line = {
-        "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": dist.ws, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "strong",
+        "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": dist.ws, "steps": steps,
+        "warmup": warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "strong",
         "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
         "config": {"workload": BATCH_WORKLOAD.format(count=args.count, nmax=args.nmax), "systems": args.count,
                    "rows": int(np.sum(M.n)), "nnz": int(np.sum(M.nnz)), "rhs_columns": int(np.sum(M.rhs)),
@@ -746,15 +843,24 @@ def run_batch(args, dist):
                      {"bound": "hbm", "kernel": dom, "achieved": fb / (ms_step * 1e-3) / 1e9, "peak": peak,
                       "unit": "GB/s", "frac": fb / (ms_step * 1e-3) / 1e9 / peak, "peak_source": peak_src,
                       "traffic": None, "algorithmic_bytes_per_launch": fb, "note": "whole solve"}),
-        "fp64_residual": fp64_rate(res_fma, prof.get("residual_f64")),
-        "fp64_panels": dict(fp64_rate(info["g_fma_f64"], prof.get("panels_f64")), g_entries=info["g_entries_f64"]),
+        "fp64_residual": fp64_rate(res_fma, prof.get("residual_f64"), dist.local),
+        "fp64_panels": dict(fp64_rate(info["g_fma_f64"], prof.get("panels_f64"), dist.local),
+                            g_entries=info["g_entries_f64"]),
         "kernel_profile_chosen": {k: {"ms": v[0], "launches": v[1]} for k, v in prof.items()},
         "kernel_profile_plain": {k: {"ms": v[0], "launches": v[1]} for k, v in pplain.items()},
         "gpu_launches": int(sum(ks)),
         "clocks": ck,
         "cpu_baseline": cpu,
+        "vs_oracle": errs,
     }
-    print(json.dumps(line), flush=True)
+    M.close()
+    return line
+
+
+def run_batch(args, dist):
+    line = batch_record(args, dist, args.steps, args.warmup, not args.no_cpu_baseline)
+    if line is not None:
+        print(json.dumps(line), flush=True)
 
 
 # ---------------------------------------------------------------------------------------
@@ -782,18 +888,21 @@ def run_supernodal(args, dist):
     for rhs in (1, 8, 32, 128):
         b = gen.uniform(3 + rhs, m.n * rhs)
         ref = oracle.base_gauss_upper(rpu, m.col, m.val, b, rhs)
+        # two correct FP64 solves differing only in summation order lie this far apart elementwise
+        floor = oracle.max_elem_rel_error(ref, oracle.base_gauss_upper_rev(rpu, m.col, m.val, b, rhs), 1e-12)
         nb = 8 * m.n * rhs
         d_b, d_x = ctypes.c_void_p(), ctypes.c_void_p()
         assert L.sptrsv_device_alloc(h, nb, ctypes.byref(d_b)) == 0
         assert L.sptrsv_device_alloc(h, nb, ctypes.byref(d_x)) == 0
         L.sptrsv_copy_h2d(h, d_b, b.ctypes.data, nb)
-        row = {"rhs": rhs}
+        row = {"rhs": rhs, "reorder_floor_elem_err": floor}
         for name, o, reps in (("fp64_supernodal", sp.make_opts(schedule="supernodal"), args.steps),
                               ("mixed_supernodal_bf16x3", sp.make_opts(schedule="supernodal", precision="mixed"),
                                args.steps),
-                              # the block sync-free kernel, once per column for several RHS (this
-                              # factor's rows are long: faster than the RHS-tiled warp kernel)
-                              ("plain_fp64_syncfree", sp.make_opts(schedule="syncfree_block"), 1 if rhs > 1 else 3)):
+                              # the plain FP64 sync-free kernels once per column (this factor's rows
+                              # are long: faster than the RHS-tiled warp kernel)
+                              ("plain_fp64_syncfree", sp.make_opts(schedule="syncfree_block"), 1 if rhs > 1 else 3),
+                              ("plain_fp64_window", sp.make_opts(schedule="syncfree_window"), 1 if rhs > 1 else 3)):
             x = np.empty(m.n * rhs)
             best = None
             for k in range(1 + reps):
@@ -809,6 +918,7 @@ def run_supernodal(args, dist):
             L.sptrsv_copy_d2h(h, x.ctypes.data, d_x, nb)
             s.sync()
             row[name] = {"ms": best, "elem_err": oracle.max_elem_rel_error(ref, x, 1e-12),
+                         "term_rel_err": oracle.term_rel_error(rpu, m.col, m.val, ref, x, b, rhs),
                          "rel_residual": oracle.rel_residual(rpu, m.col, m.val, x, b, rhs)}
         t0 = time.perf_counter()
         oracle.base_gauss_upper(rpu, m.col, m.val, b, rhs)
@@ -821,14 +931,25 @@ def run_supernodal(args, dist):
         t0 = time.perf_counter()
         oracle.supernodal_blas_upper(m.snodes, pad[0], pad[1], pad[2], b, rhs)
         row["cpu_supernodal_blas_ms"] = 1e3 * (time.perf_counter() - t0)
+        # the same algorithm with its dgemm / dtrsm on numpy's OpenBLAS, every host core
+        oracle.supernodal_blas_upper_openblas(m.snodes, pad[0], pad[1], pad[2], b, 1)
+        t0 = time.perf_counter()
+        if oracle.supernodal_blas_upper_openblas(m.snodes, pad[0], pad[1], pad[2], b, rhs) is not None:
+            row["cpu_supernodal_openblas_ms"] = 1e3 * (time.perf_counter() - t0)
         rows.append(row)
         L.sptrsv_device_free(h, d_b)
         L.sptrsv_device_free(h, d_x)
     info = s.info()
     print(json.dumps({"workload": "supernodal: 7-point 3D Laplacian Cholesky factor, 40^3 grid, nested dissection "
                                   "(8^3 leaves), supernodes <= 400 rows",
-                      "cpu": f"{cpu_model()}, 1 thread (serial, supernodal and BLAS-supernodal restatements of "
-                             "core.cpp; the BLAS-supernodal path's dgemm/dtrsm are plain loops, MKL is not on the host)",
+                      "cpu": f"{cpu_model()}: serial, supernodal and BLAS-supernodal restatements of core.cpp on 1 "
+                             "thread (the last with plain-loop dgemm/dtrsm); 'MKL-supernodal -> OpenBLAS-supernodal': "
+                             "supernodal_blas_upper with its dgemm/dtrsm on numpy's OpenBLAS "
+                             f"({(oracle.cblas64() or ['absent'])[0]}) with its default thread count, "
+                             f"{os.environ.get('OPENBLAS_NUM_THREADS', os.cpu_count())} threads (MKL is not on the host)",
+                      "elementwise": "elem_err: max |x - ref| / max(|ref|, 1e-12); term_rel_err: against "
+                                     "max(|ref_i|, (|b_i| + sum_j |U_ij ref_j|) / |U_ii|); reorder_floor_elem_err: "
+                                     "elem_err of the serial solve summed in reverse order",
                       "n": m.n, "nnz": m.nnz, "supernodes": int(len(m.snodes) - 1), "max_level": info["max_level"],
                       "generation_s": t_gen, "rows": rows}), flush=True)
 

@@ -60,7 +60,9 @@ enum sptrsv_schedule {
                                        SPTRSV_PREC_FP64 the refinement runs to a relative residual of
                                        min(tol, 1e-15), the accuracy of the exact FP64 schedules */
     SPTRSV_SCHED_SUPERNODAL = 6,    /* dense supernode blocks on tensor cores */
-    SPTRSV_SCHED_SYNCFREE_BLOCK = 7 /* CSR pull, 512-row blocks per CTA with their x in shared memory */
+    SPTRSV_SCHED_SYNCFREE_BLOCK = 7, /* CSR pull, 512-row blocks per CTA with their x in shared memory */
+    SPTRSV_SCHED_SYNCFREE_WINDOW = 8 /* CSR pull by one CTA walking 32-row blocks, recent x in a shared-memory
+                                        ring (one RHS; column-major RHS one column at a time) */
 };
 
 enum sptrsv_precision {
@@ -88,7 +90,8 @@ enum sptrsv_kernel_kind {
     SPTRSV_K_AXPY = 11,        /* x += d */
     SPTRSV_K_TRANSPOSE = 12,   /* column-major <-> row-major */
     SPTRSV_K_PULL_BLOCK = 13,  /* sync-free CSR pull, shared-memory blocks */
-    SPTRSV_K_SUPERNODAL = 14   /* supernode panel products (FP64, or BF16x3 tensor cores) */
+    SPTRSV_K_SUPERNODAL = 14,  /* supernode panel products (FP64, or BF16x3 tensor cores) */
+    SPTRSV_K_WINDOW = 15       /* sync-free CSR pull by one CTA over a shared-memory ring */
 };
 
 typedef struct sptrsv_opts {
@@ -194,6 +197,11 @@ SPTRSV_API int sptrsv_timer_end(sptrsv_handle h, float* ms);     /* synchronises
 SPTRSV_API int sptrsv_flush_l2(sptrsv_handle h);                 /* writes 512 MiB of scratch */
 SPTRSV_API int64_t sptrsv_kernel_launches(sptrsv_handle h);      /* kernels this handle has launched */
 SPTRSV_API int sptrsv_device_sm_count(sptrsv_handle h);
+/* No counterpart in the reference: the FP64 pipe of `device`, measured -- fused multiply-adds per
+ * second over every SM (independent chains, CUDA events) and SM cycles per dependent FMA (one
+ * chain, clock64).  The first bounds the FP64 kernels' throughput, the second every dependency
+ * hop of an exact FP64 solve.  Allocates a few bytes of scratch; synchronises the device. */
+SPTRSV_API int sptrsv_measure_fp64(int device, double* gfma_per_s, double* dep_fma_cycles);
 /* Largest n accepted by sptrsv_solve_noalloc (its reciprocal diagonal lives in a fixed array). */
 #define SPTRSV_NOALLOC_MAX_ROWS (1 << 20)
 

@@ -42,6 +42,44 @@ ORC_API void orc_base_gauss_upper(int n, const double* val, const uint64_t* row_
     }
 }
 
+/* NOT a restatement of a reference routine: core.cpp:18-32 with every row sum taken in the
+ * opposite order (largest column first).  Two correct FP64 solves that differ only in summation
+ * order lie this far apart; the tests use it to measure that floor on a given system. */
+ORC_API void orc_base_gauss_upper_rev(int n, const double* val, const uint64_t* row_index, const int* col,
+                                      double* x, const double* b, int rhs) {
+    for (int rh = 0; rh < rhs; ++rh) {
+        const size_t off = (size_t)rh * (size_t)n;
+        for (int ir = n - 1; ir >= 0; --ir) {
+            double sum = 0.0;
+            for (uint64_t j = row_index[ir + 1]; j-- > row_index[ir] + 1;) sum += val[j] * x[(size_t)col[j] + off];
+            x[off + ir] = (b[off + ir] - sum) / val[row_index[ir]];
+        }
+    }
+}
+
+/* Elementwise error measured against the size of what each component is computed from:
+ * max_i |x_i - x_ref_i| / max(|x_ref_i|, (|b_i| + sum_j |U_ij x_ref_j|) / |U_ii|), j over the
+ * off-diagonals of row i, column-major RHS blocks.  Where x_ref_i is small because the row's
+ * terms nearly cancel, rounding in any summation order is relative to the terms, not to
+ * x_ref_i; this denominator follows that with no free constant. */
+ORC_API double orc_term_rel_error(int n, const double* val, const uint64_t* row_index, const int* col,
+                                  const double* x_ref, const double* x, const double* b, int rhs) {
+    double worst = 0.0;
+    for (int rh = 0; rh < rhs; ++rh) {
+        const size_t off = (size_t)rh * (size_t)n;
+        for (int i = 0; i < n; ++i) {
+            double mag = fabs(b[off + i]);
+            for (uint64_t j = row_index[i] + 1; j < row_index[i + 1]; ++j) mag += fabs(val[j] * x_ref[off + col[j]]);
+            mag /= fabs(val[row_index[i]]);
+            const double r = fabs(x_ref[off + i]);
+            const double den = r > mag ? r : mag;
+            const double e = fabs(x[off + i] - x_ref[off + i]) / (den > 1e-300 ? den : 1e-300);
+            if (e > worst) worst = e;
+        }
+    }
+    return worst;
+}
+
 /* core.cpp:4-16  base_gauss_lower: forward substitution for lower-triangular CSR with the
  * diagonal LAST in every row; one right-hand side.  Row 0 divides by val[col[0]] as the
  * reference does (its only entry when col[0] = 0). */
@@ -354,6 +392,41 @@ ORC_API void orc_supernodal_blas_upper(int n, size_t sn, const int* supernodes, 
                 for (int k = r + 1; k < tr; ++k) s -= val[shift + (size_t)r * lda + k] * xs[k];
                 xs[r] = s / val[shift + (size_t)r * lda + r];
             }
+        }
+    }
+    free(B);
+    free(c);
+}
+
+/* core.cpp:164-201  supernodal_blas_upper with its two BLAS calls made through a CBLAS library
+ * loaded at run time (ILP64 interface: 64-bit dimensions, e.g. the OpenBLAS that numpy bundles,
+ * scipy_cblas_dgemm64_ / scipy_cblas_dtrsm64_), so that the CPU baseline times the reference's
+ * algorithm on an optimised multithreaded BLAS where MKL is absent.  Same calls and arguments as
+ * core.cpp:186-195: row-major dgemm (tr_dim x 1 x rec_dim, lda = padded row length, beta = 1 on a
+ * zeroed c) and dtrsm (left, upper, no transpose, non-unit, tr_dim x 1, ldb = 1). */
+typedef void (*orc_dgemm64_fn)(int, int, int, int64_t, int64_t, int64_t, double, const double*, int64_t, const double*,
+                               int64_t, double, double*, int64_t);
+typedef void (*orc_dtrsm64_fn)(int, int, int, int, int, int64_t, int64_t, double, const double*, int64_t, double*,
+                               int64_t);
+ORC_API void orc_supernodal_blas_upper_cblas(int n, size_t sn, const int* supernodes, double* x, const double* val,
+                                             const uint64_t* colidx_pad, const int* rowptr_pad, int rhs, void* dgemm,
+                                             void* dtrsm) {
+    orc_dgemm64_fn gemm = (orc_dgemm64_fn)dgemm;
+    orc_dtrsm64_fn trsm = (orc_dtrsm64_fn)dtrsm;
+    double* B = (double*)calloc((size_t)n, sizeof(double));
+    double* c = (double*)calloc((size_t)n, sizeof(double));
+    for (int rh = 0; rh < rhs; ++rh) {
+        size_t gs = (size_t)rh * n;
+        for (int i = (int)sn - 1; i >= 0; --i) {
+            int tr = supernodes[i + 1] - supernodes[i];
+            int shift = rowptr_pad[supernodes[i]];
+            int lda = (rowptr_pad[supernodes[i + 1]] - rowptr_pad[supernodes[i]]) / tr;
+            int rec = rowptr_pad[supernodes[i] + 1] - rowptr_pad[supernodes[i]] - tr;
+            for (int k = 0; k < rec; ++k) B[k] = x[gs + colidx_pad[shift + tr + k]];
+            gemm(101 /* row-major */, 111, 111, tr, 1, rec, 1.0, val + shift + tr, lda, B, 1, 1.0, c, 1);
+            for (int k = 0; k < tr; ++k) { x[gs + supernodes[i] + k] -= c[k]; c[k] = 0.0; }
+            trsm(101, 141 /* left */, 121 /* upper */, 111, 131 /* non-unit */, tr, 1, 1.0, val + shift, lda,
+                 x + gs + supernodes[i], 1);
         }
     }
     free(B);

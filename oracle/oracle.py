@@ -45,6 +45,9 @@ def lib():
         L = ctypes.CDLL(LIB_PATH)
         L.orc_base_gauss_upper.argtypes = [_c_int, _f64, _u64, _i32, _f64, _f64, _c_int]
         L.orc_base_gauss_upper_new.argtypes = [_c_int, _f64, _u64, _i32, _f64, _f64, _c_int]
+        L.orc_base_gauss_upper_rev.argtypes = [_c_int, _f64, _u64, _i32, _f64, _f64, _c_int]
+        L.orc_term_rel_error.argtypes = [_c_int, _f64, _u64, _i32, _f64, _f64, _f64, _c_int]
+        L.orc_term_rel_error.restype = _c_dbl
         L.orc_base_gauss_lower.argtypes = [_c_int, _f64, _u64, _i32, _f64, _f64]
         L.orc_set_levels.argtypes = [_c_int, _i32, _u64, _u64]
         L.orc_set_levels.restype = _c_int
@@ -60,6 +63,8 @@ def lib():
         L.orc_ccs2ccs_pad.argtypes = [_f64, _i32, _u64, _f64, _u64, _i32, _i32, _c_int]
         L.orc_ccs2ccs_pad.restype = _c_int
         L.orc_supernodal_blas_upper.argtypes = [_c_int, _c_sz, _i32, _f64, _f64, _u64, _i32, _c_int]
+        L.orc_supernodal_blas_upper_cblas.argtypes = [_c_int, _c_sz, _i32, _f64, _f64, _u64, _i32, _c_int,
+                                                      ctypes.c_void_p, ctypes.c_void_p]
         L.orc_rel_error.argtypes = [_c_sz, _f64, _f64]
         L.orc_rel_error.restype = _c_dbl
         L.orc_rel_residual.argtypes = [_c_int, _f64, _u64, _i32, _f64, _f64, _c_int]
@@ -111,6 +116,24 @@ def base_gauss_upper(row_ptr, col, val, b, rhs=1, new=False):
     x = np.zeros(n * rhs)
     (lib().orc_base_gauss_upper_new if new else lib().orc_base_gauss_upper)(n, v, rp, c, x, b, rhs)
     return x
+
+
+def base_gauss_upper_rev(row_ptr, col, val, b, rhs=1):
+    """The serial solve with every row sum in the opposite order (not a reference routine): the
+    distance between it and base_gauss_upper is the reordering floor of a system."""
+    rp, c, v = _csr(row_ptr, col, val)
+    n = len(rp) - 1
+    b = np.ascontiguousarray(b, dtype=np.float64).reshape(-1)
+    x = np.zeros(n * rhs)
+    lib().orc_base_gauss_upper_rev(n, v, rp, c, x, b, rhs)
+    return x
+
+
+def term_rel_error(row_ptr, col, val, x_ref, x, b, rhs=1):
+    """max_i |x_i - x_ref_i| / max(|x_ref_i|, (|b_i| + sum_j |U_ij x_ref_j|) / |U_ii|)."""
+    rp, c, v = _csr(row_ptr, col, val)
+    f = lambda a: np.ascontiguousarray(a, dtype=np.float64).reshape(-1)
+    return lib().orc_term_rel_error(len(rp) - 1, v, rp, c, f(x_ref), f(x), f(b), rhs)
 
 
 def base_gauss_lower(row_ptr, col, val, b):
@@ -220,6 +243,44 @@ def supernodal_blas_upper(supernodes, rowptr_pad, colidx_pad, val_pad, b, rhs=1)
     lib().orc_supernodal_blas_upper(n, len(sn) - 1, sn, x, np.ascontiguousarray(val_pad, dtype=np.float64),
                                     np.ascontiguousarray(colidx_pad, dtype=np.uint64),
                                     np.ascontiguousarray(rowptr_pad, dtype=np.int32), rhs)
+    return x
+
+
+_cblas = None
+
+
+def cblas64():
+    """(library path, dgemm address, dtrsm address) of the ILP64 CBLAS that numpy bundles (its
+    OpenBLAS, symbols scipy_cblas_dgemm64_ / scipy_cblas_dtrsm64_), or None where it is absent."""
+    global _cblas
+    if _cblas is None:
+        import glob
+        _cblas = False
+        d = os.path.join(os.path.dirname(np.__file__), "..", "numpy.libs")
+        for path in sorted(glob.glob(os.path.join(d, "libscipy_openblas64_*.so"))):
+            try:
+                B = ctypes.CDLL(path)
+                g = ctypes.cast(B.scipy_cblas_dgemm64_, ctypes.c_void_p).value
+                t = ctypes.cast(B.scipy_cblas_dtrsm64_, ctypes.c_void_p).value
+                _cblas = (os.path.abspath(path), g, t, B)
+                break
+            except (OSError, AttributeError):
+                continue
+    return _cblas[:3] if _cblas else None
+
+
+def supernodal_blas_upper_openblas(supernodes, rowptr_pad, colidx_pad, val_pad, b, rhs=1):
+    """core.cpp:164-201 with its dgemm / dtrsm on numpy's OpenBLAS (all the threads OpenBLAS is
+    given); None when that library is not present."""
+    cb = cblas64()
+    if cb is None:
+        return None
+    sn = np.ascontiguousarray(supernodes, dtype=np.int32)
+    n = int(sn[-1])
+    x = np.ascontiguousarray(b, dtype=np.float64).reshape(-1).copy()
+    lib().orc_supernodal_blas_upper_cblas(n, len(sn) - 1, sn, x, np.ascontiguousarray(val_pad, dtype=np.float64),
+                                          np.ascontiguousarray(colidx_pad, dtype=np.uint64),
+                                          np.ascontiguousarray(rowptr_pad, dtype=np.int32), rhs, cb[1], cb[2])
     return x
 
 

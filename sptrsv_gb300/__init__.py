@@ -19,7 +19,7 @@ from . import _lib
 from ._lib import Opts
 
 SCHED = {"auto": 0, "syncfree_warp": 1, "syncfree_thread": 2, "syncfree_csc": 3, "levelset": 4, "jacobi": 5,
-         "supernodal": 6, "syncfree_block": 7}
+         "supernodal": 6, "syncfree_block": 7, "syncfree_window": 8}
 PREC = {"fp64": 0, "mixed": 1}
 COL_MAJOR, ROW_MAJOR = 0, 1
 
@@ -62,6 +62,13 @@ def make_opts(schedule="auto", precision="fp64", rows_per_warp=None, rhs_tile=No
 
 N_CANDIDATES = 16
 N_FEATURES = 24
+
+
+def measure_fp64(device=0):
+    """(G FMA/s over every SM, SM cycles per dependent FMA) of the GPU's FP64 pipe, measured."""
+    g, c = ctypes.c_double(), ctypes.c_double()
+    _check(_lib.lib().sptrsv_measure_fp64(int(device), ctypes.byref(g), ctypes.byref(c)), "measure_fp64")
+    return g.value, c.value
 
 
 def candidate(cand_id):

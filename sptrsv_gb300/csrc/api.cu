@@ -134,6 +134,16 @@ int Handle::analyse() {
     return 0;
 }
 
+// Level kernel: 0 = one CTA over a shared-memory ring (window.cu, the default), 1 = warp per row
+// over the whole GPU (SPTRSV_LEVELS_KERNEL=warp), kept for comparison.
+static int levels_kernel() {
+    static int k = [] {
+        const char* e = getenv("SPTRSV_LEVELS_KERNEL");
+        return (e && strcmp(e, "warp") == 0) ? 1 : 0;
+    }();
+    return k;
+}
+
 // Levels (core.cpp:244-270) and level buckets (core.cpp:282-288), computed on first need.
 int Handle::ensure_levels() {
     if (levels_ready) return 0;
@@ -143,9 +153,13 @@ int Handle::ensure_levels() {
     if ((rc = reset_ctl())) return rc;
     const int sgrid = sm_count * 4;
     CUDA_TRY(cudaMemsetAsync(levels.p, 0, sizeof(int) * (size_t)n, st));
-    k_levels<<<sm_count * 2, 256, 0, st>>>(n, rp, col, levels.as<int>(), ctl, kDefaultBudgetNs);
-    ++launches;
-    CUDA_TRY(cudaGetLastError());
+    if (levels_kernel() == 0) {
+        if ((rc = launch_window_levels(n, rp, col, levels.as<int>(), ctl, kDefaultBudgetNs, st, &launches))) return rc;
+    } else {
+        k_levels<<<sm_count * 2, 256, 0, st>>>(n, rp, col, levels.as<int>(), ctl, kDefaultBudgetNs);
+        ++launches;
+        CUDA_TRY(cudaGetLastError());
+    }
     if ((rc = read_ctl(&c))) return rc;
     if (c.status) return c.status;
     max_level = c.max_level;
@@ -200,6 +214,15 @@ int Handle::build_csc() {
     return 0;
 }
 
+// FP64 AUTO with one RHS takes the one-CTA window kernel unless SPTRSV_AUTO_WINDOW=0.
+static bool auto_window() {
+    static bool w = [] {
+        const char* e = getenv("SPTRSV_AUTO_WINDOW");
+        return !(e && strcmp(e, "0") == 0);
+    }();
+    return w;
+}
+
 // Schedule choice from the analysis features (the autotuner overrides it).
 sptrsv_opts Handle::resolve(const sptrsv_opts* o, int rhs) const {
     sptrsv_opts r;
@@ -235,7 +258,8 @@ sptrsv_opts Handle::resolve(const sptrsv_opts* o, int rhs) const {
             // sync-free kernel for one RHS (and, once per column, for several RHS on long rows)
             // and the RHS-tiled warp kernel for several RHS on short rows
             if (levels_ready && width >= 2048.0 && max_level <= 2000) r.schedule = SPTRSV_SCHED_LEVELSET;
-            else if (rhs == 1 || mean_len >= kBlockPerColumnLen) r.schedule = SPTRSV_SCHED_SYNCFREE_BLOCK;
+            else if (rhs == 1) r.schedule = auto_window() ? SPTRSV_SCHED_SYNCFREE_WINDOW : SPTRSV_SCHED_SYNCFREE_BLOCK;
+            else if (mean_len >= kBlockPerColumnLen) r.schedule = SPTRSV_SCHED_SYNCFREE_BLOCK;
             else r.schedule = SPTRSV_SCHED_SYNCFREE_WARP;
         }
     }
@@ -371,6 +395,26 @@ int Handle::enqueue(const sptrsv_opts& o, const double* b, double* x, int rhs, i
                     }
                     break;
                 }
+                if ((rc = launch_fill_pending(false, xrm, (size_t)n * rhs, st, &launches))) return rc;
+                if ((rc = mark(SPTRSV_K_FILL))) return rc;
+                if ((rc = launch_pull_warp(false, a, o.rows_per_warp, o.rhs_tile))) return rc;
+                if ((rc = mark(SPTRSV_K_PULL_WARP))) return rc;
+                break;
+            case SPTRSV_SCHED_SYNCFREE_WINDOW:
+                if (rhs == 1 || percol) {
+                    for (int c = 0; c < rhs; ++c) {
+                        SolveArgs ac = a;
+                        ac.b = brm + (size_t)c * n;
+                        ac.x = xrm + (size_t)c * n;
+                        ac.rhs = 1;
+                        if ((rc = launch_fill_pending(false, xrm + (size_t)c * n, (size_t)n, st, &launches))) return rc;
+                        if ((rc = mark(SPTRSV_K_FILL))) return rc;
+                        if ((rc = launch_window(false, ac))) return rc;
+                        if ((rc = mark(SPTRSV_K_WINDOW))) return rc;
+                    }
+                    break;
+                }
+                // row-major right-hand sides: the RHS-tiled warp kernel
                 if ((rc = launch_fill_pending(false, xrm, (size_t)n * rhs, st, &launches))) return rc;
                 if ((rc = mark(SPTRSV_K_FILL))) return rc;
                 if ((rc = launch_pull_warp(false, a, o.rows_per_warp, o.rhs_tile))) return rc;

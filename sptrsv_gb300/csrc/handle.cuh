@@ -88,8 +88,9 @@ struct Handle {
     bool dense_skyline() const { return skyline && mean_len >= 16.0 && std_len <= 0.5 * mean_len; }
     // FP64 block sync-free solve of several column-major right-hand sides, one column at a time
     bool block_per_column(const sptrsv_opts& o, int rhs, int layout) const {
-        return o.precision == SPTRSV_PREC_FP64 && o.schedule == SPTRSV_SCHED_SYNCFREE_BLOCK && rhs > 1 &&
-               layout == SPTRSV_COL_MAJOR && mean_len >= kBlockPerColumnLen;
+        if (o.precision != SPTRSV_PREC_FP64 || rhs <= 1 || layout != SPTRSV_COL_MAJOR) return false;
+        return o.schedule == SPTRSV_SCHED_SYNCFREE_WINDOW ||
+               (o.schedule == SPTRSV_SCHED_SYNCFREE_BLOCK && mean_len >= kBlockPerColumnLen);
     }
     DevBuf csc_ptr, csc_row, csc_val;
     bool have_csc = false;

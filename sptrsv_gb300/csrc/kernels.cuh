@@ -70,6 +70,12 @@ int launch_bsf(bool f32, const SolveArgs& a);
 int launch_push_csc(const SolveArgs& a, const int* cp, const int* crow, const double* cval, int* indeg_work,
                     double* left_sum);
 int launch_levelset(bool f32, const SolveArgs& a, int max_level, const int* lptr, const int* lrows);
+// window.cu: one CTA walks the rows in 32-row blocks with recent x in a shared-memory ring
+int launch_window(bool f32, const SolveArgs& a);
+int launch_window_levels(int n, const int* rp, const int* col, int* level, Ctl* ctl, int64_t budget, cudaStream_t st,
+                         int64_t* launches);
+int window_warps();
+int window_backoff_ns();
 int launch_transpose(bool to_row_major, const double* src, double* dst, int n, int rhs, cudaStream_t st,
                      int64_t* launches);
 

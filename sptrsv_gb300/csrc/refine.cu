@@ -1331,6 +1331,7 @@ int launch_exact_inner(const RefineArgs& a, int schedule, int rows_per_warp, int
     ++*a.launches;
     if (schedule == SPTRSV_SCHED_SYNCFREE_THREAD && a.rhs == 1) return launch_pull_thread(true, s);
     if (schedule == SPTRSV_SCHED_SYNCFREE_BLOCK && a.rhs == 1) return launch_bsf(true, s);
+    if (schedule == SPTRSV_SCHED_SYNCFREE_WINDOW && a.rhs == 1) return launch_window(true, s);
     return launch_pull_warp(true, s, rows_per_warp, 0);
 }
 

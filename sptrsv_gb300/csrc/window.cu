@@ -1,0 +1,442 @@
+// window.cu -- the sync-free solve (SYNCFREE_WINDOW) and the level analysis by ONE CTA that
+// walks the rows from the bottom of U (row n-1) to the top in 32-row blocks.
+//
+// Why one CTA: a deep DAG (the 2M-row irregular system has 348,506 levels for 2M rows) is bound
+// by the latency of every dependency hop, not by bandwidth.  A hop through L2 (one SM publishes,
+// another polls) costs ~375 ns on this GPU; inside one SM a hop is a shared-memory store and
+// load.  So one CTA solves the whole system, and every recent x lives in a ring of kWinRing rows
+// in shared memory.  One SM still has ample FP64 and load throughput for the work between hops
+// (the 2M system: 15M FMAs, 206 MB of entries).
+//
+// Blocks: block t holds rows [n - 32(t+1), n - 32t) (the last one may be short); lane l of the
+// warp owning block t takes row n - 1 - 32t - l.  Warp w owns blocks w, w + W, w + 2W, ...
+// Every lane walks its CSR row from the right (largest column = solved earliest), consuming each
+// entry whose x is available, in warp lockstep: a round lets every lane consume what is ready,
+// then the warp polls again together (no lane spins alone in divergent code).  x of a column c is
+// read from the ring when c < top(t) + reach, else from global memory.
+//
+// Staging: a block's entries (when they fit kCap entries per buffer), its row pointers,
+// reciprocal diagonal and right-hand side are copied into the warp's shared buffers by cp.async
+// one block ahead (row pointers two blocks ahead, since they size the copy), so no global load of
+// the matrix sits between a dependency arriving and the row finishing.  A block with more
+// entries than the buffer reads them from global memory (L1-cached).
+//
+// Ring protocol (no slot is read while it holds another row's value):
+//   * block t starts only when blocks t-W-1 ... t-2W+1 are done (done flags in shared memory);
+//     by induction every block <= t-W-1 is then done;
+//   * at its start, block t resets the ring slots of block t+W (its warp's next block) to the
+//     pending value.  Their previous rows (block t+W - kWinRing/32) are read through the ring
+//     only by blocks up to (t+W - kWinRing/32) + reach/32 <= t-W-1, all done, and every block
+//     that reads block t+W's rows starts after block t has started;
+//   * reach = kWinRing - 32 (2W + 1) makes both hold; columns at or above top(t) + reach belong
+//     to blocks <= t-W-1 (done) and are read from global x.
+// Forward progress: every wait (a start condition, a pending x) is on a higher block, so the
+// waits form no cycle and all W warps of the one CTA are resident.  Every spin is bounded by
+// the spin budget and the abort flag, as in every other kernel here.  A round in which no lane
+// of the warp made progress may sleep `backoff_ns`, so that waiting warps leave the issue slots
+// of their SM sub-partition to the warps that compute.
+//
+// Arithmetic: the solve accumulates the ready entries right to left; at the first entry it has
+// to wait for, it switches to the scaled form p = (b_i - sum) / U_ii and folds each later term
+// as p = fma(-U_ij / U_ii, x_j, p), so a dependency hop costs one FP64 FMA.  The levels
+// (core.cpp:244-270) take the maximum over the row's columns: level_i = 1 + max_j level_j
+// (1 for a diagonal-only row), with 0 as the pending value, bit-exact.
+#include <type_traits>
+#include "common.cuh"
+#include "kernels.cuh"
+
+namespace sptrsv {
+
+constexpr int kWinRing = 4096;   // rows of x held in shared memory (power of two)
+constexpr int kWinFlags = 64;    // done-flag slots (power of two, multiple of W, >= 2W)
+constexpr int kWinSmemBudget = 200 * 1024;
+
+template <typename T> struct WinVal;
+template <> struct WinVal<double> {
+    static __device__ __forceinline__ double pending() { return Pend<double>::value(); }
+    static __device__ __forceinline__ bool is_pending(double v) { return Pend<double>::is(v); }
+};
+template <> struct WinVal<float> {
+    static __device__ __forceinline__ float pending() { return Pend<float>::value(); }
+    static __device__ __forceinline__ bool is_pending(float v) { return Pend<float>::is(v); }
+};
+template <> struct WinVal<int> {
+    static __device__ __forceinline__ int pending() { return 0; }
+    static __device__ __forceinline__ bool is_pending(int v) { return v == 0; }
+};
+
+// Shared-memory layout: the ring and the done flags, then per warp three row-pointer slots,
+// two reciprocal-diagonal / right-hand-side slots and two entry buffers of kCap entries.
+template <typename T, int W> struct WinLayout {
+    static constexpr bool kLevels = std::is_same<T, int>::value;
+    static constexpr int kRpSlot = 36;  // 33 row pointers, padded to 16 bytes
+    static constexpr size_t kFixed = (size_t)kWinRing * sizeof(T) + kWinFlags * sizeof(int);
+    static constexpr size_t kPerWarpFixed = 3 * kRpSlot * sizeof(int) + (kLevels ? 0 : 2 * 2 * 32 * sizeof(T));
+    static constexpr size_t kPerEntry = 2 * (sizeof(int) + (kLevels ? 0 : sizeof(T)));
+    // entries per buffer: what the budget leaves, a multiple of 32
+    static constexpr int kCap = (int)(((kWinSmemBudget - kFixed) / W - kPerWarpFixed) / kPerEntry) / 32 * 32;
+    static constexpr size_t kPerWarp = kPerWarpFixed + (size_t)kCap * kPerEntry;
+    static constexpr size_t kBytes = kFixed + (size_t)W * kPerWarp;
+    static_assert(kCap >= 64, "staging buffers too small");
+};
+
+__device__ __forceinline__ void cpa4(void* s, const void* g) {
+    const unsigned a = (unsigned)__cvta_generic_to_shared(s);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(a), "l"(g) : "memory");
+}
+__device__ __forceinline__ void cpa8(void* s, const void* g) {
+    const unsigned a = (unsigned)__cvta_generic_to_shared(s);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(a), "l"(g) : "memory");
+}
+template <typename T> __device__ __forceinline__ void cpa(T* s, const T* g) {
+    if constexpr (sizeof(T) == 8) cpa8(s, g);
+    else cpa4(s, g);
+}
+__device__ __forceinline__ void cpa_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cpa_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// Rows [lo, top) of block t.
+__device__ __forceinline__ int win_top(int n, int t) { return n - 32 * t; }
+__device__ __forceinline__ int win_lo(int n, int t) { return max(0, n - 32 * t - 32); }
+
+// One warp's staging buffers.
+template <typename T, int W> struct WinStage {
+    int* rp;   // [3][kRpSlot]
+    T* inv;    // [2][32]
+    T* bb;     // [2][32]
+    int* col;  // [2][kCap]
+    T* val;    // [2][kCap]
+    __device__ WinStage(char* base) {
+        using L = WinLayout<T, W>;
+        rp = (int*)base;
+        char* p = base + 3 * L::kRpSlot * sizeof(int);
+        if constexpr (!L::kLevels) {
+            inv = (T*)p;
+            bb = inv + 64;
+            p += 2 * 2 * 32 * sizeof(T);
+        } else {
+            inv = bb = nullptr;
+        }
+        col = (int*)p;
+        p += 2 * (size_t)L::kCap * sizeof(int);
+        val = L::kLevels ? nullptr : (T*)p;
+    }
+};
+
+// Copy block t's row pointers (rows lo .. top, inclusive) into rp slot `rs`.
+template <typename T, int W>
+__device__ __forceinline__ void win_stage_rp(const WinStage<T, W>& S, int rs, const int* rp, int n, int t, int lane) {
+    const int lo = win_lo(n, t), top = win_top(n, t);
+    int* d = S.rp + rs * WinLayout<T, W>::kRpSlot;
+    for (int q = lane; q <= top - lo; q += 32) cpa4(d + q, rp + lo + q);
+}
+
+// Copy block t's entries (when they fit), reciprocal diagonal and right-hand side into data slot
+// `ds`; its row pointers are already in rp slot `rs`.
+template <typename T, int W>
+__device__ __forceinline__ void win_stage_data(const WinStage<T, W>& S, int rs, int ds, const int* col, const T* val,
+                                               const T* invd, const T* b, int n, int t, int lane) {
+    using L = WinLayout<T, W>;
+    const int lo = win_lo(n, t), top = win_top(n, t);
+    const int* r = S.rp + rs * L::kRpSlot;
+    const int e0 = r[0], cnt = r[top - lo] - e0;
+    if (cnt <= L::kCap) {
+        int* dc = S.col + ds * L::kCap;
+        for (int q = lane; q < cnt; q += 32) cpa4(dc + q, col + e0 + q);
+        if constexpr (!L::kLevels) {
+            T* dv = S.val + ds * L::kCap;
+            for (int q = lane; q < cnt; q += 32) cpa(dv + q, val + e0 + q);
+        }
+    }
+    if constexpr (!L::kLevels) {
+        const int i = top - 1 - lane;
+        if (i >= lo) {
+            cpa(S.inv + ds * 32 + lane, invd + i);
+            cpa(S.bb + ds * 32 + lane, b + i);
+        }
+    }
+}
+
+template <typename T, int W>
+__global__ void __launch_bounds__(W * 32, 1)
+k_window(int n, const int* __restrict__ rp, const int* __restrict__ col, const T* __restrict__ val,
+         const T* __restrict__ invd, const T* __restrict__ b, T* x, Ctl* ctl, int64_t budget, int backoff_ns) {
+    using L = WinLayout<T, W>;
+    constexpr bool kLevels = L::kLevels;
+    constexpr int RM = kWinRing - 1;
+    constexpr int reach = kWinRing - 32 * (2 * W + 1);
+    static_assert(reach >= 32 * (W + 1), "ring too small for W warps");
+    static_assert(kWinFlags % W == 0 && kWinFlags >= 2 * W, "flag slots");
+    if (*(volatile const int*)&ctl->done) return;  // an inner solve after the refinement converged
+    extern __shared__ __align__(16) char win_smem[];
+    T* ring = reinterpret_cast<T*>(win_smem);
+    int* dflag = reinterpret_cast<int*>(win_smem + (size_t)kWinRing * sizeof(T));
+    volatile T* vring = ring;
+    volatile int* vflag = dflag;
+    for (int q = threadIdx.x; q < kWinRing; q += blockDim.x) ring[q] = WinVal<T>::pending();
+    for (int q = threadIdx.x; q < kWinFlags; q += blockDim.x) dflag[q] = -1;
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int nblk = (n + 31) >> 5;
+    const WinStage<T, W> S(win_smem + L::kFixed + (size_t)warp * L::kPerWarp);
+    // prologue: row pointers of the warp's first two blocks, then the first block's data
+    if (warp < nblk) {
+        win_stage_rp<T, W>(S, 0, rp, n, warp, lane);
+        if (warp + W < nblk) win_stage_rp<T, W>(S, 1, rp, n, warp + W, lane);
+        cpa_commit();
+        cpa_wait_all();
+        __syncwarp();
+        win_stage_data<T, W>(S, 0, 0, col, val, invd, b, n, warp, lane);
+        cpa_commit();
+    }
+    __syncthreads();
+
+    int lmax = 0;  // levels: largest level of this lane's rows
+    int j = 0;     // this warp's block count
+    for (int t = warp; t < nblk; t += W, ++j) {
+        // 1. start condition: blocks t-W-1 ... t-2W+1 done (lane q checks block t-W-1-q)
+        {
+            const int tt = t - W - 1 - lane;
+            bool ready = lane >= W - 1 || tt < 0 || vflag[tt & (kWinFlags - 1)] >= tt;
+            if (!__all_sync(0xffffffffu, ready)) {
+                const uint64_t t0 = gtimer();
+                unsigned it = 0;
+                bool fail = false;
+                while (!__all_sync(0xffffffffu, ready || fail)) {
+                    __nanosleep(32);
+                    if (!ready) ready = vflag[tt & (kWinFlags - 1)] >= tt;
+                    if ((++it & 63u) == 0) {
+                        if (aborted(ctl)) fail = true;
+                        else if ((int64_t)(gtimer() - t0) > budget) {
+                            record_error(ctl, SPTRSV_ERR_TIMEOUT);
+                            fail = true;
+                        }
+                    }
+                }
+                if (__any_sync(0xffffffffu, fail)) {
+            cpa_wait_all();  // the warp's own copies in flight end before it returns
+            return;
+        }
+            }
+            __threadfence_block();
+        }
+        // 2. this block's staged data (copied one block ago) is complete
+        cpa_wait_all();
+        __syncwarp();
+        const int rs = j % 3, ds = j & 1;
+        // 3. stage ahead: row pointers of block t+2W, data of block t+W; reset block t+W's ring slots
+        if (t + 2 * W < nblk) win_stage_rp<T, W>(S, (j + 2) % 3, rp, n, t + 2 * W, lane);
+        if (t + W < nblk) win_stage_data<T, W>(S, (j + 1) % 3, (j + 1) & 1, col, val, invd, b, n, t + W, lane);
+        cpa_commit();
+        const int top = win_top(n, t), lo = win_lo(n, t);
+        if (t + W < nblk) {
+            const int r2 = top - 32 * W - 1 - lane;
+            if (r2 >= 0) vring[r2 & RM] = WinVal<T>::pending();
+        }
+        // 4. the rows of block t
+        const int* rS = S.rp + rs * L::kRpSlot;
+        const int e0 = rS[0];
+        const bool staged = rS[top - lo] - e0 <= L::kCap;
+        const int* colS = S.col + ds * L::kCap;
+        const T* valS = kLevels ? nullptr : S.val + ds * L::kCap;
+        auto ecol = [&](int k) -> int { return staged ? colS[k - e0] : __ldg(col + k); };
+        auto eval = [&](int k) -> T {
+            if constexpr (kLevels) return T(0);
+            else return staged ? valS[k - e0] : __ldg(val + k);
+        };
+        const int i = top - 1 - lane;
+        const int far = top + reach;
+        bool done = i < lo;
+        int s = 0, k = 0, c = 0;
+        T v = T(0), acc = T(0), di = T(0), bd = T(0), vs = T(0), p = T(0);
+        bool scaled = false;
+        if (!done) {
+            s = rS[i - lo];
+            k = rS[i - lo + 1] - 1;
+            if constexpr (!kLevels) {
+                di = S.inv[ds * 32 + lane];
+                bd = S.bb[ds * 32 + lane] * di;
+            }
+            if (k > s) {
+                c = ecol(k);
+                v = eval(k);
+            }
+            // far columns (blocks <= t-W-1, all done) from global x, four loads in flight
+            while (k > s && c >= far) {
+                int cq[4];
+                T vq[4], xq[4];
+                bool use[4];
+                cq[0] = c;
+                vq[0] = v;
+                use[0] = true;
+#pragma unroll
+                for (int q = 1; q < 4; ++q) {
+                    const int kq = k - q;
+                    use[q] = use[q - 1] && kq > s;
+                    cq[q] = use[q] ? ecol(kq) : 0;
+                    use[q] = use[q] && cq[q] >= far;
+                    vq[q] = use[q] ? eval(kq) : T(0);
+                }
+#pragma unroll
+                for (int q = 0; q < 4; ++q) xq[q] = use[q] ? ld_relaxed(x + cq[q]) : T(0);
+                bool bad = false;
+#pragma unroll
+                for (int q = 0; q < 4; ++q) bad |= use[q] && WinVal<T>::is_pending(xq[q]);
+                if (bad) break;  // not expected; the rounds below poll for it
+                int used = 0;
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    if (use[q]) {
+                        if constexpr (kLevels) acc = max(acc, xq[q]);
+                        else acc = fma(vq[q], xq[q], acc);
+                        ++used;
+                    }
+                }
+                k -= used;
+                if (k > s) {
+                    c = ecol(k);
+                    v = eval(k);
+                }
+            }
+        }
+        // the rest in warp lockstep rounds
+        const uint64_t t0 = gtimer();
+        unsigned it = 0;
+        bool fail = false;
+        for (;;) {
+            bool prog = false;
+            if (!done) {
+                while (k > s) {
+                    const T xv = c >= far ? ld_relaxed(x + c) : vring[c & RM];
+                    if (WinVal<T>::is_pending(xv)) {
+                        if constexpr (!kLevels) {
+                            if (!scaled) {  // from here on one FMA per term
+                                p = fma(-acc, di, bd);
+                                vs = -v * di;
+                                scaled = true;
+                            }
+                        }
+                        break;
+                    }
+                    prog = true;
+                    if constexpr (kLevels) {
+                        acc = max(acc, xv);
+                    } else {
+                        if (scaled) p = fma(vs, xv, p);
+                        else acc = fma(v, xv, acc);
+                    }
+                    if (--k > s) {
+                        c = ecol(k);
+                        v = eval(k);
+                        if constexpr (!kLevels) {
+                            if (scaled) vs = -v * di;
+                        }
+                    }
+                }
+                if (k <= s) {
+                    T xi;
+                    if constexpr (kLevels) {
+                        xi = 1 + acc;
+                        lmax = max(lmax, xi);
+                    } else {
+                        xi = Pend<T>::fix(scaled ? p : fma(-acc, di, bd));
+                    }
+                    vring[i & RM] = xi;
+                    st_relaxed(x + i, xi);
+                    done = true;
+                    prog = true;
+                }
+            }
+            if (__all_sync(0xffffffffu, done || fail)) break;
+            if (backoff_ns > 0 && !__any_sync(0xffffffffu, prog)) __nanosleep(backoff_ns);
+            // the budget is checked at round 31 of a block (a 32-row chain takes 32 rounds) and
+            // every 256 rounds after
+            if ((++it & 255u) == 31u) {
+                if (aborted(ctl)) fail = true;
+                else if ((int64_t)(gtimer() - t0) > budget) {
+                    record_error(ctl, SPTRSV_ERR_TIMEOUT);
+                    fail = true;
+                }
+            }
+        }
+        if (__any_sync(0xffffffffu, fail)) {
+            cpa_wait_all();  // the warp's own copies in flight end before it returns
+            return;
+        }
+        // 5. block t done: its ring stores and the reset of block t+W's slots before the flag
+        __threadfence_block();
+        __syncwarp();
+        if (lane == 0) vflag[t & (kWinFlags - 1)] = t;
+    }
+    cpa_wait_all();  // no copy left in flight when the warp exits
+    if constexpr (kLevels) {
+        for (int o = 16; o > 0; o >>= 1) lmax = max(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
+        if (lane == 0 && lmax > 0) atomicMax(&ctl->max_level, lmax);
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+template <typename T, int W>
+static int window_launch(int n, const int* rp, const int* col, const T* val, const T* invd, const T* b, T* x,
+                         Ctl* ctl, int64_t budget, int backoff_ns, cudaStream_t st, int64_t* launches) {
+    using L = WinLayout<T, W>;
+    static bool configured[64] = {};
+    int dev = 0;
+    CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return SPTRSV_ERR_INVALID_ARG;
+    if (!configured[dev]) {
+        CUDA_TRY(cudaFuncSetAttribute(k_window<T, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L::kBytes));
+        configured[dev] = true;
+    }
+    k_window<T, W><<<1, W * 32, L::kBytes, st>>>(n, rp, col, val, invd, b, x, ctl, budget, backoff_ns);
+    ++*launches;
+    CUDA_TRY(cudaGetLastError());
+    return 0;
+}
+
+template <typename T>
+static int window_dispatch(int n, const int* rp, const int* col, const T* val, const T* invd, const T* b, T* x,
+                           Ctl* ctl, int64_t budget, cudaStream_t st, int64_t* launches) {
+    const int bo = window_backoff_ns();
+    switch (window_warps()) {
+        case 2: return window_launch<T, 2>(n, rp, col, val, invd, b, x, ctl, budget, bo, st, launches);
+        case 4: return window_launch<T, 4>(n, rp, col, val, invd, b, x, ctl, budget, bo, st, launches);
+        case 16: return window_launch<T, 16>(n, rp, col, val, invd, b, x, ctl, budget, bo, st, launches);
+        default: return window_launch<T, 8>(n, rp, col, val, invd, b, x, ctl, budget, bo, st, launches);
+    }
+}
+
+// Warps of the window CTA (SPTRSV_WINDOW_WARPS = 2, 4, 8 or 16) and the sleep of a round that made
+// no progress (SPTRSV_WINDOW_BACKOFF_NS, 0 = poll without sleeping).
+int window_warps() {
+    static int w = [] {
+        const char* e = getenv("SPTRSV_WINDOW_WARPS");
+        const int v = e ? atoi(e) : 8;
+        return (v == 2 || v == 4 || v == 8 || v == 16) ? v : 8;
+    }();
+    return w;
+}
+int window_backoff_ns() {
+    static int b = [] {
+        const char* e = getenv("SPTRSV_WINDOW_BACKOFF_NS");
+        const int v = e ? atoi(e) : 0;
+        return v < 0 ? 0 : (v > 1000 ? 1000 : v);
+    }();
+    return b;
+}
+
+int launch_window(bool f32, const SolveArgs& a) {
+    if (a.rhs != 1) return SPTRSV_ERR_UNSUPPORTED;
+    if (f32)
+        return window_dispatch<float>(a.n, a.rp, a.col, (const float*)a.val, (const float*)a.invd, (const float*)a.b,
+                                      (float*)a.x, a.ctl, a.budget, a.st, a.launches);
+    return window_dispatch<double>(a.n, a.rp, a.col, (const double*)a.val, (const double*)a.invd,
+                                   (const double*)a.b, (double*)a.x, a.ctl, a.budget, a.st, a.launches);
+}
+
+int launch_window_levels(int n, const int* rp, const int* col, int* level, Ctl* ctl, int64_t budget, cudaStream_t st,
+                         int64_t* launches) {
+    return window_dispatch<int>(n, rp, col, nullptr, nullptr, nullptr, level, ctl, budget, st, launches);
+}
+
+}  // namespace sptrsv

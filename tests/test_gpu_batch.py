@@ -279,3 +279,36 @@ def test_new_handles_report_no_status_after_batches_free_memory(mixsys):
     for _ in range(8):
         with sp.Solver(0) as s:
             assert s.sync() == 0
+
+
+def test_large_mix_up_to_200k(orc):
+    """Systems at the batched workload's sizes: 16 from the mix generator (n log-uniform in [1k,
+    200k], 1-16 RHS) plus the largest of each kind at 16 RHS (the 447 x 447 grid factor, n =
+    199,809, and a 200,000-row random dominant system), in both modes against the serial oracle.
+    FP64 systems also meet a term-relative bound of 1e-12 (the error against the size of the terms
+    a component is summed from, oracle.term_rel_error)."""
+    M = gen.mix(count=16, seed=21, nmin=1000, nmax=200_000, rhs_max=16)
+    items = _from_mix(M)
+    M.close()
+    rng = np.random.default_rng(22)
+    band = gen.laplace2d_cholesky(447)
+    items.append((band, 16, rng.uniform(-1, 1, band.n * 16)))
+    rnd = gen.random_upper(200_000, 16.0, 0.9, 64, 23)
+    items.append((rnd, 16, rng.uniform(-1, 1, rnd.n * 16)))
+    S = Systems(orc, items)
+    with S.batch() as B:
+        for mode in ("plain", "chosen"):
+            x = B.solve(S.b, mode=mode)
+            mixed = [False] * B.count if mode == "plain" else [int(v) not in (0, 4) for v in B.schedule]
+            if mode == "chosen":
+                st = B.stats()
+                assert np.all(st["status"] == 0)
+                assert np.all(st["rel"][np.array(mixed)] <= RES_TOL)
+            S.check(orc, B, x, mixed)
+            for s, part in enumerate(B.split(x)):
+                if mixed[s]:
+                    continue
+                m, r, b = S.items[s]
+                term = orc.term_rel_error(m.row_ptr.astype(np.uint64), m.col, m.val, _cm(S.ref[s], m.n, r),
+                                          _cm(part, m.n, r), _cm(b, m.n, r), r)
+                assert term <= 1e-12, (mode, s, term)

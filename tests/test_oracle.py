@@ -66,6 +66,10 @@ def test_supernodal_matches_reference(golden, orc, tag):
     x = orc.supernodal_blas_upper(sn, rpp, cp, vp, b, rhs)
     ref = golden[tag + "/blas"]
     assert np.max(np.abs(x - ref) / np.maximum(np.abs(ref), 1e-300)) <= 1e-12
+    # the same algorithm with its dgemm / dtrsm on numpy's OpenBLAS (the CPU baseline's BLAS)
+    xo = orc.supernodal_blas_upper_openblas(sn, rpp, cp, vp, b, rhs)
+    if xo is not None:
+        assert np.max(np.abs(xo - ref) / np.maximum(np.abs(ref), 1e-300)) <= 1e-12
 
 
 def test_shipped_fixture_known_answers(golden):
