@@ -68,19 +68,21 @@ class Systems:
 
     def check(self, orc, B, x, mixed):
         parts = B.split(x)
-        for s, (m, r, b) in enumerate(self.items):
-            if mixed[s]:
-                err = elem_err(parts[s], self.ref[s], floor=1e-3)
-                assert err <= MIXED_ELEM_TOL, (s, err)
-                assert norm_err(parts[s], self.ref[s]) <= MIXED_NORM_TOL, s
-            else:
-                err = elem_err(parts[s], self.ref[s])
-                assert err <= ELEM_TOL, (s, err)
-                assert norm_err(parts[s], self.ref[s]) <= 1e-12, s
-            if mixed[s]:
-                res = orc.rel_residual(m.row_ptr.astype(np.uint64), m.col, m.val, _cm(parts[s], m.n, r),
-                                       _cm(b, m.n, r), r)
-                assert res <= 2 * RES_TOL, (s, res)
+        for s in range(len(self.items)):
+            self.check_one(orc, s, parts[s], mixed[s])
+
+    def check_one(self, orc, s, part, mixed):
+        m, r, b = self.items[s]
+        if mixed:
+            err = elem_err(part, self.ref[s], floor=1e-3)
+            assert err <= MIXED_ELEM_TOL, (s, err)
+            assert norm_err(part, self.ref[s]) <= MIXED_NORM_TOL, s
+            res = orc.rel_residual(m.row_ptr.astype(np.uint64), m.col, m.val, _cm(part, m.n, r), _cm(b, m.n, r), r)
+            assert res <= 2 * RES_TOL, (s, res)
+        else:
+            err = elem_err(part, self.ref[s])
+            assert err <= ELEM_TOL, (s, err)
+            assert norm_err(part, self.ref[s]) <= 1e-12, s
 
 
 def _from_mix(M):
@@ -285,8 +287,14 @@ def test_large_mix_up_to_200k(orc):
     """Systems at the batched workload's sizes: 16 from the mix generator (n log-uniform in [1k,
     200k], 1-16 RHS) plus the largest of each kind at 16 RHS (the 447 x 447 grid factor, n =
     199,809, and a 200,000-row random dominant system), in both modes against the serial oracle.
-    FP64 systems also meet a term-relative bound of 1e-12 (the error against the size of the terms
-    a component is summed from, oracle.term_rel_error)."""
+
+    At these sizes two correct FP64 solves that differ only in summation order (the oracle against
+    itself with every row summed in reverse) already disagree by more than 1e-10 on the smallest
+    of ~3 million solution components, so an FP64 system's elementwise error (guarded as in this
+    file) is bounded by max(1e-10, 10 x that floor measured on the same system), and its
+    term-relative error (against the size of the terms a component is summed from,
+    oracle.term_rel_error) by 1e-12.  Mixed systems: residual, normwise and guarded elementwise
+    bounds as in Systems.check."""
     M = gen.mix(count=16, seed=21, nmin=1000, nmax=200_000, rhs_max=16)
     items = _from_mix(M)
     M.close()
@@ -296,6 +304,10 @@ def test_large_mix_up_to_200k(orc):
     rnd = gen.random_upper(200_000, 16.0, 0.9, 64, 23)
     items.append((rnd, 16, rng.uniform(-1, 1, rnd.n * 16)))
     S = Systems(orc, items)
+    floors = []
+    for s, (m, r, b) in enumerate(items):
+        rev = orc.base_gauss_upper_rev(m.row_ptr.astype(np.uint64), m.col, m.val, _cm(b, m.n, r), r)
+        floors.append(elem_err(rev.reshape(r, m.n).T, S.ref[s]))
     with S.batch() as B:
         for mode in ("plain", "chosen"):
             x = B.solve(S.b, mode=mode)
@@ -304,11 +316,14 @@ def test_large_mix_up_to_200k(orc):
                 st = B.stats()
                 assert np.all(st["status"] == 0)
                 assert np.all(st["rel"][np.array(mixed)] <= RES_TOL)
-            S.check(orc, B, x, mixed)
-            for s, part in enumerate(B.split(x)):
+            parts = B.split(x)
+            for s, (m, r, b) in enumerate(items):
                 if mixed[s]:
+                    S.check_one(orc, s, parts[s], True)
                     continue
-                m, r, b = S.items[s]
+                err = elem_err(parts[s], S.ref[s])
+                assert err <= max(ELEM_TOL, 10 * floors[s]), (mode, s, err, floors[s])
+                assert norm_err(parts[s], S.ref[s]) <= 1e-12, (mode, s)
                 term = orc.term_rel_error(m.row_ptr.astype(np.uint64), m.col, m.val, _cm(S.ref[s], m.n, r),
-                                          _cm(part, m.n, r), _cm(b, m.n, r), r)
+                                          _cm(parts[s], m.n, r), _cm(b, m.n, r), r)
                 assert term <= 1e-12, (mode, s, term)
