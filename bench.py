@@ -62,7 +62,7 @@ WORKLOAD = ("irregular-2M: n=2,000,000 upper CSR, Poisson(8) off-diagonals/row, 
 RES_TOL = 1e-12
 # the plain FP64 sync-free baseline of the single-system workload: the fastest exact sync-free
 # kernel for one RHS
-PLAIN_SCHEDULE = "syncfree_window"
+PLAIN_SCHEDULE = "syncfree_block"
 
 
 def parse():

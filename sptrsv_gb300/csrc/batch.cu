@@ -1055,6 +1055,7 @@ int Batch::build_panels(int s, bool f64) {
         scratch = reinterpret_cast<Handle*>(h);
     }
     Handle& H = *scratch;
+    H.build_tc = false;  // the batch builds its own tensor-core records per chunk below
     const BSys& S = sys[s];
     H.drop_matrix();
     H.n = S.n;
@@ -1083,7 +1084,7 @@ int Batch::build_panels(int s, bool f64) {
     const long long gtot = goff[C];
     // buffers of this system: [bf16 hi, bf16 lo] and/or [f64], then the rectangle columns
     const int k0 = (int)gbufs.size();
-    gbufs.resize(k0 + 4);
+    gbufs.resize(k0 + 5);
     if ((rc = gbufs[k0 + 3].ensure(sizeof(int) * ((size_t)roff[C] + 1)))) return rc;
     if (!f64) {
         if ((rc = gbufs[k0].ensure(2 * (size_t)gtot)) || (rc = gbufs[k0 + 1].ensure(2 * (size_t)gtot))) return rc;
@@ -1112,7 +1113,10 @@ int Batch::build_panels(int s, bool f64) {
         if (!f64) {
             ch.ghi = gbufs[k0].as<__nv_bfloat16>() + goff[c];
             ch.glo = gbufs[k0 + 1].as<__nv_bfloat16>() + goff[c];
-            if ((int)old.size() == C) ch.g64 = old[c].g64;
+            if ((int)old.size() == C) {
+                ch.g64 = old[c].g64;
+                ch.gtc = old[c].gtc;
+            }
         } else {
             ch.g64 = gbufs[k0 + 2].as<double>() + goff[c];
             if ((int)old.size() == C) {
@@ -1122,6 +1126,29 @@ int Batch::build_panels(int s, bool f64) {
         }
         ch.rect = gbufs[k0 + 3].as<int>() + roff[c];
         pchunks[s].push_back(ch);
+    }
+    if (f64 && panels_mode() == 1) {
+        // the tensor-core schedule's digit-slice G records of every chunk (one 64-row panel each)
+        std::vector<size_t> toff(C + 1, 0);
+        std::vector<int2> recs;
+        for (int c = 0; c < C; ++c) {
+            const BChunk& b = pchunks[s][c];
+            toff[c + 1] = toff[c] + ((tc_panel_bytes(b.w, b.w + b.m) + 127) & ~(size_t)127);
+            for (int q = 0; q < b.nblk; ++q) recs.push_back(make_int2(c, q));
+        }
+        if ((rc = gbufs[k0 + 4].ensure(std::max<size_t>(toff[C], 128)))) return rc;
+        for (int c = 0; c < C; ++c) pchunks[s][c].gtc = gbufs[k0 + 4].as<unsigned char>() + toff[c];
+        DevBuf tch, trec;
+        if ((rc = tch.ensure(sizeof(BChunk) * C)) || (rc = trec.ensure(sizeof(int2) * std::max<size_t>(1, recs.size()))))
+            return rc;
+        CUDA_TRY(cudaMemcpyAsync(tch.p, pchunks[s].data(), sizeof(BChunk) * C, cudaMemcpyHostToDevice, st));
+        CUDA_TRY(cudaMemcpyAsync(trec.p, recs.data(), sizeof(int2) * recs.size(), cudaMemcpyHostToDevice, st));
+        int64_t lsplit = 0;
+        rc = launch_tc_split(tch.as<BChunk>(), trec.as<int2>(), (int)recs.size(), sm_count, st, &lsplit);
+        if (!rc) CUDA_TRY(cudaStreamSynchronize(st));
+        tch.release();
+        trec.release();
+        if (rc) return rc;
     }
     H.drop_matrix();
     panel_ok[s] = 1;
@@ -1210,7 +1237,7 @@ int Batch::build_lists() {
     g_entries64 = g_fma64 = 0;
     for (int s = 0; s < count; ++s) {
         if (sched[s] != BS_PANEL64) continue;
-        const int base = (int)ch64.size(), ng = p64_groups(sys[s].rhs);
+        const int base = (int)ch64.size(), ng = panels_mode() == 1 ? tc_groups_host(sys[s].rhs) : p64_groups(sys[s].rhs);
         if (ng > 0x7FFF) return SPTRSV_ERR_TOO_LARGE;  // items carry the group in 15 bits
         for (const BChunk& b : pchunks[s])
             if (b.nblk > 0xFFFF) return SPTRSV_ERR_TOO_LARGE;  // and the block in 16
@@ -1344,9 +1371,13 @@ int Batch::build_graph(int mode, const double* b, double* x, cudaGraphExec_t* ou
             cudaEventRecord(ev_fork, st);
             cudaStreamWaitEvent(st2, ev_fork, 0);
             int64_t l64 = 0;
-            if (launch_panels64(A.sys, 0, A.b, A.x, &A.bc->c, &A.bc->ticket_p64, A.budget, items64.as<int2>(),
-                                n_items64, chunks64.as<BChunk>(), part64.as<double>(), cnt64.as<int>(), n_cnt64,
-                                p64_ctas_per_sm, sm_count, st2, &l64))
+            if (panels_mode() == 1
+                    ? launch_panels_tc(A.sys, 0, A.b, A.x, &A.bc->c, &A.bc->ticket_p64, A.budget, items64.as<int2>(),
+                                       n_items64, chunks64.as<BChunk>(), part64.as<double>(), cnt64.as<int>(),
+                                       n_cnt64, sm_count, st2, &l64)
+                    : launch_panels64(A.sys, 0, A.b, A.x, &A.bc->c, &A.bc->ticket_p64, A.budget, items64.as<int2>(),
+                                      n_items64, chunks64.as<BChunk>(), part64.as<double>(), cnt64.as<int>(), n_cnt64,
+                                      p64_ctas_per_sm, sm_count, st2, &l64))
                 rc = SPTRSV_ERR_CUDA;
             cudaEventRecord(ev_join, st2);
             nk += (int)l64;
@@ -1501,9 +1532,14 @@ int Batch::profile(int mode, const double* b, double* x, float* kind_ms, int* ki
         if (n_items64) {
             int64_t l64 = 0;
             if ((rc = timed(13, [&] {
-                     launch_panels64(A.sys, 0, A.b, A.x, &A.bc->c, &A.bc->ticket_p64, A.budget, items64.as<int2>(),
-                                     n_items64, chunks64.as<BChunk>(), part64.as<double>(), cnt64.as<int>(),
-                                     n_cnt64, 64, sm_count, st, &l64);
+                     if (panels_mode() == 1)
+                         launch_panels_tc(A.sys, 0, A.b, A.x, &A.bc->c, &A.bc->ticket_p64, A.budget, items64.as<int2>(),
+                                          n_items64, chunks64.as<BChunk>(), part64.as<double>(), cnt64.as<int>(),
+                                          n_cnt64, sm_count, st, &l64);
+                     else
+                         launch_panels64(A.sys, 0, A.b, A.x, &A.bc->c, &A.bc->ticket_p64, A.budget, items64.as<int2>(),
+                                         n_items64, chunks64.as<BChunk>(), part64.as<double>(), cnt64.as<int>(),
+                                         n_cnt64, 64, sm_count, st, &l64);
                  })))
                 goto out;
         }

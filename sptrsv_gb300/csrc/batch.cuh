@@ -37,6 +37,7 @@ struct BChunk {
     int nblk;                  // FP64 schedule: column blocks of G
     int r0, pw;                // the panel's rows within the chunk
     int cbase;                 // FP64 schedule: first completion counter (one per RHS group)
+    unsigned char* gtc;        // tensor-core FP64 schedule: the panel's digit-slice G records (panels_tc.cu)
 };
 
 // Column blocks of a panel's G (w own columns, then K - w solved columns): the own part in
@@ -73,5 +74,19 @@ __host__ __device__ __forceinline__ void p64_block(int w, int K, int blk, int& k
 int launch_panels64(const BSys* sys, int rhs, const double* b, double* x, Ctl* ctl, unsigned* ticket, int64_t budget,
                     const int2* items, unsigned nitems, const BChunk* panels, double* part, int* cnt, int ncnt,
                     int ctas_per_sm, int sm_count, cudaStream_t st, int64_t* launches);
+
+// FP64-accurate panel products on the tensor cores (panels_tc.cu): the same items, partial sums
+// and counters as launch_panels64, with tc_groups_host(rhs) groups per item for one system.  The
+// panels' gtc records come from launch_tc_split over every (panel, block) pair in recs.
+int launch_panels_tc(const BSys* sys, int rhs, const double* b, double* x, Ctl* ctl, unsigned* ticket, int64_t budget,
+                     const int2* items, unsigned nitems, const BChunk* panels, double* part, int* cnt, int ncnt,
+                     int sm_count, cudaStream_t st, int64_t* launches);
+int launch_tc_split(const BChunk* panels, const int2* recs, int nrec, int sm_count, cudaStream_t st,
+                    int64_t* launches);
+size_t tc_panel_bytes(int w, int K);  // bytes of one panel's G records
+int tc_groups_host(int rhs);
+// Panel products of the exact FP64 schedules: 0 = FP64 FMAs (default), 1 = tensor cores
+// (SPTRSV_PANELS=tc).
+int panels_mode();
 
 }  // namespace sptrsv

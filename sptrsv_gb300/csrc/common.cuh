@@ -165,11 +165,17 @@ __device__ __forceinline__ bool grid_barrier(Ctl* ctl, unsigned nblocks, int64_t
             __threadfence();
             st_release(&ctl->bar_gen, gen + 1);
         } else {
-            const uint64_t t0 = gtimer();
+            // poll without sleeping first (a level usually ends within microseconds), then back off;
+            // the timer and the abort flag are read every 64 polls
+            uint64_t t0 = 0;
+            unsigned it = 0;
             while (ld_acquire(&ctl->bar_gen) == gen) {
-                if (aborted(ctl)) { ok = 0; break; }
-                if ((int64_t)(gtimer() - t0) > budget_ns) { record_error(ctl, SPTRSV_ERR_TIMEOUT); ok = 0; break; }
-                __nanosleep(32);
+                if ((++it & 63u) == 0) {
+                    if (aborted(ctl)) { ok = 0; break; }
+                    if (t0 == 0) t0 = gtimer();
+                    else if ((int64_t)(gtimer() - t0) > budget_ns) { record_error(ctl, SPTRSV_ERR_TIMEOUT); ok = 0; break; }
+                }
+                if (it > 4096) __nanosleep(32);
             }
         }
         s_ok = ok;

@@ -108,6 +108,9 @@ struct Handle {
     // the FP64 solve's 64-row panels split into column blocks (panels64.cu): panel records,
     // (panel, block) items, per-panel completion counters, partial sums (sn_prows per column)
     DevBuf sn_pan, sn_pitems, sn_pcnt, sn_ppart;
+    DevBuf sn_gtc, sn_tcrec;  // tensor-core schedule: digit-slice G records of every panel block
+    bool sn_tc = false;       // the records are built
+    bool build_tc = true;     // set_supernodes builds them (off for the batch's scratch handle)
     int sn_npan = 0;
     unsigned sn_npitems = 0;
     long long sn_prows = 0;

@@ -263,8 +263,10 @@ __global__ void __launch_bounds__(256) k_push_csc(int n, int rhs, const int* __r
 template <typename T>
 __device__ __forceinline__ T ldcg(const T* p) { return __ldcg(p); }
 
+constexpr int kLevelsetThreads = 1024;  // one CTA per SM: a grid barrier takes one arrival per SM
+
 template <typename T>
-__global__ void __launch_bounds__(256) k_levelset(int n, int rhs, const int* __restrict__ rp, const int* __restrict__ col,
+__global__ void __launch_bounds__(kLevelsetThreads) k_levelset(int n, int rhs, const int* __restrict__ rp, const int* __restrict__ col,
                                                   const T* __restrict__ val, const T* __restrict__ invd,
                                                   const T* __restrict__ b, T* x, int max_level,
                                                   const int* __restrict__ lptr, const int* __restrict__ lrows,
@@ -438,17 +440,17 @@ template <typename T>
 static int levelset_t(const SolveArgs& a, int max_level, const int* lptr, const int* lrows) {
     const void* fn = (const void*)k_levelset<T>;
     int per_sm = 0;
-    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 256, 0));
+    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kLevelsetThreads, 0));
     if (per_sm < 1) return SPTRSV_ERR_UNSUPPORTED;
-    int grid = per_sm * a.sm_count;
-    if (a.warps > 0) grid = std::max(1, std::min(grid, (a.warps * 32 + 255) / 256));
+    int grid = a.sm_count;  // one CTA per SM (co-resident: per_sm >= 1)
+    if (a.warps > 0) grid = std::max(1, std::min(grid, (a.warps * 32 + kLevelsetThreads - 1) / kLevelsetThreads));
     const T* val = (const T*)a.val;
     const T* invd = (const T*)a.invd;
     const T* b = (const T*)a.b;
     T* x = (T*)a.x;
     void* args[] = {(void*)&a.n, (void*)&a.rhs, (void*)&a.rp, (void*)&a.col, (void*)&val, (void*)&invd, (void*)&b,
                     (void*)&x, (void*)&max_level, (void*)&lptr, (void*)&lrows, (void*)&a.ctl, (void*)&a.budget};
-    CUDA_TRY(cudaLaunchCooperativeKernel(fn, grid, 256, args, 0, a.st));
+    CUDA_TRY(cudaLaunchCooperativeKernel(fn, grid, kLevelsetThreads, args, 0, a.st));
     ++*a.launches;
     return 0;
 }

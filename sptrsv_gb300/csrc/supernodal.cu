@@ -401,10 +401,30 @@ int Handle::set_supernodes(int sn, const int* snodes_host) {
         for (int q = nb - 1; q >= no; --q)
             for (int p = 0; p < np; ++p) pit.push_back(make_int2(first + p, q));
     }
+    // tensor-core schedule: every panel's G records (digit slices, panels_tc.cu), built below
+    std::vector<int2> recs;
+    sn_tc = false;
+    if (panels_mode() == 1 && build_tc) {
+        size_t tot = 0;
+        std::vector<size_t> toff(pan.size());
+        for (size_t p = 0; p < pan.size(); ++p) {
+            toff[p] = tot;
+            tot += (tc_panel_bytes(pan[p].w, pan[p].w + pan[p].m) + 127) & ~(size_t)127;
+            for (int q = 0; q < pan[p].nblk; ++q) recs.push_back(make_int2((int)p, q));
+        }
+        if ((rc = sn_gtc.ensure(tot)) || (rc = sn_tcrec.ensure(sizeof(int2) * recs.size()))) return rc;
+        for (size_t p = 0; p < pan.size(); ++p) pan[p].gtc = sn_gtc.as<unsigned char>() + toff[p];
+    }
     if ((rc = sn_pan.ensure(sizeof(BChunk) * pan.size())) || (rc = sn_pitems.ensure(sizeof(int2) * pit.size())))
         return rc;
     CUDA_TRY(cudaMemcpyAsync(sn_pan.p, pan.data(), sizeof(BChunk) * pan.size(), cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaMemcpyAsync(sn_pitems.p, pit.data(), sizeof(int2) * pit.size(), cudaMemcpyHostToDevice, st));
+    if (!recs.empty()) {
+        CUDA_TRY(cudaMemcpyAsync(sn_tcrec.p, recs.data(), sizeof(int2) * recs.size(), cudaMemcpyHostToDevice, st));
+        if ((rc = launch_tc_split(sn_pan.as<BChunk>(), sn_tcrec.as<int2>(), (int)recs.size(), sm_count, st, &launches)))
+            return rc;
+        sn_tc = true;
+    }
     CUDA_TRY(cudaStreamSynchronize(st));
     sn_npan = (int)pan.size();
     sn_npitems = (unsigned)pit.size();
@@ -437,6 +457,11 @@ int launch_sn_solve(const Handle& h, bool mixed, const void* b, void* x, int rhs
         const int ncnt = h.sn_npan * p64_groups(rhs);
         if (h.sn_ppart.cap < sizeof(double) * (size_t)h.sn_prows * rhs || h.sn_pcnt.cap < sizeof(int) * (size_t)ncnt)
             return SPTRSV_ERR_INVALID_ARG;
+        if (h.sn_tc)
+            return launch_panels_tc(nullptr, rhs, (const double*)b, (double*)x, h.ctl, &h.ctl->ticket, budget,
+                                    h.sn_pitems.as<int2>(), h.sn_npitems, h.sn_pan.as<BChunk>(),
+                                    h.sn_ppart.as<double>(), h.sn_pcnt.as<int>(), h.sn_npan * tc_groups_host(rhs),
+                                    h.sm_count, h.st, launches);
         return launch_panels64(nullptr, rhs, (const double*)b, (double*)x, h.ctl, &h.ctl->ticket, budget,
                                h.sn_pitems.as<int2>(), h.sn_npitems, h.sn_pan.as<BChunk>(), h.sn_ppart.as<double>(),
                                h.sn_pcnt.as<int>(), ncnt, 64, h.sm_count, h.st, launches);

@@ -41,6 +41,8 @@
 // as p = fma(-U_ij / U_ii, x_j, p), so a dependency hop costs one FP64 FMA.  The levels
 // (core.cpp:244-270) take the maximum over the row's columns: level_i = 1 + max_j level_j
 // (1 for a diagonal-only row), with 0 as the pending value, bit-exact.
+#include <cstdlib>
+#include <cstring>
 #include <type_traits>
 #include "common.cuh"
 #include "kernels.cuh"
@@ -157,7 +159,21 @@ __device__ __forceinline__ void win_stage_data(const WinStage<T, W>& S, int rs, 
     }
 }
 
-template <typename T, int W>
+// x in global memory: rows of this CTA only.  kWeak: plain stores and loads, ordered by the
+// done-flag protocol's CTA fences (a reader only loads x of rows in finished blocks, after the
+// acquire fence that follows the flag); otherwise GPU-scope relaxed ones.
+template <typename T, bool kWeak>
+__device__ __forceinline__ T win_ld(const T* p) {
+    if constexpr (kWeak) return *p;
+    else return ld_relaxed(p);
+}
+template <typename T, bool kWeak>
+__device__ __forceinline__ void win_st(T* p, T v) {
+    if constexpr (kWeak) *p = v;
+    else st_relaxed(p, v);
+}
+
+template <typename T, int W, bool kWeak>
 __global__ void __launch_bounds__(W * 32, 1)
 k_window(int n, const int* __restrict__ rp, const int* __restrict__ col, const T* __restrict__ val,
          const T* __restrict__ invd, const T* __restrict__ b, T* x, Ctl* ctl, int64_t budget, int backoff_ns) {
@@ -278,7 +294,7 @@ k_window(int n, const int* __restrict__ rp, const int* __restrict__ col, const T
                     vq[q] = use[q] ? eval(kq) : T(0);
                 }
 #pragma unroll
-                for (int q = 0; q < 4; ++q) xq[q] = use[q] ? ld_relaxed(x + cq[q]) : T(0);
+                for (int q = 0; q < 4; ++q) xq[q] = use[q] ? win_ld<T, kWeak>(x + cq[q]) : T(0);
                 bool bad = false;
 #pragma unroll
                 for (int q = 0; q < 4; ++q) bad |= use[q] && WinVal<T>::is_pending(xq[q]);
@@ -299,60 +315,122 @@ k_window(int n, const int* __restrict__ rp, const int* __restrict__ col, const T
                 }
             }
         }
-        // the rest in warp lockstep rounds
-        const uint64_t t0 = gtimer();
-        unsigned it = 0;
-        bool fail = false;
-        for (;;) {
-            bool prog = false;
-            if (!done) {
-                while (k > s) {
-                    const T xv = c >= far ? ld_relaxed(x + c) : vring[c & RM];
-                    if (WinVal<T>::is_pending(xv)) {
-                        if constexpr (!kLevels) {
-                            if (!scaled) {  // from here on one FMA per term
-                                p = fma(-acc, di, bd);
-                                vs = -v * di;
-                                scaled = true;
-                            }
-                        }
-                        break;
-                    }
-                    prog = true;
-                    if constexpr (kLevels) {
-                        acc = max(acc, xv);
-                    } else {
-                        if (scaled) p = fma(vs, xv, p);
-                        else acc = fma(v, xv, acc);
-                    }
-                    if (--k > s) {
-                        c = ecol(k);
-                        v = eval(k);
-                        if constexpr (!kLevels) {
-                            if (scaled) vs = -v * di;
+        // the rest: one walk over what is ready, then lockstep rounds over the remaining entries
+        bool prog = false;
+        // walk right to left consuming ready entries; stops at the first pending one
+        auto walk = [&]() {
+            while (k > s) {
+                const T xv = c >= far ? win_ld<T, kWeak>(x + c) : vring[c & RM];
+                if (WinVal<T>::is_pending(xv)) {
+                    if constexpr (!kLevels) {
+                        if (!scaled) {  // from here on one FMA per term
+                            p = fma(-acc, di, bd);
+                            vs = -v * di;
+                            scaled = true;
                         }
                     }
+                    break;
                 }
-                if (k <= s) {
-                    T xi;
-                    if constexpr (kLevels) {
-                        xi = 1 + acc;
-                        lmax = max(lmax, xi);
-                    } else {
-                        xi = Pend<T>::fix(scaled ? p : fma(-acc, di, bd));
+                prog = true;
+                if constexpr (kLevels) {
+                    acc = max(acc, xv);
+                } else {
+                    if (scaled) p = fma(vs, xv, p);
+                    else acc = fma(v, xv, acc);
+                }
+                if (--k > s) {
+                    c = ecol(k);
+                    v = eval(k);
+                    if constexpr (!kLevels) {
+                        if (scaled) vs = -v * di;
                     }
-                    vring[i & RM] = xi;
-                    st_relaxed(x + i, xi);
-                    done = true;
-                    prog = true;
                 }
             }
-            if (__all_sync(0xffffffffu, done || fail)) break;
+        };
+        auto publish = [&](T xi) {
+            vring[i & RM] = xi;
+            win_st<T, kWeak>(x + i, xi);
+            done = true;
+            prog = true;
+        };
+        auto finish = [&]() {
+            if constexpr (kLevels) {
+                const T xi = 1 + acc;
+                lmax = max(lmax, xi);
+                publish(xi);
+            } else {
+                publish(Pend<T>::fix(scaled ? p : fma(-acc, di, bd)));
+            }
+        };
+        if (!done) {
+            walk();
+            if (k <= s) finish();
+        }
+        // the remaining entries (the first is pending) in registers when they are few: a round is
+        // then two polls, at most two FMAs and a shift
+        constexpr int RS = 6;
+        int cs[RS];
+        T ws[RS];
+        int nrem = 0;
+        bool lean = false;
+        if (!done && k - s <= RS) {
+            lean = true;
+            nrem = k - s;
+#pragma unroll
+            for (int q = 0; q < RS; ++q) {
+                cs[q] = q < nrem ? ecol(k - q) : 0;
+                if constexpr (kLevels) ws[q] = 0;
+                else ws[q] = q < nrem ? -eval(k - q) * di : T(0);
+            }
+        }
+        // the budget's timer starts at the block for short budgets, else at round 31 of the block
+        uint64_t t0 = budget < 1000000 ? gtimer() : 0;
+        unsigned it = 0;
+        bool fail = false;
+        while (!__all_sync(0xffffffffu, done || fail)) {
+            prog = false;
+            if (!done) {
+                if (lean) {
+                    const T x0 = cs[0] >= far ? win_ld<T, kWeak>(x + cs[0]) : vring[cs[0] & RM];
+                    const T x1 = nrem > 1 ? (cs[1] >= far ? win_ld<T, kWeak>(x + cs[1]) : vring[cs[1] & RM])
+                                          : WinVal<T>::pending();
+                    if (!WinVal<T>::is_pending(x0)) {
+                        const bool two = nrem > 1 && !WinVal<T>::is_pending(x1);
+                        if constexpr (kLevels) {
+                            acc = max(acc, x0);
+                            if (two) acc = max(acc, x1);
+                        } else {
+                            p = fma(ws[0], x0, p);
+                            if (two) p = fma(ws[1], x1, p);
+                        }
+                        if (two) {
+                            nrem -= 2;
+#pragma unroll
+                            for (int q = 0; q + 2 < RS; ++q) {
+                                cs[q] = cs[q + 2];
+                                ws[q] = ws[q + 2];
+                            }
+                        } else {
+                            nrem -= 1;
+#pragma unroll
+                            for (int q = 0; q + 1 < RS; ++q) {
+                                cs[q] = cs[q + 1];
+                                ws[q] = ws[q + 1];
+                            }
+                        }
+                        prog = true;
+                        if (nrem == 0) finish();
+                    }
+                } else {
+                    walk();
+                    if (k <= s) finish();
+                }
+            }
             if (backoff_ns > 0 && !__any_sync(0xffffffffu, prog)) __nanosleep(backoff_ns);
-            // the budget is checked at round 31 of a block (a 32-row chain takes 32 rounds) and
-            // every 256 rounds after
+            // checked at round 31 of a block (a 32-row chain takes 32 rounds) and every 256 after
             if ((++it & 255u) == 31u) {
                 if (aborted(ctl)) fail = true;
+                else if (t0 == 0) t0 = gtimer();
                 else if ((int64_t)(gtimer() - t0) > budget) {
                     record_error(ctl, SPTRSV_ERR_TIMEOUT);
                     fail = true;
@@ -376,8 +454,8 @@ k_window(int n, const int* __restrict__ rp, const int* __restrict__ col, const T
 }
 
 // ---------------------------------------------------------------------------------------
-template <typename T, int W>
-static int window_launch(int n, const int* rp, const int* col, const T* val, const T* invd, const T* b, T* x,
+template <typename T, int W, bool kWeak>
+static int window_launch_t(int n, const int* rp, const int* col, const T* val, const T* invd, const T* b, T* x,
                          Ctl* ctl, int64_t budget, int backoff_ns, cudaStream_t st, int64_t* launches) {
     using L = WinLayout<T, W>;
     static bool configured[64] = {};
@@ -385,13 +463,31 @@ static int window_launch(int n, const int* rp, const int* col, const T* val, con
     CUDA_TRY(cudaGetDevice(&dev));
     if (dev < 0 || dev >= 64) return SPTRSV_ERR_INVALID_ARG;
     if (!configured[dev]) {
-        CUDA_TRY(cudaFuncSetAttribute(k_window<T, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L::kBytes));
+        CUDA_TRY(cudaFuncSetAttribute(k_window<T, W, kWeak>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)L::kBytes));
         configured[dev] = true;
     }
-    k_window<T, W><<<1, W * 32, L::kBytes, st>>>(n, rp, col, val, invd, b, x, ctl, budget, backoff_ns);
+    k_window<T, W, kWeak><<<1, W * 32, L::kBytes, st>>>(n, rp, col, val, invd, b, x, ctl, budget, backoff_ns);
     ++*launches;
     CUDA_TRY(cudaGetLastError());
     return 0;
+}
+
+// x stores and loads: weak (the default) or GPU-scope relaxed (SPTRSV_WINDOW_STORE=relaxed)
+static bool window_weak() {
+    static bool w = [] {
+        const char* e = getenv("SPTRSV_WINDOW_STORE");
+        return !(e && strcmp(e, "relaxed") == 0);
+    }();
+    return w;
+}
+
+template <typename T, int W>
+static int window_launch(int n, const int* rp, const int* col, const T* val, const T* invd, const T* b, T* x,
+                         Ctl* ctl, int64_t budget, int backoff_ns, cudaStream_t st, int64_t* launches) {
+    return window_weak() ? window_launch_t<T, W, true>(n, rp, col, val, invd, b, x, ctl, budget, backoff_ns, st, launches)
+                         : window_launch_t<T, W, false>(n, rp, col, val, invd, b, x, ctl, budget, backoff_ns, st,
+                                                        launches);
 }
 
 template <typename T>
