@@ -62,7 +62,7 @@ WORKLOAD = ("irregular-2M: n=2,000,000 upper CSR, Poisson(8) off-diagonals/row, 
 RES_TOL = 1e-12
 # the plain FP64 sync-free baseline of the single-system workload: the fastest exact sync-free
 # kernel for one RHS
-PLAIN_SCHEDULE = "syncfree_block"
+PLAIN_SCHEDULE = "syncfree_window"
 
 
 def parse():
@@ -82,6 +82,11 @@ def parse():
     ap.add_argument("--batch-steps", type=int, default=10,
                     help="default workload: timed steps of the batched mix measured after the 2M-row system")
     ap.add_argument("--no-batch", action="store_true", help="default workload: skip the nested batched-mix record")
+    ap.add_argument("--panels", default="fp64", choices=["fp64", "tc"],
+                    help="panel products of the exact FP64 supernodal / batched schedules: FP64 FMAs or the tensor "
+                         "cores (BF16 digit slices, FP64-accurate)")
+    ap.add_argument("--plain-schedule", default=None, choices=["syncfree_block", "syncfree_window", "syncfree_warp"],
+                    help="default workload: the plain FP64 sync-free baseline's schedule")
     return ap.parse_args()
 
 
@@ -819,6 +824,8 @@ def batch_record(args, dist, steps, warmup, with_cpu=True, sample_errors=True):
         "config": {"workload": BATCH_WORKLOAD.format(count=args.count, nmax=args.nmax), "systems": args.count,
                    "rows": int(np.sum(M.n)), "nnz": int(np.sum(M.nnz)), "rhs_columns": int(np.sum(M.rhs)),
                    "rank0_systems": count_l, "schedules": counts, "picked_by": picked_by, "generation_s": t_gen,
+                   "panel_products": "tensor cores (BF16 digit slices, FP64-accurate)" if args.panels == "tc"
+                   else "FP64 FMAs",
                    "l2": "no flush: the arena (%.1f GB) is far larger than L2" % (fb / 1e9),
                    "parallelism": f"systems sharded over {dist.ws} GPU(s) by LPT on nnz x rhs"},
         "solve_unit": "one system with all its right-hand sides",
@@ -951,7 +958,7 @@ def run_supernodal(args, dist):
                                      "max(|ref_i|, (|b_i| + sum_j |U_ij ref_j|) / |U_ii|); reorder_floor_elem_err: "
                                      "elem_err of the serial solve summed in reverse order",
                       "n": m.n, "nnz": m.nnz, "supernodes": int(len(m.snodes) - 1), "max_level": info["max_level"],
-                      "generation_s": t_gen, "rows": rows}), flush=True)
+                      "panels": args.panels, "generation_s": t_gen, "rows": rows}), flush=True)
 
 
 def run_dropin(args, dist):
@@ -1001,10 +1008,21 @@ def run_dropin(args, dist):
                       "rows": rows}), flush=True)
 
 
+def apply_options(args):
+    """Process-wide choices the command line makes before anything is built."""
+    global PLAIN_SCHEDULE
+    if args.impl == "ours":
+        import sptrsv_gb300 as sp
+        sp.set_panels_mode(args.panels)
+        if args.plain_schedule:
+            PLAIN_SCHEDULE = args.plain_schedule
+
+
 def main():
     args = parse()
     dist = Dist()
     try:
+        apply_options(args)
         if args.impl == "reference":
             run_reference(args, dist)
         elif args.workload == "batch":

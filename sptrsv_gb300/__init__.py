@@ -71,6 +71,15 @@ def measure_fp64(device=0):
     return g.value, c.value
 
 
+def set_panels_mode(mode):
+    """Panel products of the exact FP64 schedules: "fp64" (FP64 FMAs) or "tc" (tensor cores, FP64
+    accurate); applies to partitions and batches built afterwards; returns the previous mode."""
+    rc = _lib.lib().sptrsv_set_panels_mode({"fp64": 0, "tc": 1}[mode])
+    if rc < 0:
+        raise SptrsvError(rc, "set_panels_mode")
+    return ("fp64", "tc")[rc]
+
+
 def candidate(cand_id):
     """sptrsv_opts of entry `cand_id` of the autotuner's candidate table."""
     o = Opts()

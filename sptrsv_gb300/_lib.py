@@ -91,6 +91,7 @@ C_API = {
     "sptrsv_get_in_degree": ([c_vp, i32], c_int),
     "sptrsv_get_csc": ([c_vp, i32, i32, f64], c_int),
     "sptrsv_measure_fp64": ([c_int, ctypes.POINTER(c_dbl), ctypes.POINTER(c_dbl)], c_int),
+    "sptrsv_set_panels_mode": ([c_int], c_int),
     "sptrsv_get_level_buckets": ([c_vp, i32, i32], c_int),
     "sptrsv_get_level_tasks": ([c_vp, c_int, i32], c_int),
     "sptrsv_solve": ([c_vp, ctypes.POINTER(Opts), c_vp, c_vp, c_int, c_int], c_int),

@@ -214,15 +214,16 @@ int Handle::build_csc() {
     return 0;
 }
 
-// FP64 AUTO with one RHS takes the one-CTA window kernel when SPTRSV_AUTO_WINDOW=1; by default the
-// block kernel, which measured faster on the 2M-row system (324 against 355 ms) and on the
-// 64 x 64 band factor (2.25 against 2.8 ms).
-static bool auto_window() {
-    static bool w = [] {
+// FP64 AUTO with one RHS: the one-CTA window kernel on short rows (its lanes hold a row's pending
+// entries in registers; 2M-row system, 8.6 entries per row: 208 against 324 ms for the block
+// kernel), the block kernel on long rows (64 x 64 band factor, 65 entries per row: 2.25 against
+// 3.25 ms).  SPTRSV_AUTO_WINDOW=0 / 1 forces either.
+static bool auto_window(double mean_len) {
+    static int w = [] {
         const char* e = getenv("SPTRSV_AUTO_WINDOW");
-        return e && strcmp(e, "1") == 0;
+        return e ? (strcmp(e, "1") == 0 ? 1 : 0) : -1;
     }();
-    return w;
+    return w < 0 ? mean_len <= 24.0 : w == 1;
 }
 
 // Schedule choice from the analysis features (the autotuner overrides it).
@@ -260,7 +261,7 @@ sptrsv_opts Handle::resolve(const sptrsv_opts* o, int rhs) const {
             // sync-free kernel for one RHS (and, once per column, for several RHS on long rows)
             // and the RHS-tiled warp kernel for several RHS on short rows
             if (levels_ready && width >= 2048.0 && max_level <= 2000) r.schedule = SPTRSV_SCHED_LEVELSET;
-            else if (rhs == 1) r.schedule = auto_window() ? SPTRSV_SCHED_SYNCFREE_WINDOW : SPTRSV_SCHED_SYNCFREE_BLOCK;
+            else if (rhs == 1) r.schedule = auto_window(mean_len) ? SPTRSV_SCHED_SYNCFREE_WINDOW : SPTRSV_SCHED_SYNCFREE_BLOCK;
             else if (mean_len >= kBlockPerColumnLen) r.schedule = SPTRSV_SCHED_SYNCFREE_BLOCK;
             else r.schedule = SPTRSV_SCHED_SYNCFREE_WARP;
         }

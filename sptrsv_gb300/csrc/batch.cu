@@ -920,7 +920,8 @@ struct Batch {
     std::vector<float> ratio;
     std::vector<int> sched;
     std::vector<int> panel_ok;  // -1 unknown, 0 no, 1 yes
-    std::vector<char> have_bf16, have_f64;
+    std::vector<char> have_bf16, have_f64, have_tc;  // have_tc: tensor-core records of the FP64 panels
+    bool use_tc = false;  // the FP64 panel items run on the tensor cores (set by build_lists)
     long long tot_rows = 0, tot_nnz = 0, tot_x = 0, tot_rp = 0;
     DevBuf rp, col, val, val32, invd, invd32, dsys, dstate, dctl;
     DevBuf r32, d0, d1, bw, xw;
@@ -1127,6 +1128,7 @@ int Batch::build_panels(int s, bool f64) {
         ch.rect = gbufs[k0 + 3].as<int>() + roff[c];
         pchunks[s].push_back(ch);
     }
+    have_tc[s] = 0;
     if (f64 && panels_mode() == 1) {
         // the tensor-core schedule's digit-slice G records of every chunk (one 64-row panel each)
         std::vector<size_t> toff(C + 1, 0);
@@ -1149,6 +1151,7 @@ int Batch::build_panels(int s, bool f64) {
         tch.release();
         trec.release();
         if (rc) return rc;
+        have_tc[s] = 1;
     }
     H.drop_matrix();
     panel_ok[s] = 1;
@@ -1232,12 +1235,16 @@ int Batch::build_lists() {
     // systems; partial-sum slots per chunk, completion counters per (chunk, group)
     std::vector<BChunk> ch64;
     std::vector<std::vector<std::vector<int2>>> per64;  // per system, per step (chunk from the last)
+    // the tensor cores take the FP64 panels when every panel system has its records
+    use_tc = panels_mode() == 1;
+    for (int s = 0; s < count; ++s)
+        if (sched[s] == BS_PANEL64 && !have_tc[s]) use_tc = false;
     long long poff = 0;
     int cbase = 0;
     g_entries64 = g_fma64 = 0;
     for (int s = 0; s < count; ++s) {
         if (sched[s] != BS_PANEL64) continue;
-        const int base = (int)ch64.size(), ng = panels_mode() == 1 ? tc_groups_host(sys[s].rhs) : p64_groups(sys[s].rhs);
+        const int base = (int)ch64.size(), ng = use_tc ? tc_groups_host(sys[s].rhs) : p64_groups(sys[s].rhs);
         if (ng > 0x7FFF) return SPTRSV_ERR_TOO_LARGE;  // items carry the group in 15 bits
         for (const BChunk& b : pchunks[s])
             if (b.nblk > 0xFFFF) return SPTRSV_ERR_TOO_LARGE;  // and the block in 16
@@ -1371,7 +1378,7 @@ int Batch::build_graph(int mode, const double* b, double* x, cudaGraphExec_t* ou
             cudaEventRecord(ev_fork, st);
             cudaStreamWaitEvent(st2, ev_fork, 0);
             int64_t l64 = 0;
-            if (panels_mode() == 1
+            if (use_tc
                     ? launch_panels_tc(A.sys, 0, A.b, A.x, &A.bc->c, &A.bc->ticket_p64, A.budget, items64.as<int2>(),
                                        n_items64, chunks64.as<BChunk>(), part64.as<double>(), cnt64.as<int>(),
                                        n_cnt64, sm_count, st2, &l64)
@@ -1532,7 +1539,7 @@ int Batch::profile(int mode, const double* b, double* x, float* kind_ms, int* ki
         if (n_items64) {
             int64_t l64 = 0;
             if ((rc = timed(13, [&] {
-                     if (panels_mode() == 1)
+                     if (use_tc)
                          launch_panels_tc(A.sys, 0, A.b, A.x, &A.bc->c, &A.bc->ticket_p64, A.budget, items64.as<int2>(),
                                           n_items64, chunks64.as<BChunk>(), part64.as<double>(), cnt64.as<int>(),
                                           n_cnt64, sm_count, st, &l64);
@@ -1678,6 +1685,7 @@ int sptrsv_batch_create(sptrsv_batch* out, int device, int count, const int* n, 
     if (const char* e = getenv("SPTRSV_P64_CTAS")) B->p64_ctas_per_sm = std::max(1, atoi(e));
     if (const char* e = getenv("SPTRSV_BJAC")) B->jacobi_elem = strcmp(e, "elem") == 0;
     B->have_f64.assign(count, 0);
+    B->have_tc.assign(count, 0);
     B->gidx.assign(count, -1);
     B->pchunks.resize(count);
     int rc = 0;

@@ -58,12 +58,13 @@ size_t tc_panel_bytes(int w, int K) { return tc_block_offset(w, K, p64_nblk(w, K
 __host__ __device__ __forceinline__ int tc_group_width(int rhs) { return rhs < kTcN ? rhs : kTcN; }
 __host__ __device__ __forceinline__ int tc_groups(int rhs) { return (rhs + kTcN - 1) / kTcN; }
 int tc_groups_host(int rhs) { return tc_groups(rhs); }
+static int g_panels_mode = -1;
 int panels_mode() {
-    static int m = [] {
+    if (g_panels_mode < 0) {
         const char* e = getenv("SPTRSV_PANELS");
-        return (e && strcmp(e, "tc") == 0) ? 1 : 0;
-    }();
-    return m;
+        g_panels_mode = (e && strcmp(e, "tc") == 0) ? 1 : 0;
+    }
+    return g_panels_mode;
 }
 
 // G records of every (panel, block) in recs: digit slices in K-major tile layout, row exponents.
@@ -129,8 +130,8 @@ __global__ void __launch_bounds__(128, 2) k_panels_tc(const BSys* __restrict__ s
     __syncthreads();
     tc::fence_after();
     const uint32_t tmem = s_tmem;
-    unsigned phase = 0;
-    for (;; phase ^= 1u) {
+    unsigned phase = 0;  // of both mbarriers: each completes once per tensor-core item
+    for (;;) {
         if (tid == 0) s_t = aborted(ctl) ? 0xFFFFFFFFu : atomicAdd(ticket, 1u);
         __syncthreads();
         const unsigned t = s_t;
@@ -160,140 +161,178 @@ __global__ void __launch_bounds__(128, 2) k_panels_tc(const BSys* __restrict__ s
         const double* b = bbase + xb0;
         double* x = xbase + xb0;
         double* pb = part + poff + (long long)blk * pw * m;
-        // 1. the G record (digit slices + row exponents), one bulk copy
-        if (tid == 0) {
-            tc::mbar_expect_tx(&barG, rec_bytes);
-            tc::bulk_g2s(sG, C.gtc + tc_block_offset(w, K, blk), rec_bytes, &barG);
-            s_ok = 1;
-        }
-        if (tid < kTcN) s_vexp[tid] = tc::kExpZero;
-        __syncthreads();
-        // 2. the right-hand-side block (kc x nc), waiting on unsolved rows; column scales; digits
-        constexpr int kPer = (kP64 * kTcN + 127) / 128;
-        double v[kPer];
-#pragma unroll
-        for (int u = 0; u < kPer; ++u) {
-            const int e = tid + u * 128;
-            double val = 0.0;
-            if (e < kc * nc) {
-                const int kk = e / nc, j = e - kk * nc, k = k0 + kk;
-                val = k < w ? b[(size_t)(a + k) * m + c0 + j] : ld_relaxed(x + (size_t)C.rect[k - w] * m + c0 + j);
+        const int no = p64_nown(w), nn = p64_nnear(w, K);
+        if (blk >= no && blk < no + nn) {
+            // a narrow block next to the dependency chain (the nearest solved rows): FP64 FMAs, as
+            // in the FP64 panel kernel -- no digit split, TMEM round trip or record copy on the chain
+            double* Gs = reinterpret_cast<double*>(sG);  // pw x kc
+            double* Vs = red;                             // kc x nc
+            for (int e = tid; e < pw * kc; e += 128) {
+                const int r = e / kc, kk = e - r * kc;
+                tc::cp_async8(&Gs[e], C.g64 + (size_t)(r0 + r) * C.ld + k0 + kk);
             }
-            v[u] = val;
-        }
-#pragma unroll
-        for (int u = 0; u < kPer; ++u) {
-            const int e = tid + u * 128;
-            if (e < kc * nc) {
+            if (tid == 0) s_ok = 1;
+            __syncthreads();
+            for (int e = tid; e < kc * nc; e += 128) {
                 const int kk = e / nc, j = e - kk * nc, k = k0 + kk;
-                if (k >= w && Pend<double>::is(v[u]) &&
-                    !wait_ready<double>(x + (size_t)C.rect[k - w] * m + c0 + j, v[u], ctl, budget)) {
+                double val = k < w ? b[(size_t)(a + k) * m + c0 + j] : ld_relaxed(x + (size_t)C.rect[k - w] * m + c0 + j);
+                if (k >= w && Pend<double>::is(val) &&
+                    !wait_ready<double>(x + (size_t)C.rect[k - w] * m + c0 + j, val, ctl, budget)) {
                     s_ok = 0;
-                    v[u] = 0.0;
+                    val = 0.0;
                 }
-                atomicMax(&s_vexp[j], tc::exp_bound(v[u]));
+                Vs[e] = val;
             }
-        }
-        __syncthreads();
-        const size_t vtile = (size_t)N * kcp * 2;
+            tc::cp_async_wait_all();
+            if (__syncthreads_or(!s_ok)) break;
+            for (int o = tid; o < pw * nc; o += 128) {
+                const int r = o / nc, j = o - r * nc;
+                double s0 = 0.0, s1 = 0.0;
+                int kk = 0;
+                for (; kk + 1 < kc; kk += 2) {
+                    s0 = fma(Gs[r * kc + kk], Vs[kk * nc + j], s0);
+                    s1 = fma(Gs[r * kc + kk + 1], Vs[(kk + 1) * nc + j], s1);
+                }
+                if (kk < kc) s0 = fma(Gs[r * kc + kk], Vs[kk * nc + j], s0);
+                pb[(size_t)r * m + c0 + j] = s0 + s1;
+            }
+        } else {
+            // 1. the G record (digit slices + row exponents), one bulk copy
+            if (tid == 0) {
+                tc::mbar_expect_tx(&barG, rec_bytes);
+                tc::bulk_g2s(sG, C.gtc + tc_block_offset(w, K, blk), rec_bytes, &barG);
+                s_ok = 1;
+            }
+            if (tid < kTcN) s_vexp[tid] = tc::kExpZero;
+            __syncthreads();
+            // 2. the right-hand-side block (kc x nc), waiting on unsolved rows; column scales; digits
+            constexpr int kPer = (kP64 * kTcN + 127) / 128;
+            double v[kPer];
 #pragma unroll
-        for (int u = 0; u < kPer; ++u) {
-            const int e = tid + u * 128;
-            if (e < kc * nc) {
-                const int kk = e / nc, j = e - kk * nc;
-                float d[tc::kDigits];
-                tc::digits(v[u], s_vexp[j], d);
-                const int o = tc::tile_off(j, kk, kcp);
+            for (int u = 0; u < kPer; ++u) {
+                const int e = tid + u * 128;
+                double val = 0.0;
+                if (e < kc * nc) {
+                    const int kk = e / nc, j = e - kk * nc, k = k0 + kk;
+                    val = k < w ? b[(size_t)(a + k) * m + c0 + j] : ld_relaxed(x + (size_t)C.rect[k - w] * m + c0 + j);
+                }
+                v[u] = val;
+            }
 #pragma unroll
-                for (int p = 0; p < tc::kDigits; ++p) *(__nv_bfloat16*)(sV + p * vtile + o) = __float2bfloat16(d[p]);
+            for (int u = 0; u < kPer; ++u) {
+                const int e = tid + u * 128;
+                if (e < kc * nc) {
+                    const int kk = e / nc, j = e - kk * nc, k = k0 + kk;
+                    if (k >= w && Pend<double>::is(v[u]) &&
+                        !wait_ready<double>(x + (size_t)C.rect[k - w] * m + c0 + j, v[u], ctl, budget)) {
+                        s_ok = 0;
+                        v[u] = 0.0;
+                    }
+                    atomicMax(&s_vexp[j], tc::exp_bound(v[u]));
+                }
             }
-        }
-        // zero digits of the padding (columns nc .. N, rows kc .. kcp)
-        for (int e = tid; e < N * kcp; e += 128) {
-            const int j = e / kcp, kk = e - j * kcp;
-            if (j >= nc || kk >= kc) {
-                const int o = tc::tile_off(j, kk, kcp);
+            __syncthreads();
+            const size_t vtile = (size_t)N * kcp * 2;
 #pragma unroll
-                for (int p = 0; p < tc::kDigits; ++p) *(__nv_bfloat16*)(sV + p * vtile + o) = __float2bfloat16(0.f);
+            for (int u = 0; u < kPer; ++u) {
+                const int e = tid + u * 128;
+                if (e < kc * nc) {
+                    const int kk = e / nc, j = e - kk * nc;
+                    float d[tc::kDigits];
+                    tc::digits(v[u], s_vexp[j], d);
+                    const int o = tc::tile_off(j, kk, kcp);
+#pragma unroll
+                    for (int p = 0; p < tc::kDigits; ++p) *(__nv_bfloat16*)(sV + p * vtile + o) = __float2bfloat16(d[p]);
+                }
             }
-        }
-        tc::fence_async_smem();
-        const bool ok = !__syncthreads_or(!s_ok);
-        if (!ok) {
-            if (tid == 0) tc::mbar_drain(&barG, phase, budget);  // the copy this CTA started ends first
-            break;
-        }
-        // 3. the MMAs: accumulator k - 2 of the 20 stacked pairs (p odd, q = k - p), once every thread
-        //    has seen the G record land (its row exponents are read below)
-        {
-            const bool got = tc::mbar_wait(&barG, phase, ctl, budget);
-            if (!got) {
-                tc::mbar_drain(&barG, phase, budget);
-                s_ok = 0;
+            // zero digits of the padding (columns nc .. N, rows kc .. kcp)
+            for (int e = tid; e < N * kcp; e += 128) {
+                const int j = e / kcp, kk = e - j * kcp;
+                if (j >= nc || kk >= kc) {
+                    const int o = tc::tile_off(j, kk, kcp);
+#pragma unroll
+                    for (int p = 0; p < tc::kDigits; ++p) *(__nv_bfloat16*)(sV + p * vtile + o) = __float2bfloat16(0.f);
+                }
             }
-        }
-        if (__syncthreads_or(!s_ok)) break;
-        if (tid == 0) {
+            tc::fence_async_smem();
+            const bool ok = !__syncthreads_or(!s_ok);
+            if (!ok) {
+                if (tid == 0) tc::mbar_drain(&barG, phase, budget);  // the copy this CTA started ends first
+                break;
+            }
+            // 3. the MMAs: accumulator k - 2 of the 20 stacked pairs (p odd, q = k - p), once every thread
+            //    has seen the G record land (its row exponents are read below)
             {
-                tc::fence_after();
-                const uint32_t sbo = (uint32_t)kcp * 16;
-                const uint32_t tileA = (uint32_t)kTcRows * kcp * 2;
-                const uint32_t id = tc::idesc_bf16_f32(128, N);
-                const uint32_t gA = tc::smem(sG), gB = tc::smem(sV);
-                for (int k = 2; k <= 9; ++k) {
-                    uint32_t acc = 0;
-                    for (int p = 1; p <= 7; p += 2) {
-                        const int q = k - p;
-                        if (q < 1 || q > tc::kDigits) continue;
-                        for (int ks = 0; ks < kcp / 16; ++ks) {
-                            const uint64_t da = tc::desc(gA + (p - 1) * tileA + ks * 256, 128, sbo);
-                            const uint64_t db = tc::desc(gB + (q - 1) * (uint32_t)vtile + ks * 256, 128, sbo);
-                            tc::mma_bf16(tmem + (uint32_t)(k - 2) * kTcN, da, db, id, acc);
-                            acc = 1;
+                const bool got = tc::mbar_wait(&barG, phase, ctl, budget);
+                if (!got) {
+                    tc::mbar_drain(&barG, phase, budget);
+                    s_ok = 0;
+                }
+            }
+            if (__syncthreads_or(!s_ok)) break;
+            if (tid == 0) {
+                {
+                    tc::fence_after();
+                    const uint32_t sbo = (uint32_t)kcp * 16;
+                    const uint32_t tileA = (uint32_t)kTcRows * kcp * 2;
+                    const uint32_t id = tc::idesc_bf16_f32(128, N);
+                    const uint32_t gA = tc::smem(sG), gB = tc::smem(sV);
+                    for (int k = 2; k <= 9; ++k) {
+                        uint32_t acc = 0;
+                        for (int p = 1; p <= 7; p += 2) {
+                            const int q = k - p;
+                            if (q < 1 || q > tc::kDigits) continue;
+                            for (int ks = 0; ks < kcp / 16; ++ks) {
+                                const uint64_t da = tc::desc(gA + (p - 1) * tileA + ks * 256, 128, sbo);
+                                const uint64_t db = tc::desc(gB + (q - 1) * (uint32_t)vtile + ks * 256, 128, sbo);
+                                tc::mma_bf16(tmem + (uint32_t)(k - 2) * kTcN, da, db, id, acc);
+                                acc = 1;
+                            }
                         }
                     }
-                }
-                tc::mma_commit(&barM);
-            }
-        }
-        {
-            // every thread waits for the MMAs (the wait has its own bound; a timeout is recorded)
-            const bool got = tc::mbar_wait(&barM, phase, ctl, budget);
-            if (!got) tc::mbar_drain(&barM, phase, budget);
-            if (!got) s_ok = 0;
-        }
-        tc::fence_after();
-        // 4. combine the accumulators in FP64: lane R = 32 warp + lane of TMEM, R < 64 the top half
-        const int R = 32 * warp + lane;
-        const bool top = R < kTcRows;
-        const int r = top ? R : R - kTcRows;
-        double accd[kTcN];
-#pragma unroll
-        for (int j = 0; j < kTcN; ++j) accd[j] = 0.0;
-        for (int k = 9; k >= 2; --k) {
-            float f[16];
-            tc::tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(k - 2) * kTcN, f);
-            const double sc = ldexp(1.0, -tc::kDigitBits * (top ? k : k + 1));
-#pragma unroll
-            for (int j = 0; j < kTcN; ++j) accd[j] = fma((double)f[j], sc, accd[j]);
-        }
-        tc::fence_before();
-        if (!top) {
-#pragma unroll
-            for (int j = 0; j < kTcN; ++j) red[r * kTcN + j] = accd[j];
-        }
-        if (__syncthreads_or(!s_ok)) break;
-        if (top && r < pw) {
-            const int er = reinterpret_cast<const int*>(sG + (size_t)tc::kDigits * kTcRows * kcp * 2)[r];
-#pragma unroll
-            for (int j = 0; j < kTcN; ++j) {
-                if (j < nc) {
-                    const int fj = s_vexp[j];
-                    const double vsum = accd[j] + red[r * kTcN + j];
-                    pb[(size_t)r * m + c0 + j] =
-                        (er == tc::kExpZero || fj == tc::kExpZero) ? 0.0 : ldexp(vsum, er + fj);
+                    tc::mma_commit(&barM);
                 }
             }
+            {
+                // every thread waits for the MMAs (the wait has its own bound; a timeout is recorded)
+                const bool got = tc::mbar_wait(&barM, phase, ctl, budget);
+                if (!got) tc::mbar_drain(&barM, phase, budget);
+                if (!got) s_ok = 0;
+            }
+            tc::fence_after();
+            // 4. combine the accumulators in FP64: lane R = 32 warp + lane of TMEM, R < 64 the top half
+            const int R = 32 * warp + lane;
+            const bool top = R < kTcRows;
+            const int r = top ? R : R - kTcRows;
+            double accd[kTcN];
+#pragma unroll
+            for (int j = 0; j < kTcN; ++j) accd[j] = 0.0;
+            for (int k = 9; k >= 2; --k) {
+                float f[16];
+                tc::tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(k - 2) * kTcN, f);
+                const double sc = ldexp(1.0, -tc::kDigitBits * (top ? k : k + 1));
+#pragma unroll
+                for (int j = 0; j < kTcN; ++j) accd[j] = fma((double)f[j], sc, accd[j]);
+            }
+            tc::fence_before();
+            if (!top) {
+#pragma unroll
+                for (int j = 0; j < kTcN; ++j) red[r * kTcN + j] = accd[j];
+            }
+            if (__syncthreads_or(!s_ok)) break;
+            if (top && r < pw) {
+                const int er = reinterpret_cast<const int*>(sG + (size_t)tc::kDigits * kTcRows * kcp * 2)[r];
+#pragma unroll
+                for (int j = 0; j < kTcN; ++j) {
+                    if (j < nc) {
+                        const int fj = s_vexp[j];
+                        const double vsum = accd[j] + red[r * kTcN + j];
+                        pb[(size_t)r * m + c0 + j] =
+                            (er == tc::kExpZero || fj == tc::kExpZero) ? 0.0 : ldexp(vsum, er + fj);
+                    }
+                }
+            }
+            phase ^= 1u;
         }
         __threadfence();  // this thread's partial sums visible before the count moves
         __syncthreads();
@@ -354,3 +393,10 @@ int launch_tc_split(const BChunk* panels, const int2* recs, int nrec, int sm_cou
 }
 
 }  // namespace sptrsv
+
+extern "C" int sptrsv_set_panels_mode(int mode) {
+    if (mode != 0 && mode != 1) return SPTRSV_ERR_INVALID_ARG;
+    const int prev = sptrsv::panels_mode();
+    sptrsv::g_panels_mode = mode;
+    return prev;
+}

@@ -366,13 +366,21 @@ k_window(int n, const int* __restrict__ rp, const int* __restrict__ col, const T
             walk();
             if (k <= s) finish();
         }
-        // the remaining entries (the first is pending) in registers when they are few: a round is
-        // then two polls, at most two FMAs and a shift
-        constexpr int RS = 6;
+        // the remaining entries (the first is pending) in registers when they are few.  A round is
+        // then branch-free: one ballot of the finished lanes, two shuffles that hand every lane the
+        // values of its next two in-block dependencies (rows of this block are lanes of this warp),
+        // two ring polls for dependencies in other blocks, at most two FMAs and a register shift.
+        // An in-block hop costs one round and no shared-memory round trip.
+        constexpr int RS = 16;
         int cs[RS];
         T ws[RS];
         int nrem = 0;
         bool lean = false;
+        T xm = T(0);  // this lane's value once its row is finished (what the shuffles hand over)
+        if (done && i >= lo) {
+            if constexpr (kLevels) xm = T(1) + acc;
+            else xm = Pend<T>::fix(scaled ? p : fma(-acc, di, bd));
+        }
         if (!done && k - s <= RS) {
             lean = true;
             nrem = k - s;
@@ -387,43 +395,73 @@ k_window(int n, const int* __restrict__ rp, const int* __restrict__ col, const T
         uint64_t t0 = budget < 1000000 ? gtimer() : 0;
         unsigned it = 0;
         bool fail = false;
-        while (!__all_sync(0xffffffffu, done || fail)) {
+        for (;;) {
+            const unsigned dm = __ballot_sync(0xffffffffu, done || fail);
+            if (dm == 0xffffffffu) break;
             prog = false;
-            if (!done) {
-                if (lean) {
-                    const T x0 = cs[0] >= far ? win_ld<T, kWeak>(x + cs[0]) : vring[cs[0] & RM];
-                    const T x1 = nrem > 1 ? (cs[1] >= far ? win_ld<T, kWeak>(x + cs[1]) : vring[cs[1] & RM])
-                                          : WinVal<T>::pending();
-                    if (!WinVal<T>::is_pending(x0)) {
-                        const bool two = nrem > 1 && !WinVal<T>::is_pending(x1);
-                        if constexpr (kLevels) {
-                            acc = max(acc, x0);
-                            if (two) acc = max(acc, x1);
-                        } else {
-                            p = fma(ws[0], x0, p);
-                            if (two) p = fma(ws[1], x1, p);
-                        }
-                        if (two) {
-                            nrem -= 2;
-#pragma unroll
-                            for (int q = 0; q + 2 < RS; ++q) {
-                                cs[q] = cs[q + 2];
-                                ws[q] = ws[q + 2];
-                            }
-                        } else {
-                            nrem -= 1;
-#pragma unroll
-                            for (int q = 0; q + 1 < RS; ++q) {
-                                cs[q] = cs[q + 1];
-                                ws[q] = ws[q + 1];
-                            }
-                        }
-                        prog = true;
-                        if (nrem == 0) finish();
-                    }
+            const bool act = !done && lean;
+            // slot 0 and slot 1: in this block (a shuffle from the row's lane) or elsewhere (ring)
+            const int c0 = cs[0], c1 = cs[1];
+            const bool in0 = act && nrem > 0 && c0 < top, in1 = act && nrem > 1 && c1 < top;
+            const int src0 = in0 ? top - 1 - c0 : lane, src1 = in1 ? top - 1 - c1 : lane;
+            const T s0 = __shfl_sync(0xffffffffu, xm, src0);
+            const T s1 = __shfl_sync(0xffffffffu, xm, src1);
+            if (act) {
+                T v0, v1 = T(0);
+                bool r0, r1 = false;
+                if (in0) {
+                    v0 = s0;
+                    r0 = (dm >> src0) & 1u;
                 } else {
-                    walk();
-                    if (k <= s) finish();
+                    v0 = c0 >= far ? win_ld<T, kWeak>(x + c0) : vring[c0 & RM];
+                    r0 = !WinVal<T>::is_pending(v0);
+                }
+                if (nrem > 1) {
+                    if (in1) {
+                        v1 = s1;
+                        r1 = (dm >> src1) & 1u;
+                    } else {
+                        v1 = c1 >= far ? win_ld<T, kWeak>(x + c1) : vring[c1 & RM];
+                        r1 = !WinVal<T>::is_pending(v1);
+                    }
+                }
+                if (r0) {
+                    const bool two = r1;
+                    if constexpr (kLevels) {
+                        acc = max(acc, v0);
+                        if (two) acc = max(acc, v1);
+                    } else {
+                        p = fma(ws[0], v0, p);
+                        if (two) p = fma(ws[1], v1, p);
+                    }
+                    if (two) {
+                        nrem -= 2;
+#pragma unroll
+                        for (int q = 0; q + 2 < RS; ++q) {
+                            cs[q] = cs[q + 2];
+                            ws[q] = ws[q + 2];
+                        }
+                    } else {
+                        nrem -= 1;
+#pragma unroll
+                        for (int q = 0; q + 1 < RS; ++q) {
+                            cs[q] = cs[q + 1];
+                            ws[q] = ws[q + 1];
+                        }
+                    }
+                    prog = true;
+                    if (nrem == 0) {
+                        finish();
+                        if constexpr (kLevels) xm = T(1) + acc;
+                        else xm = Pend<T>::fix(p);
+                    }
+                }
+            } else if (!done) {
+                walk();
+                if (k <= s) {
+                    finish();
+                    if constexpr (kLevels) xm = T(1) + acc;
+                    else xm = Pend<T>::fix(scaled ? p : fma(-acc, di, bd));
                 }
             }
             if (backoff_ns > 0 && !__any_sync(0xffffffffu, prog)) __nanosleep(backoff_ns);
@@ -496,9 +534,9 @@ static int window_dispatch(int n, const int* rp, const int* col, const T* val, c
     const int bo = window_backoff_ns();
     switch (window_warps()) {
         case 2: return window_launch<T, 2>(n, rp, col, val, invd, b, x, ctl, budget, bo, st, launches);
-        case 4: return window_launch<T, 4>(n, rp, col, val, invd, b, x, ctl, budget, bo, st, launches);
         case 16: return window_launch<T, 16>(n, rp, col, val, invd, b, x, ctl, budget, bo, st, launches);
-        default: return window_launch<T, 8>(n, rp, col, val, invd, b, x, ctl, budget, bo, st, launches);
+        case 8: return window_launch<T, 8>(n, rp, col, val, invd, b, x, ctl, budget, bo, st, launches);
+        default: return window_launch<T, 4>(n, rp, col, val, invd, b, x, ctl, budget, bo, st, launches);
     }
 }
 
@@ -507,8 +545,8 @@ static int window_dispatch(int n, const int* rp, const int* col, const T* val, c
 int window_warps() {
     static int w = [] {
         const char* e = getenv("SPTRSV_WINDOW_WARPS");
-        const int v = e ? atoi(e) : 8;
-        return (v == 2 || v == 4 || v == 8 || v == 16) ? v : 8;
+        const int v = e ? atoi(e) : 4;
+        return (v == 2 || v == 4 || v == 8 || v == 16) ? v : 4;
     }();
     return w;
 }
