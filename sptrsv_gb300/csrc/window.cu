@@ -73,7 +73,9 @@ template <typename T, int W> struct WinLayout {
     static constexpr bool kLevels = std::is_same<T, int>::value;
     static constexpr int kRpSlot = 36;  // 33 row pointers, padded to 16 bytes
     static constexpr size_t kFixed = (size_t)kWinRing * sizeof(T) + kWinFlags * sizeof(int);
-    static constexpr size_t kPerWarpFixed = 3 * kRpSlot * sizeof(int) + (kLevels ? 0 : 2 * 2 * 32 * sizeof(T));
+    static constexpr int kQueue = 16;  // pending entries per lane held in its queue
+    static constexpr size_t kPerWarpFixed = 3 * kRpSlot * sizeof(int) + (kLevels ? 0 : 2 * 2 * 32 * sizeof(T)) +
+                                            (size_t)kQueue * 32 * (sizeof(int) + (kLevels ? 0 : sizeof(T)));
     static constexpr size_t kPerEntry = 2 * (sizeof(int) + (kLevels ? 0 : sizeof(T)));
     // entries per buffer: what the budget leaves, a multiple of 32
     static constexpr int kCap = (int)(((kWinSmemBudget - kFixed) / W - kPerWarpFixed) / kPerEntry) / 32 * 32;
@@ -106,6 +108,8 @@ template <typename T, int W> struct WinStage {
     int* rp;   // [3][kRpSlot]
     T* inv;    // [2][32]
     T* bb;     // [2][32]
+    T* qw;     // [kQueue][32] scaled weights of the pending entries (lane-minor)
+    int* qc;   // [kQueue][32] their columns
     int* col;  // [2][kCap]
     T* val;    // [2][kCap]
     __device__ WinStage(char* base) {
@@ -116,9 +120,13 @@ template <typename T, int W> struct WinStage {
             inv = (T*)p;
             bb = inv + 64;
             p += 2 * 2 * 32 * sizeof(T);
+            qw = (T*)p;
+            p += (size_t)L::kQueue * 32 * sizeof(T);
         } else {
-            inv = bb = nullptr;
+            inv = bb = qw = nullptr;
         }
+        qc = (int*)p;
+        p += (size_t)L::kQueue * 32 * sizeof(int);
         col = (int*)p;
         p += 2 * (size_t)L::kCap * sizeof(int);
         val = L::kLevels ? nullptr : (T*)p;
@@ -366,29 +374,33 @@ k_window(int n, const int* __restrict__ rp, const int* __restrict__ col, const T
             walk();
             if (k <= s) finish();
         }
-        // the remaining entries (the first is pending) in registers when they are few.  A round is
-        // then branch-free: one ballot of the finished lanes, two shuffles that hand every lane the
-        // values of its next two in-block dependencies (rows of this block are lanes of this warp),
-        // two ring polls for dependencies in other blocks, at most two FMAs and a register shift.
-        // An in-block hop costs one round and no shared-memory round trip.
-        constexpr int RS = 16;
-        int cs[RS];
-        T ws[RS];
-        int nrem = 0;
+        // the remaining entries (the first is pending) go to the lane's queue in shared memory when
+        // they are few.  A round is then branch-free: one ballot of the finished lanes, two shuffles
+        // that hand every lane the values of its next two in-block dependencies (rows of this block
+        // are lanes of this warp), two ring polls for dependencies in other blocks, at most two FMAs
+        // and a head move; an in-block hop costs one round and no shared-memory round trip.
+        constexpr int RS = L::kQueue;
+        int nrem = 0, h = 0;
         bool lean = false;
         T xm = T(0);  // this lane's value once its row is finished (what the shuffles hand over)
         if (done && i >= lo) {
             if constexpr (kLevels) xm = T(1) + acc;
             else xm = Pend<T>::fix(scaled ? p : fma(-acc, di, bd));
         }
+        int c0 = 0, c1 = 0;
+        T w0 = T(0), w1 = T(0);
         if (!done && k - s <= RS) {
             lean = true;
             nrem = k - s;
-#pragma unroll
-            for (int q = 0; q < RS; ++q) {
-                cs[q] = q < nrem ? ecol(k - q) : 0;
-                if constexpr (kLevels) ws[q] = 0;
-                else ws[q] = q < nrem ? -eval(k - q) * di : T(0);
+            for (int q = 0; q < nrem; ++q) {
+                S.qc[q * 32 + lane] = ecol(k - q);
+                if constexpr (!kLevels) S.qw[q * 32 + lane] = -eval(k - q) * di;
+            }
+            c0 = S.qc[lane];
+            c1 = nrem > 1 ? S.qc[32 + lane] : 0;
+            if constexpr (!kLevels) {
+                w0 = S.qw[lane];
+                w1 = nrem > 1 ? S.qw[32 + lane] : T(0);
             }
         }
         // the budget's timer starts at the block for short budgets, else at round 31 of the block
@@ -400,9 +412,7 @@ k_window(int n, const int* __restrict__ rp, const int* __restrict__ col, const T
             if (dm == 0xffffffffu) break;
             prog = false;
             const bool act = !done && lean;
-            // slot 0 and slot 1: in this block (a shuffle from the row's lane) or elsewhere (ring)
-            const int c0 = cs[0], c1 = cs[1];
-            const bool in0 = act && nrem > 0 && c0 < top, in1 = act && nrem > 1 && c1 < top;
+            const bool in0 = act && c0 < top, in1 = act && nrem > 1 && c1 < top;
             const int src0 = in0 ? top - 1 - c0 : lane, src1 = in1 ? top - 1 - c1 : lane;
             const T s0 = __shfl_sync(0xffffffffu, xm, src0);
             const T s1 = __shfl_sync(0xffffffffu, xm, src1);
@@ -426,34 +436,28 @@ k_window(int n, const int* __restrict__ rp, const int* __restrict__ col, const T
                     }
                 }
                 if (r0) {
-                    const bool two = r1;
+                    const int used = r1 ? 2 : 1;
                     if constexpr (kLevels) {
                         acc = max(acc, v0);
-                        if (two) acc = max(acc, v1);
+                        if (r1) acc = max(acc, v1);
                     } else {
-                        p = fma(ws[0], v0, p);
-                        if (two) p = fma(ws[1], v1, p);
+                        p = fma(w0, v0, p);
+                        if (r1) p = fma(w1, v1, p);
                     }
-                    if (two) {
-                        nrem -= 2;
-#pragma unroll
-                        for (int q = 0; q + 2 < RS; ++q) {
-                            cs[q] = cs[q + 2];
-                            ws[q] = ws[q + 2];
-                        }
-                    } else {
-                        nrem -= 1;
-#pragma unroll
-                        for (int q = 0; q + 1 < RS; ++q) {
-                            cs[q] = cs[q + 1];
-                            ws[q] = ws[q + 1];
-                        }
-                    }
+                    nrem -= used;
+                    h += used;
                     prog = true;
                     if (nrem == 0) {
                         finish();
                         if constexpr (kLevels) xm = T(1) + acc;
                         else xm = Pend<T>::fix(p);
+                    } else {
+                        c0 = S.qc[h * 32 + lane];
+                        c1 = nrem > 1 ? S.qc[(h + 1) * 32 + lane] : 0;
+                        if constexpr (!kLevels) {
+                            w0 = S.qw[h * 32 + lane];
+                            w1 = nrem > 1 ? S.qw[(h + 1) * 32 + lane] : T(0);
+                        }
                     }
                 }
             } else if (!done) {
