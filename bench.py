@@ -85,6 +85,7 @@ def parse():
     ap.add_argument("--panels", default="fp64", choices=["fp64", "tc"],
                     help="panel products of the exact FP64 supernodal / batched schedules: FP64 FMAs or the tensor "
                          "cores (BF16 digit slices, FP64-accurate)")
+    ap.add_argument("--rhs", default="1,8,32,128", help="supernodal: right-hand-side counts (comma list)")
     ap.add_argument("--plain-schedule", default=None, choices=["syncfree_block", "syncfree_window", "syncfree_warp"],
                     help="default workload: the plain FP64 sync-free baseline's schedule")
     return ap.parse_args()
@@ -892,7 +893,7 @@ def run_supernodal(args, dist):
     rows = []
     pad = None  # the padded format of the BLAS-supernodal CPU path (core.cpp:136-161), built once
     rpu = m.row_ptr.astype(np.uint64)
-    for rhs in (1, 8, 32, 128):
+    for rhs in [int(v) for v in args.rhs.split(",")]:
         b = gen.uniform(3 + rhs, m.n * rhs)
         ref = oracle.base_gauss_upper(rpu, m.col, m.val, b, rhs)
         # two correct FP64 solves differing only in summation order lie this far apart elementwise

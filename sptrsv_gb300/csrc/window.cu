@@ -389,7 +389,7 @@ k_window(int n, const int* __restrict__ rp, const int* __restrict__ col, const T
         }
         int c0 = 0, c1 = 0;
         T w0 = T(0), w1 = T(0);
-        if (!done && k - s <= RS) {
+        if (!done && k - s <= RS && c < far) {  // queued entries then all lie within the ring's reach
             lean = true;
             nrem = k - s;
             for (int q = 0; q < nrem; ++q) {
@@ -411,56 +411,43 @@ k_window(int n, const int* __restrict__ rp, const int* __restrict__ col, const T
             const unsigned dm = __ballot_sync(0xffffffffu, done || fail);
             if (dm == 0xffffffffu) break;
             prog = false;
+            // straight-line for every lane (results of lanes with nothing to do are discarded):
+            // the values of the next two queued entries from a shuffle (in this block) or the ring
             const bool act = !done && lean;
-            const bool in0 = act && c0 < top, in1 = act && nrem > 1 && c1 < top;
-            const int src0 = in0 ? top - 1 - c0 : lane, src1 = in1 ? top - 1 - c1 : lane;
+            const bool in0 = c0 < top, in1 = c1 < top;
+            const int src0 = in0 ? (top - 1 - c0) & 31 : lane, src1 = in1 ? (top - 1 - c1) & 31 : lane;
             const T s0 = __shfl_sync(0xffffffffu, xm, src0);
             const T s1 = __shfl_sync(0xffffffffu, xm, src1);
-            if (act) {
-                T v0, v1 = T(0);
-                bool r0, r1 = false;
-                if (in0) {
-                    v0 = s0;
-                    r0 = (dm >> src0) & 1u;
-                } else {
-                    v0 = c0 >= far ? win_ld<T, kWeak>(x + c0) : vring[c0 & RM];
-                    r0 = !WinVal<T>::is_pending(v0);
+            const T g0 = vring[c0 & RM], g1 = vring[c1 & RM];
+            const T v0 = in0 ? s0 : g0, v1 = in1 ? s1 : g1;
+            const bool r0 = act && (in0 ? ((dm >> src0) & 1u) != 0 : !WinVal<T>::is_pending(g0));
+            const bool r1 = r0 && nrem > 1 && (in1 ? ((dm >> src1) & 1u) != 0 : !WinVal<T>::is_pending(g1));
+            if constexpr (kLevels) {
+                acc = r0 ? max(acc, v0) : acc;
+                acc = r1 ? max(acc, v1) : acc;
+            } else {
+                p = r0 ? fma(w0, v0, p) : p;
+                p = r1 ? fma(w1, v1, p) : p;
+            }
+            const int used = (int)r0 + (int)r1;
+            nrem -= used;
+            h += used;
+            {
+                const int h0 = min(h, RS - 1), h1 = min(h + 1, RS - 1);
+                c0 = S.qc[h0 * 32 + lane];
+                c1 = S.qc[h1 * 32 + lane];
+                if constexpr (!kLevels) {
+                    w0 = S.qw[h0 * 32 + lane];
+                    w1 = S.qw[h1 * 32 + lane];
                 }
-                if (nrem > 1) {
-                    if (in1) {
-                        v1 = s1;
-                        r1 = (dm >> src1) & 1u;
-                    } else {
-                        v1 = c1 >= far ? win_ld<T, kWeak>(x + c1) : vring[c1 & RM];
-                        r1 = !WinVal<T>::is_pending(v1);
-                    }
-                }
-                if (r0) {
-                    const int used = r1 ? 2 : 1;
-                    if constexpr (kLevels) {
-                        acc = max(acc, v0);
-                        if (r1) acc = max(acc, v1);
-                    } else {
-                        p = fma(w0, v0, p);
-                        if (r1) p = fma(w1, v1, p);
-                    }
-                    nrem -= used;
-                    h += used;
-                    prog = true;
-                    if (nrem == 0) {
-                        finish();
-                        if constexpr (kLevels) xm = T(1) + acc;
-                        else xm = Pend<T>::fix(p);
-                    } else {
-                        c0 = S.qc[h * 32 + lane];
-                        c1 = nrem > 1 ? S.qc[(h + 1) * 32 + lane] : 0;
-                        if constexpr (!kLevels) {
-                            w0 = S.qw[h * 32 + lane];
-                            w1 = nrem > 1 ? S.qw[(h + 1) * 32 + lane] : T(0);
-                        }
-                    }
-                }
-            } else if (!done) {
+            }
+            prog = used > 0;
+            if (r0 && nrem == 0) {
+                finish();
+                if constexpr (kLevels) xm = T(1) + acc;
+                else xm = Pend<T>::fix(p);
+            }
+            if (!done && !lean) {
                 walk();
                 if (k <= s) {
                     finish();
