@@ -321,6 +321,24 @@ __global__ void k_level_hist(int n, const int* __restrict__ level, int* __restri
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) atomicAdd(&cnt[level[i]], 1);
 }
 
+// Passes over the levels of a level-set solve: out[0] = sum over levels of ceil(width / 32) (one
+// CTA of 32 warps, a warp per row), out[1] = the same with 32 x `ctas` warps (the full grid).
+__global__ void k_level_passes(int max_level, const int* __restrict__ lptr, int ctas, unsigned long long* out) {
+    const int l = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    unsigned p1 = 0, pg = 0;
+    if (l <= max_level) {
+        const unsigned w = (unsigned)(lptr[l + 1] - lptr[l]);
+        p1 = (w + 31) / 32;
+        pg = (w + 32u * ctas - 1) / (32u * ctas);
+    }
+    p1 = __reduce_add_sync(0xffffffffu, p1);
+    pg = __reduce_add_sync(0xffffffffu, pg);
+    if ((threadIdx.x & 31) == 0 && p1) {
+        atomicAdd(&out[0], (unsigned long long)p1);
+        atomicAdd(&out[1], (unsigned long long)pg);
+    }
+}
+
 __global__ void k_level_tasks(int max_level, const int* __restrict__ lptr, const int* __restrict__ lrows,
                               const int* __restrict__ rp, int T, int* __restrict__ tasks) {
     for (int l = blockIdx.x * blockDim.x + threadIdx.x; l <= max_level; l += gridDim.x * blockDim.x) {

@@ -180,7 +180,19 @@ int Handle::ensure_levels() {
     while ((1ll << bits) <= (long long)max_level) ++bits;
     if ((rc = stable_sort_perm((const unsigned*)levels.p, n, bits, level_rows.as<int>(), scr, st, &launches)))
         return rc;
+    // level-set grid: one CTA when its cost model wins.  Measured on GB300: a level costs ~0.3 us of
+    // CTA barrier plus ~0.5 us per pass of 32 rows with one CTA; a grid barrier through L2 costs
+    // ~1.5 us (one GPU-scope acq_rel atomic per CTA, acquire polls) plus ~0.5 us per pass.
+    unsigned long long* passes = scr.take<unsigned long long>(2);
+    unsigned long long hp[2] = {0, 0};
+    CUDA_TRY(cudaMemsetAsync(passes, 0, sizeof(hp), st));
+    if (max_level > 0) {
+        k_level_passes<<<(max_level + 255) / 256, 256, 0, st>>>(max_level, level_ptr.as<int>(), sm_count, passes);
+        ++launches;
+    }
+    CUDA_TRY(cudaMemcpyAsync(hp, passes, sizeof(hp), cudaMemcpyDeviceToHost, st));
     CUDA_TRY(cudaStreamSynchronize(st));
+    levelset_one_cta = 0.3 * max_level + 0.5 * (double)hp[0] < 1.5 * max_level + 0.5 * (double)hp[1];
     levels_ready = true;
     return 0;
 }
@@ -431,10 +443,13 @@ int Handle::enqueue(const sptrsv_opts& o, const double* b, double* x, int rhs, i
                     return rc;
                 if ((rc = mark(SPTRSV_K_PUSH_CSC))) return rc;
                 break;
-            case SPTRSV_SCHED_LEVELSET:
-                if ((rc = launch_levelset(false, a, max_level, level_ptr.as<int>(), level_rows.as<int>()))) return rc;
+            case SPTRSV_SCHED_LEVELSET: {
+                SolveArgs al = a;
+                al.warps = levelset_warps(o);
+                if ((rc = launch_levelset(false, al, max_level, level_ptr.as<int>(), level_rows.as<int>()))) return rc;
                 if ((rc = mark(SPTRSV_K_LEVELSET))) return rc;
                 break;
+            }
             case SPTRSV_SCHED_SUPERNODAL:
                 if (!have_supernodes) return SPTRSV_ERR_SUPERNODES;
                 if ((rc = launch_fill_pending(false, xrm, (size_t)n * rhs, st, &launches))) return rc;
@@ -476,7 +491,8 @@ int Handle::enqueue(const sptrsv_opts& o, const double* b, double* x, int rhs, i
                 if ((rc = mark(SPTRSV_K_AXPY))) return rc;
             } else {
                 if ((rc = launch_exact_inner(ra, o.inner, o.rows_per_warp, 0, max_level, level_ptr.as<int>(),
-                                             level_rows.as<int>(), resident_warps(o))))
+                                             level_rows.as<int>(),
+                                             o.inner == SPTRSV_SCHED_LEVELSET ? levelset_warps(o) : resident_warps(o))))
                     return rc;
                 if ((rc = mark(SPTRSV_K_INNER))) return rc;
                 if ((rc = launch_axpy_pending(ra, 0))) return rc;
@@ -493,6 +509,13 @@ int Handle::enqueue(const sptrsv_opts& o, const double* b, double* x, int rhs, i
         if ((rc = mark(SPTRSV_K_TRANSPOSE))) return rc;
     }
     return 0;
+}
+
+// Warps of a level-set launch: the caller's or tuner's choice, else one CTA (32 warps) when the
+// level widths favour it, else the rows model below.
+int Handle::levelset_warps(const sptrsv_opts& o) const {
+    if (o.resident_warps > 0 || warps_override > 0) return resident_warps(o);
+    return levelset_one_cta ? 32 : resident_warps(o);
 }
 
 int Handle::resident_warps(const sptrsv_opts& o) const {

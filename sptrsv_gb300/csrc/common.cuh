@@ -29,8 +29,7 @@ struct Ctl {
     int status;            // first error (0 = ok)
     int abort;             // set when any waiter gives up
     int done;              // MIXED: residual reached the tolerance
-    unsigned int bar_count;  // grid barrier arrivals
-    unsigned int bar_gen;    // grid barrier generation
+    unsigned long long bar_count;  // grid barrier arrivals (monotonic within a solve)
     int steps;             // MIXED: refinement steps taken
     int max_level;         // analysis: largest level
     double rnorm2;         // MIXED: ||r||^2 of the last residual
@@ -152,24 +151,37 @@ __device__ __forceinline__ T warp_sum(T v, unsigned mask = 0xffffffffu) {
 }
 
 // Grid-wide barrier for a cooperative launch, bounded: returns false on timeout/abort.
+// Arrivals count up in ctl->bar_count and the count is never reset inside a solve: the k-th
+// arrival (from 0) belongs to barrier generation k / nblocks, which is complete once the count
+// reaches (k / nblocks + 1) * nblocks.  Every launch of a solve runs the same grid and passes the
+// same number of barriers in every CTA, so the count is a multiple of nblocks between launches
+// (the control block is cleared at the start of every solve).  One acq_rel atomic per CTA and
+// acquire polls of the same word: the last arrival releases everybody with its own add, with no
+// second store to wait for.
+__device__ __forceinline__ unsigned long long atom_add_acq_rel(unsigned long long* p, unsigned long long v) {
+    unsigned long long old;
+    asm volatile("atom.acq_rel.gpu.global.add.u64 %0, [%1], %2;" : "=l"(old) : "l"(p), "l"(v) : "memory");
+    return old;
+}
+__device__ __forceinline__ unsigned long long ld_acquire(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
 __device__ __forceinline__ bool grid_barrier(Ctl* ctl, unsigned nblocks, int64_t budget_ns) {
     __syncthreads();
+    if (nblocks == 1) return true;  // one CTA: the CTA barrier orders its global accesses
     __shared__ int s_ok;
     if (threadIdx.x == 0) {
         int ok = 1;
-        const unsigned gen = ld_acquire(&ctl->bar_gen);
-        __threadfence();
-        const unsigned arrived = atomicAdd(&ctl->bar_count, 1u);
-        if (arrived == nblocks - 1) {
-            atomicExch(&ctl->bar_count, 0u);
-            __threadfence();
-            st_release(&ctl->bar_gen, gen + 1);
-        } else {
+        const unsigned long long k = atom_add_acq_rel(&ctl->bar_count, 1ull);
+        const unsigned long long target = (k / nblocks + 1) * nblocks;
+        if (k + 1 != target) {
             // poll without sleeping first (a level usually ends within microseconds), then back off;
             // the timer and the abort flag are read every 64 polls
             uint64_t t0 = 0;
             unsigned it = 0;
-            while (ld_acquire(&ctl->bar_gen) == gen) {
+            while (ld_acquire(&ctl->bar_count) < target) {
                 if ((++it & 63u) == 0) {
                     if (aborted(ctl)) { ok = 0; break; }
                     if (t0 == 0) t0 = gtimer();

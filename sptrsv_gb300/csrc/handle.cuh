@@ -71,6 +71,7 @@ struct Handle {
     int n = 0, nnz = 0;
     bool analysed = false;
     bool levels_ready = false;
+    bool levelset_one_cta = false;  // the level-set solve's grid: one CTA (narrow levels) or the rows model
     const int* rp = nullptr;
     const int* col = nullptr;
     const double* val = nullptr;
@@ -157,6 +158,7 @@ struct Handle {
     int build_cond_graph(const sptrsv_opts& o, const double* b, double* x, double* x_out, int rhs, int layout,
                          cudaGraphExec_t* out, int64_t* fixed_kernels);
     int resident_warps(const sptrsv_opts& o) const;
+    int levelset_warps(const sptrsv_opts& o) const;
     int set_supernodes(int sn, const int* snodes_host);
     SnArgs sn_args() const;
     // autotuner state (tune.cu)

@@ -35,6 +35,7 @@ __global__ void k_row_stats(int n, const int* rp, const int* col, const double* 
 __global__ void k_levels(int n, const int* rp, const int* col, int* level, Ctl* ctl, int64_t budget);
 __global__ void k_level_hist(int n, const int* level, int* cnt);
 __global__ void k_level_tasks(int max_level, const int* lptr, const int* lrows, const int* rp, int T, int* tasks);
+__global__ void k_level_passes(int max_level, const int* lptr, int ctas, unsigned long long* out);
 __global__ void k_entry_rows(int n, const int* rp, int* erow);
 __global__ void k_gather_csc(int nnz, const int* perm, const int* erow, const double* val, int* crow, double* cval);
 __global__ void k_col_hist(int nnz, const int* col, int* cnt);

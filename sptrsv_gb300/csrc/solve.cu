@@ -266,7 +266,7 @@ __device__ __forceinline__ T ldcg(const T* p) { return __ldcg(p); }
 constexpr int kLevelsetThreads = 1024;  // one CTA per SM: a grid barrier takes one arrival per SM
 
 template <typename T>
-__global__ void __launch_bounds__(kLevelsetThreads) k_levelset(int n, int rhs, const int* __restrict__ rp, const int* __restrict__ col,
+__global__ void __launch_bounds__(kLevelsetThreads, 1) k_levelset(int n, int rhs, const int* __restrict__ rp, const int* __restrict__ col,
                                                   const T* __restrict__ val, const T* __restrict__ invd,
                                                   const T* __restrict__ b, T* x, int max_level,
                                                   const int* __restrict__ lptr, const int* __restrict__ lrows,
@@ -275,24 +275,71 @@ __global__ void __launch_bounds__(kLevelsetThreads) k_levelset(int n, int rhs, c
     const int lane = threadIdx.x & 31;
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
+    if (rhs == 1) {
+        // The matrix data of this warp's first row of a level (row index, row pointers, the first
+        // kPre x 32 entries, b_i and 1/U_ii) is loaded before the barrier that opens the level, so
+        // after the barrier a row waits only for its loads of x.
+        constexpr int kPre = 2;
+        int i = -1, s = 0, e = 0;
+        int pc[kPre];
+        T pv[kPre], pb = T(0), pd = T(0);
+        auto fetch = [&](int l) {
+            i = -1;
+            const int k = lptr[l] + gw;
+            if (k >= lptr[l + 1]) return;
+            i = lrows[k];
+            s = rp[i] + 1;
+            e = rp[i + 1];
+#pragma unroll
+            for (int u = 0; u < kPre; ++u) {
+                const int q = s + lane + 32 * u;
+                pc[u] = q < e ? col[q] : 0;
+                pv[u] = q < e ? val[q] : T(0);
+            }
+            pb = b[i];
+            pd = invd[i];
+        };
+        fetch(1);
+        // x of earlier levels: through L2 (written by other SMs), or through L1 when the grid is one
+        // CTA (its own stores, ordered by the CTA barrier)
+        const bool one = gridDim.x == 1;
+        auto ldx = [&](int c) -> T { return one ? x[c] : ldcg(x + c); };
+        for (int l = 1; l <= max_level; ++l) {
+            if (i >= 0) {
+                T sum = T(0);
+#pragma unroll
+                for (int u = 0; u < kPre; ++u)
+                    if (s + lane + 32 * u < e) sum = fma_t(pv[u], ldx(pc[u]), sum);
+                for (int q = s + 32 * kPre + lane; q < e; q += 32) sum = fma_t(val[q], ldx(col[q]), sum);
+                sum = warp_sum(sum);
+                if (lane == 0) x[i] = (pb - sum) * pd;
+                // more rows of this level for this warp (levels wider than the grid's warps)
+                for (int k = lptr[l] + gw + nw; k < lptr[l + 1]; k += nw) {
+                    const int r = lrows[k];
+                    T t = T(0);
+                    for (int q = rp[r] + 1 + lane; q < rp[r + 1]; q += 32) t = fma_t(val[q], ldx(col[q]), t);
+                    t = warp_sum(t);
+                    if (lane == 0) x[r] = (b[r] - t) * invd[r];
+                }
+            }
+            if (l < max_level) {
+                fetch(l + 1);
+                if (!grid_barrier(ctl, gridDim.x, budget)) return;
+            }
+        }
+        return;
+    }
     for (int l = 1; l <= max_level; ++l) {
         const int beg = lptr[l], end = lptr[l + 1];
         for (int k = beg + gw; k < end; k += nw) {
             const int i = lrows[k];
             const int s = rp[i], e = rp[i + 1];
-            if (rhs == 1) {
+            const T di = invd[i];
+            for (int c = lane; c < rhs; c += 32) {
                 T sum = T(0);
-                for (int q = s + 1 + lane; q < e; q += 32) sum = fma_t(val[q], ldcg(x + col[q]), sum);
-                sum = warp_sum(sum);
-                if (lane == 0) x[i] = (b[i] - sum) * invd[i];
-            } else {
-                const T di = invd[i];
-                for (int c = lane; c < rhs; c += 32) {
-                    T sum = T(0);
-                    for (int q = s + 1; q < e; ++q) sum = fma_t(val[q], ldcg(x + (size_t)col[q] * rhs + c), sum);
-                    const size_t p = (size_t)i * rhs + c;
-                    x[p] = (b[p] - sum) * di;
-                }
+                for (int q = s + 1; q < e; ++q) sum = fma_t(val[q], ldcg(x + (size_t)col[q] * rhs + c), sum);
+                const size_t p = (size_t)i * rhs + c;
+                x[p] = (b[p] - sum) * di;
             }
         }
         if (l < max_level && !grid_barrier(ctl, gridDim.x, budget)) return;

@@ -10,10 +10,10 @@
 //
 // Blocks: block t holds rows [n - 32(t+1), n - 32t) (the last one may be short); lane l of the
 // warp owning block t takes row n - 1 - 32t - l.  Warp w owns blocks w, w + W, w + 2W, ...
-// Every lane walks its CSR row from the right (largest column = solved earliest), consuming each
-// entry whose x is available, in warp lockstep: a round lets every lane consume what is ready,
-// then the warp polls again together (no lane spins alone in divergent code).  x of a column c is
-// read from the ring when c < top(t) + reach, else from global memory.
+// Every lane walks its CSR row from the right (largest column = solved earliest).  At the block's
+// start it consumes every entry that is already available; the rest go in warp lockstep rounds
+// of straight-line code, one entry per lane per round (no lane spins alone in divergent code).
+// x of a column c is read from the ring when c < top(t) + reach, else from global memory.
 //
 // Staging: a block's entries (when they fit kCap entries per buffer), its row pointers,
 // reciprocal diagonal and right-hand side are copied into the warp's shared buffers by cp.async
@@ -73,9 +73,7 @@ template <typename T, int W> struct WinLayout {
     static constexpr bool kLevels = std::is_same<T, int>::value;
     static constexpr int kRpSlot = 36;  // 33 row pointers, padded to 16 bytes
     static constexpr size_t kFixed = (size_t)kWinRing * sizeof(T) + kWinFlags * sizeof(int);
-    static constexpr int kQueue = 16;  // pending entries per lane held in its queue
-    static constexpr size_t kPerWarpFixed = 3 * kRpSlot * sizeof(int) + (kLevels ? 0 : 2 * 2 * 32 * sizeof(T)) +
-                                            (size_t)kQueue * 32 * (sizeof(int) + (kLevels ? 0 : sizeof(T)));
+    static constexpr size_t kPerWarpFixed = 3 * kRpSlot * sizeof(int) + (kLevels ? 0 : 2 * 2 * 32 * sizeof(T));
     static constexpr size_t kPerEntry = 2 * (sizeof(int) + (kLevels ? 0 : sizeof(T)));
     // entries per buffer: what the budget leaves, a multiple of 32
     static constexpr int kCap = (int)(((kWinSmemBudget - kFixed) / W - kPerWarpFixed) / kPerEntry) / 32 * 32;
@@ -108,8 +106,6 @@ template <typename T, int W> struct WinStage {
     int* rp;   // [3][kRpSlot]
     T* inv;    // [2][32]
     T* bb;     // [2][32]
-    T* qw;     // [kQueue][32] scaled weights of the pending entries (lane-minor)
-    int* qc;   // [kQueue][32] their columns
     int* col;  // [2][kCap]
     T* val;    // [2][kCap]
     __device__ WinStage(char* base) {
@@ -120,13 +116,9 @@ template <typename T, int W> struct WinStage {
             inv = (T*)p;
             bb = inv + 64;
             p += 2 * 2 * 32 * sizeof(T);
-            qw = (T*)p;
-            p += (size_t)L::kQueue * 32 * sizeof(T);
         } else {
-            inv = bb = qw = nullptr;
+            inv = bb = nullptr;
         }
-        qc = (int*)p;
-        p += (size_t)L::kQueue * 32 * sizeof(int);
         col = (int*)p;
         p += 2 * (size_t)L::kCap * sizeof(int);
         val = L::kLevels ? nullptr : (T*)p;
@@ -167,21 +159,15 @@ __device__ __forceinline__ void win_stage_data(const WinStage<T, W>& S, int rs, 
     }
 }
 
-// x in global memory: rows of this CTA only.  kWeak: plain stores and loads, ordered by the
-// done-flag protocol's CTA fences (a reader only loads x of rows in finished blocks, after the
-// acquire fence that follows the flag); otherwise GPU-scope relaxed ones.
-template <typename T, bool kWeak>
-__device__ __forceinline__ T win_ld(const T* p) {
-    if constexpr (kWeak) return *p;
-    else return ld_relaxed(p);
-}
-template <typename T, bool kWeak>
-__device__ __forceinline__ void win_st(T* p, T v) {
-    if constexpr (kWeak) *p = v;
-    else st_relaxed(p, v);
-}
+// x in global memory: rows of this CTA only, plain stores and loads, ordered by the done-flag
+// protocol's CTA fences (a reader only loads x of rows in finished blocks, after the acquire fence
+// that follows the flag).  GPU-scope relaxed accesses measured no different.
+template <typename T>
+__device__ __forceinline__ T win_ld(const T* p) { return *p; }
+template <typename T>
+__device__ __forceinline__ void win_st(T* p, T v) { *p = v; }
 
-template <typename T, int W, bool kWeak>
+template <typename T, int W, bool kTwo>
 __global__ void __launch_bounds__(W * 32, 1)
 k_window(int n, const int* __restrict__ rp, const int* __restrict__ col, const T* __restrict__ val,
          const T* __restrict__ invd, const T* __restrict__ b, T* x, Ctl* ctl, int64_t budget, int backoff_ns) {
@@ -271,7 +257,7 @@ k_window(int n, const int* __restrict__ rp, const int* __restrict__ col, const T
         const int i = top - 1 - lane;
         const int far = top + reach;
         bool done = i < lo;
-        int s = 0, k = 0, c = 0;
+        int s = e0, k = e0, c = 0;  // a lane without a row (short last block) reads entry e0 harmlessly
         T v = T(0), acc = T(0), di = T(0), bd = T(0), vs = T(0), p = T(0);
         bool scaled = false;
         if (!done) {
@@ -302,7 +288,7 @@ k_window(int n, const int* __restrict__ rp, const int* __restrict__ col, const T
                     vq[q] = use[q] ? eval(kq) : T(0);
                 }
 #pragma unroll
-                for (int q = 0; q < 4; ++q) xq[q] = use[q] ? win_ld<T, kWeak>(x + cq[q]) : T(0);
+                for (int q = 0; q < 4; ++q) xq[q] = use[q] ? win_ld<T>(x + cq[q]) : T(0);
                 bool bad = false;
 #pragma unroll
                 for (int q = 0; q < 4; ++q) bad |= use[q] && WinVal<T>::is_pending(xq[q]);
@@ -323,12 +309,13 @@ k_window(int n, const int* __restrict__ rp, const int* __restrict__ col, const T
                 }
             }
         }
-        // the rest: one walk over what is ready, then lockstep rounds over the remaining entries
-        bool prog = false;
+        // the rest: one walk over what is ready, then lockstep rounds over the remaining entries.
+        // xm is this lane's value once its row is finished, the pending pattern before.
+        T xm = WinVal<T>::pending();
         // walk right to left consuming ready entries; stops at the first pending one
         auto walk = [&]() {
             while (k > s) {
-                const T xv = c >= far ? win_ld<T, kWeak>(x + c) : vring[c & RM];
+                const T xv = c >= far ? win_ld<T>(x + c) : vring[c & RM];
                 if (WinVal<T>::is_pending(xv)) {
                     if constexpr (!kLevels) {
                         if (!scaled) {  // from here on one FMA per term
@@ -339,7 +326,6 @@ k_window(int n, const int* __restrict__ rp, const int* __restrict__ col, const T
                     }
                     break;
                 }
-                prog = true;
                 if constexpr (kLevels) {
                     acc = max(acc, xv);
                 } else {
@@ -355,52 +341,45 @@ k_window(int n, const int* __restrict__ rp, const int* __restrict__ col, const T
                 }
             }
         };
-        auto publish = [&](T xi) {
-            vring[i & RM] = xi;
-            win_st<T, kWeak>(x + i, xi);
-            done = true;
-            prog = true;
-        };
         auto finish = [&]() {
             if constexpr (kLevels) {
-                const T xi = 1 + acc;
-                lmax = max(lmax, xi);
-                publish(xi);
+                xm = T(1) + acc;
+                lmax = max(lmax, xm);
             } else {
-                publish(Pend<T>::fix(scaled ? p : fma(-acc, di, bd)));
+                xm = Pend<T>::fix(scaled ? p : fma(-acc, di, bd));
             }
+            vring[i & RM] = xm;
+            win_st<T>(x + i, xm);
+            done = true;
         };
         if (!done) {
             walk();
             if (k <= s) finish();
         }
-        // the remaining entries (the first is pending) go to the lane's queue in shared memory when
-        // they are few.  A round is then branch-free: one ballot of the finished lanes, two shuffles
-        // that hand every lane the values of its next two in-block dependencies (rows of this block
-        // are lanes of this warp), two ring polls for dependencies in other blocks, at most two FMAs
-        // and a head move; an in-block hop costs one round and no shared-memory round trip.
-        constexpr int RS = L::kQueue;
-        int nrem = 0, h = 0;
-        bool lean = false;
-        T xm = T(0);  // this lane's value once its row is finished (what the shuffles hand over)
-        if (done && i >= lo) {
-            if constexpr (kLevels) xm = T(1) + acc;
-            else xm = Pend<T>::fix(scaled ? p : fma(-acc, di, bd));
-        }
-        int c0 = 0, c1 = 0;
-        T w0 = T(0), w1 = T(0);
-        if (!done && k - s <= RS && c < far) {  // queued entries then all lie within the ring's reach
-            lean = true;
-            nrem = k - s;
-            for (int q = 0; q < nrem; ++q) {
-                S.qc[q * 32 + lane] = ecol(k - q);
-                if constexpr (!kLevels) S.qw[q * 32 + lane] = -eval(k - q) * di;
-            }
-            c0 = S.qc[lane];
-            c1 = nrem > 1 ? S.qc[32 + lane] : 0;
-            if constexpr (!kLevels) {
-                w0 = S.qw[lane];
-                w1 = nrem > 1 ? S.qw[32 + lane] : T(0);
+        // The remaining entries, one per round (the head, entry k, is pending).  A round is the same
+        // straight-line code for every lane: the head's value from a shuffle when its row is in this
+        // block (rows of this block are lanes of this warp) and from the ring otherwise, its pending
+        // test, one FMA, and the move to the next entry, whose column and weight were loaded a round
+        // ahead.  A lane's own value xm holds the pending pattern until its row is finished, so the
+        // shuffled value itself says whether an in-block dependency is done.
+        // Registers hold the head (entry k: column c, scaled weight w = -U_ik / U_ii) and the next two
+        // entries (cn, wn: k-1; c2, w2: k-2), loaded a round ahead; indices past the row's start are
+        // clamped to a valid entry and never consumed.  kTwo: a round consumes up to two entries.
+        T w = T(0), wn = T(0), w2 = T(0);
+        int cn = 0, c2 = 0;
+        auto weight = [&](int q) -> T {
+            if constexpr (kLevels) return T(0);
+            else return -eval(q) * di;
+        };
+        if (!done) {
+            if constexpr (!kLevels) w = vs;
+            const int k1 = k - 1 > s ? k - 1 : k;
+            cn = ecol(k1);
+            wn = weight(k1);
+            if constexpr (kTwo) {
+                const int k2 = k - 2 > s ? k - 2 : k1;
+                c2 = ecol(k2);
+                w2 = weight(k2);
             }
         }
         // the budget's timer starts at the block for short budgets, else at round 31 of the block
@@ -408,54 +387,47 @@ k_window(int n, const int* __restrict__ rp, const int* __restrict__ col, const T
         unsigned it = 0;
         bool fail = false;
         for (;;) {
-            const unsigned dm = __ballot_sync(0xffffffffu, done || fail);
-            if (dm == 0xffffffffu) break;
-            prog = false;
-            // straight-line for every lane (results of lanes with nothing to do are discarded):
-            // the values of the next two queued entries from a shuffle (in this block) or the ring
-            const bool act = !done && lean;
-            const bool in0 = c0 < top, in1 = c1 < top;
-            const int src0 = in0 ? (top - 1 - c0) & 31 : lane, src1 = in1 ? (top - 1 - c1) & 31 : lane;
-            const T s0 = __shfl_sync(0xffffffffu, xm, src0);
-            const T s1 = __shfl_sync(0xffffffffu, xm, src1);
-            const T g0 = vring[c0 & RM], g1 = vring[c1 & RM];
-            const T v0 = in0 ? s0 : g0, v1 = in1 ? s1 : g1;
-            const bool r0 = act && (in0 ? ((dm >> src0) & 1u) != 0 : !WinVal<T>::is_pending(g0));
-            const bool r1 = r0 && nrem > 1 && (in1 ? ((dm >> src1) & 1u) != 0 : !WinVal<T>::is_pending(g1));
-            if constexpr (kLevels) {
-                acc = r0 ? max(acc, v0) : acc;
-                acc = r1 ? max(acc, v1) : acc;
+            if (__all_sync(0xffffffffu, done || fail)) break;
+            auto value = [&](int cc) -> T {
+                const T sv = __shfl_sync(0xffffffffu, xm, (top - 1 - cc) & 31);
+                T gv;
+                if (cc < far) gv = vring[cc & RM];
+                else gv = win_ld<T>(x + cc);  // a done block's row (not expected here)
+                return cc < top ? sv : gv;
+            };
+            const T x0 = value(c);
+            const bool rdy = !done && !WinVal<T>::is_pending(x0);
+            bool rdy1 = false;
+            if constexpr (kLevels) acc = rdy ? max(acc, x0) : acc;
+            else p = rdy ? fma(w, x0, p) : p;
+            if constexpr (kTwo) {
+                const T x1 = value(cn);
+                rdy1 = rdy && k - 1 > s && !WinVal<T>::is_pending(x1);
+                if constexpr (kLevels) acc = rdy1 ? max(acc, x1) : acc;
+                else if (rdy1) p = fma(wn, x1, p);
+            }
+            const int used = (int)rdy + (int)rdy1;
+            k -= used;
+            const int k1 = k - 1 > s ? k - 1 : k;
+            if constexpr (kTwo) {
+                const int k2 = k - 2 > s ? k - 2 : k1;
+                const int l1 = ecol(k1);
+                const T v1 = weight(k1);
+                c = used == 0 ? c : (used == 1 ? cn : c2);
+                w = used == 0 ? w : (used == 1 ? wn : w2);
+                cn = used == 0 ? cn : (used == 1 ? c2 : l1);
+                wn = used == 0 ? wn : (used == 1 ? w2 : v1);
+                c2 = ecol(k2);
+                w2 = weight(k2);
             } else {
-                p = r0 ? fma(w0, v0, p) : p;
-                p = r1 ? fma(w1, v1, p) : p;
+                // the entry after the head, for the next round (a repeated load when nothing moved)
+                c = rdy ? cn : c;
+                w = rdy ? wn : w;
+                cn = ecol(k1);
+                wn = weight(k1);
             }
-            const int used = (int)r0 + (int)r1;
-            nrem -= used;
-            h += used;
-            {
-                const int h0 = min(h, RS - 1), h1 = min(h + 1, RS - 1);
-                c0 = S.qc[h0 * 32 + lane];
-                c1 = S.qc[h1 * 32 + lane];
-                if constexpr (!kLevels) {
-                    w0 = S.qw[h0 * 32 + lane];
-                    w1 = S.qw[h1 * 32 + lane];
-                }
-            }
-            prog = used > 0;
-            if (r0 && nrem == 0) {
-                finish();
-                if constexpr (kLevels) xm = T(1) + acc;
-                else xm = Pend<T>::fix(p);
-            }
-            if (!done && !lean) {
-                walk();
-                if (k <= s) {
-                    finish();
-                    if constexpr (kLevels) xm = T(1) + acc;
-                    else xm = Pend<T>::fix(scaled ? p : fma(-acc, di, bd));
-                }
-            }
-            if (backoff_ns > 0 && !__any_sync(0xffffffffu, prog)) __nanosleep(backoff_ns);
+            if (rdy && k <= s) finish();
+            if (backoff_ns > 0 && !__any_sync(0xffffffffu, rdy)) __nanosleep(backoff_ns);
             // checked at round 31 of a block (a 32-row chain takes 32 rounds) and every 256 after
             if ((++it & 255u) == 31u) {
                 if (aborted(ctl)) fail = true;
@@ -483,40 +455,42 @@ k_window(int n, const int* __restrict__ rp, const int* __restrict__ col, const T
 }
 
 // ---------------------------------------------------------------------------------------
-template <typename T, int W, bool kWeak>
+template <typename T, int W, bool kTwo>
 static int window_launch_t(int n, const int* rp, const int* col, const T* val, const T* invd, const T* b, T* x,
-                         Ctl* ctl, int64_t budget, int backoff_ns, cudaStream_t st, int64_t* launches) {
+                           Ctl* ctl, int64_t budget, int backoff_ns, cudaStream_t st, int64_t* launches) {
     using L = WinLayout<T, W>;
     static bool configured[64] = {};
     int dev = 0;
     CUDA_TRY(cudaGetDevice(&dev));
     if (dev < 0 || dev >= 64) return SPTRSV_ERR_INVALID_ARG;
     if (!configured[dev]) {
-        CUDA_TRY(cudaFuncSetAttribute(k_window<T, W, kWeak>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        CUDA_TRY(cudaFuncSetAttribute(k_window<T, W, kTwo>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)L::kBytes));
         configured[dev] = true;
     }
-    k_window<T, W, kWeak><<<1, W * 32, L::kBytes, st>>>(n, rp, col, val, invd, b, x, ctl, budget, backoff_ns);
+    k_window<T, W, kTwo><<<1, W * 32, L::kBytes, st>>>(n, rp, col, val, invd, b, x, ctl, budget, backoff_ns);
     ++*launches;
     CUDA_TRY(cudaGetLastError());
     return 0;
 }
 
-// x stores and loads: weak (the default) or GPU-scope relaxed (SPTRSV_WINDOW_STORE=relaxed)
-static bool window_weak() {
-    static bool w = [] {
-        const char* e = getenv("SPTRSV_WINDOW_STORE");
-        return !(e && strcmp(e, "relaxed") == 0);
+// Entries a round consumes per lane: SPTRSV_WINDOW_PER_ROUND = 1 or 2; by default 2 for the
+// level analysis (integer maxima, short rounds) and 1 for the solves (one FP64 FMA per round).
+template <typename T>
+static bool window_two() {
+    static int v = [] {
+        const char* e = getenv("SPTRSV_WINDOW_PER_ROUND");
+        return e ? atoi(e) : 0;
     }();
-    return w;
+    return v == 0 ? std::is_same<T, int>::value : v == 2;
 }
 
 template <typename T, int W>
 static int window_launch(int n, const int* rp, const int* col, const T* val, const T* invd, const T* b, T* x,
                          Ctl* ctl, int64_t budget, int backoff_ns, cudaStream_t st, int64_t* launches) {
-    return window_weak() ? window_launch_t<T, W, true>(n, rp, col, val, invd, b, x, ctl, budget, backoff_ns, st, launches)
-                         : window_launch_t<T, W, false>(n, rp, col, val, invd, b, x, ctl, budget, backoff_ns, st,
-                                                        launches);
+    return window_two<T>()
+               ? window_launch_t<T, W, true>(n, rp, col, val, invd, b, x, ctl, budget, backoff_ns, st, launches)
+               : window_launch_t<T, W, false>(n, rp, col, val, invd, b, x, ctl, budget, backoff_ns, st, launches);
 }
 
 template <typename T>
