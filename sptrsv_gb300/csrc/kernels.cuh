@@ -76,7 +76,6 @@ int launch_window(bool f32, const SolveArgs& a);
 int launch_window_levels(int n, const int* rp, const int* col, int* level, Ctl* ctl, int64_t budget, cudaStream_t st,
                          int64_t* launches);
 int window_warps();
-int window_backoff_ns();
 int launch_transpose(bool to_row_major, const double* src, double* dst, int n, int rhs, cudaStream_t st,
                      int64_t* launches);
 

@@ -32,9 +32,8 @@
 //     to blocks <= t-W-1 (done) and are read from global x.
 // Forward progress: every wait (a start condition, a pending x) is on a higher block, so the
 // waits form no cycle and all W warps of the one CTA are resident.  Every spin is bounded by
-// the spin budget and the abort flag, as in every other kernel here.  A round in which no lane
-// of the warp made progress may sleep `backoff_ns`, so that waiting warps leave the issue slots
-// of their SM sub-partition to the warps that compute.
+// the spin budget and the abort flag, as in every other kernel here.  Rounds do not sleep: each
+// warp has its own SM sub-partition at W = 4, and a sleeping round only delays the next hop.
 //
 // Arithmetic: the solve accumulates the ready entries right to left; at the first entry it has
 // to wait for, it switches to the scaled form p = (b_i - sum) / U_ii and folds each later term
@@ -166,11 +165,27 @@ template <typename T>
 __device__ __forceinline__ T win_ld(const T* p) { return *p; }
 template <typename T>
 __device__ __forceinline__ void win_st(T* p, T v) { *p = v; }
+// Bounded wait for x of a row in a finished block (never expected to wait): the value, or the
+// pending value on timeout or abort (the timeout recorded).
+template <typename T>
+__device__ __noinline__ T win_wait(const T* p, Ctl* ctl, int64_t budget) {
+    const uint64_t t0 = gtimer();
+    for (;;) {
+        const T v = *(const volatile T*)p;
+        if (!WinVal<T>::is_pending(v)) return v;
+        if (aborted(ctl)) return v;
+        if ((int64_t)(gtimer() - t0) > budget) {
+            record_error(ctl, SPTRSV_ERR_TIMEOUT);
+            return v;
+        }
+        __nanosleep(64);
+    }
+}
 
-template <typename T, int W, bool kTwo>
+template <typename T, int W>
 __global__ void __launch_bounds__(W * 32, 1)
 k_window(int n, const int* __restrict__ rp, const int* __restrict__ col, const T* __restrict__ val,
-         const T* __restrict__ invd, const T* __restrict__ b, T* x, Ctl* ctl, int64_t budget, int backoff_ns) {
+         const T* __restrict__ invd, const T* __restrict__ b, T* x, Ctl* ctl, int64_t budget) {
     using L = WinLayout<T, W>;
     constexpr bool kLevels = L::kLevels;
     constexpr int RM = kWinRing - 1;
@@ -247,22 +262,26 @@ k_window(int n, const int* __restrict__ rp, const int* __restrict__ col, const T
         const int* rS = S.rp + rs * L::kRpSlot;
         const int e0 = rS[0];
         const bool staged = rS[top - lo] - e0 <= L::kCap;
-        const int* colS = S.col + ds * L::kCap;
-        const T* valS = kLevels ? nullptr : S.val + ds * L::kCap;
-        auto ecol = [&](int k) -> int { return staged ? colS[k - e0] : __ldg(col + k); };
-        auto eval = [&](int k) -> T {
-            if constexpr (kLevels) return T(0);
-            else return staged ? valS[k - e0] : __ldg(val + k);
-        };
         const int i = top - 1 - lane;
         const int far = top + reach;
         bool done = i < lo;
         int s = e0, k = e0, c = 0;  // a lane without a row (short last block) reads entry e0 harmlessly
-        T v = T(0), acc = T(0), di = T(0), bd = T(0), vs = T(0), p = T(0);
-        bool scaled = false;
         if (!done) {
             s = rS[i - lo];
             k = rS[i - lo + 1] - 1;
+        }
+        // the lane's entries through one pointer: the staged copy in shared memory, else global
+        const int* rcol = staged ? S.col + ds * L::kCap + (s - e0) : col + s;
+        const T* rval = nullptr;
+        if constexpr (!kLevels) rval = staged ? S.val + ds * L::kCap + (s - e0) : val + s;
+        auto ecol = [&](int q) -> int { return rcol[q - s]; };
+        auto eval = [&](int q) -> T {
+            if constexpr (kLevels) return T(0);
+            else return rval[q - s];
+        };
+        T v = T(0), acc = T(0), di = T(0), bd = T(0), vs = T(0), p = T(0);
+        bool scaled = false, fail = false;
+        if (!done) {
             if constexpr (!kLevels) {
                 di = S.inv[ds * 32 + lane];
                 bd = S.bb[ds * 32 + lane] * di;
@@ -292,7 +311,21 @@ k_window(int n, const int* __restrict__ rp, const int* __restrict__ col, const T
                 bool bad = false;
 #pragma unroll
                 for (int q = 0; q < 4; ++q) bad |= use[q] && WinVal<T>::is_pending(xq[q]);
-                if (bad) break;  // not expected; the rounds below poll for it
+                if (bad) {
+                    // not expected: the start condition has every block at or beyond `far` done.
+                    // Wait all the same, bounded like every other wait.
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        if (use[q] && !fail && WinVal<T>::is_pending(xq[q])) {
+                            xq[q] = win_wait<T>(x + cq[q], ctl, budget);
+                            fail = WinVal<T>::is_pending(xq[q]);
+                        }
+                    }
+                    if (fail) {
+                        done = true;  // the lane gives up: no rounds, no publication; the warp returns
+                        break;
+                    }
+                }
                 int used = 0;
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
@@ -310,7 +343,7 @@ k_window(int n, const int* __restrict__ rp, const int* __restrict__ col, const T
             }
         }
         // the rest: one walk over what is ready, then lockstep rounds over the remaining entries.
-        // xm is this lane's value once its row is finished, the pending pattern before.
+        // xm is this lane's value once its row is finished.
         T xm = WinVal<T>::pending();
         // walk right to left consuming ready entries; stops at the first pending one
         auto walk = [&]() {
@@ -357,84 +390,68 @@ k_window(int n, const int* __restrict__ rp, const int* __restrict__ col, const T
             if (k <= s) finish();
         }
         // The remaining entries, one per round (the head, entry k, is pending).  A round is the same
-        // straight-line code for every lane: the head's value from a shuffle when its row is in this
-        // block (rows of this block are lanes of this warp) and from the ring otherwise, its pending
-        // test, one FMA, and the move to the next entry, whose column and weight were loaded a round
-        // ahead.  A lane's own value xm holds the pending pattern until its row is finished, so the
-        // shuffled value itself says whether an in-block dependency is done.
-        // Registers hold the head (entry k: column c, scaled weight w = -U_ik / U_ii) and the next two
-        // entries (cn, wn: k-1; c2, w2: k-2), loaded a round ahead; indices past the row's start are
-        // clamped to a valid entry and never consumed.  kTwo: a round consumes up to two entries.
-        T w = T(0), wn = T(0), w2 = T(0);
-        int cn = 0, c2 = 0;
+        // straight-line code for every lane: the head's value from the ring (the pending pattern
+        // until its row is finished, in this block or another), one FMA, and the move to the next
+        // entry, whose column and weight were loaded a round ahead.  (Handing in-block values over
+        // by warp shuffles instead -- two shuffles and a select a round -- measured slower on the
+        // 2M-row system: 140.5 against 131.0 ms for the solve, 97.2 against 80.4 ms for the
+        // levels, same GPU; so did two entries a round, and an L1 prefetch of the far columns.)
+        // Registers hold the head (entry k: column c, scaled weight w = -U_ik / U_ii) and the next
+        // entry (cn, wn: k-1, an index past the row's start clamped to it and never consumed),
+        // loaded a round ahead.
+        T w = T(0), wn = T(0);
+        int cn = 0;
         auto weight = [&](int q) -> T {
             if constexpr (kLevels) return T(0);
             else return -eval(q) * di;
         };
         if (!done) {
             if constexpr (!kLevels) w = vs;
-            const int k1 = k - 1 > s ? k - 1 : k;
+            const int k1 = max(k - 1, s);
             cn = ecol(k1);
             wn = weight(k1);
-            if constexpr (kTwo) {
-                const int k2 = k - 2 > s ? k - 2 : k1;
-                c2 = ecol(k2);
-                w2 = weight(k2);
-            }
         }
+        __syncwarp();  // the lanes' ring stores of rows finished above before the rounds' loads
         // the budget's timer starts at the block for short budgets, else at round 31 of the block
         uint64_t t0 = budget < 1000000 ? gtimer() : 0;
-        unsigned it = 0;
-        bool fail = false;
+        unsigned cd = 31;  // rounds to the next timer check
         for (;;) {
-            if (__all_sync(0xffffffffu, done || fail)) break;
-            auto value = [&](int cc) -> T {
-                const T sv = __shfl_sync(0xffffffffu, xm, (top - 1 - cc) & 31);
-                T gv;
-                if (cc < far) gv = vring[cc & RM];
-                else gv = win_ld<T>(x + cc);  // a done block's row (not expected here)
-                return cc < top ? sv : gv;
-            };
-            const T x0 = value(c);
+            if (__all_sync(0xffffffffu, done)) break;
+            // The head's value from the ring: rows of this block and of the blocks in flight are
+            // stored there when they finish (the __syncwarp that ends a round orders this warp's
+            // stores before the next round's loads).  A column beyond the ring's reach is read
+            // from global x: rows need not be sorted, so such an entry can follow a near one (rare;
+            // the far loop took the sorted case).  A finished lane's stale column reads a slot whose
+            // value is discarded.
+            T x0;
+            if (__builtin_expect(c >= far, 0)) x0 = win_ld<T>(x + c);
+            else x0 = vring[c & RM];
             const bool rdy = !done && !WinVal<T>::is_pending(x0);
-            bool rdy1 = false;
             if constexpr (kLevels) acc = rdy ? max(acc, x0) : acc;
             else p = rdy ? fma(w, x0, p) : p;
-            if constexpr (kTwo) {
-                const T x1 = value(cn);
-                rdy1 = rdy && k - 1 > s && !WinVal<T>::is_pending(x1);
-                if constexpr (kLevels) acc = rdy1 ? max(acc, x1) : acc;
-                else if (rdy1) p = fma(wn, x1, p);
-            }
-            const int used = (int)rdy + (int)rdy1;
-            k -= used;
-            const int k1 = k - 1 > s ? k - 1 : k;
-            if constexpr (kTwo) {
-                const int k2 = k - 2 > s ? k - 2 : k1;
-                const int l1 = ecol(k1);
-                const T v1 = weight(k1);
-                c = used == 0 ? c : (used == 1 ? cn : c2);
-                w = used == 0 ? w : (used == 1 ? wn : w2);
-                cn = used == 0 ? cn : (used == 1 ? c2 : l1);
-                wn = used == 0 ? wn : (used == 1 ? w2 : v1);
-                c2 = ecol(k2);
-                w2 = weight(k2);
-            } else {
+            k -= (int)rdy;
+            c = rdy ? cn : c;
+            if constexpr (!kLevels) w = rdy ? wn : w;
+            {
                 // the entry after the head, for the next round (a repeated load when nothing moved)
-                c = rdy ? cn : c;
-                w = rdy ? wn : w;
+                const int k1 = max(k - 1, s);
                 cn = ecol(k1);
                 wn = weight(k1);
             }
             if (rdy && k <= s) finish();
-            if (backoff_ns > 0 && !__any_sync(0xffffffffu, rdy)) __nanosleep(backoff_ns);
+            __syncwarp();
             // checked at round 31 of a block (a 32-row chain takes 32 rounds) and every 256 after
-            if ((++it & 255u) == 31u) {
+            if (--cd == 0) {
+                cd = 256;
                 if (aborted(ctl)) fail = true;
                 else if (t0 == 0) t0 = gtimer();
                 else if ((int64_t)(gtimer() - t0) > budget) {
                     record_error(ctl, SPTRSV_ERR_TIMEOUT);
                     fail = true;
+                }
+                if (__any_sync(0xffffffffu, fail)) {
+                    fail = true;
+                    break;
                 }
             }
         }
@@ -455,58 +472,36 @@ k_window(int n, const int* __restrict__ rp, const int* __restrict__ col, const T
 }
 
 // ---------------------------------------------------------------------------------------
-template <typename T, int W, bool kTwo>
-static int window_launch_t(int n, const int* rp, const int* col, const T* val, const T* invd, const T* b, T* x,
-                           Ctl* ctl, int64_t budget, int backoff_ns, cudaStream_t st, int64_t* launches) {
+template <typename T, int W>
+static int window_launch(int n, const int* rp, const int* col, const T* val, const T* invd, const T* b, T* x,
+                         Ctl* ctl, int64_t budget, cudaStream_t st, int64_t* launches) {
     using L = WinLayout<T, W>;
     static bool configured[64] = {};
     int dev = 0;
     CUDA_TRY(cudaGetDevice(&dev));
     if (dev < 0 || dev >= 64) return SPTRSV_ERR_INVALID_ARG;
     if (!configured[dev]) {
-        CUDA_TRY(cudaFuncSetAttribute(k_window<T, W, kTwo>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)L::kBytes));
+        CUDA_TRY(cudaFuncSetAttribute(k_window<T, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L::kBytes));
         configured[dev] = true;
     }
-    k_window<T, W, kTwo><<<1, W * 32, L::kBytes, st>>>(n, rp, col, val, invd, b, x, ctl, budget, backoff_ns);
+    k_window<T, W><<<1, W * 32, L::kBytes, st>>>(n, rp, col, val, invd, b, x, ctl, budget);
     ++*launches;
     CUDA_TRY(cudaGetLastError());
     return 0;
 }
 
-// Entries a round consumes per lane: SPTRSV_WINDOW_PER_ROUND = 1 or 2; by default 2 for the
-// level analysis (integer maxima, short rounds) and 1 for the solves (one FP64 FMA per round).
-template <typename T>
-static bool window_two() {
-    static int v = [] {
-        const char* e = getenv("SPTRSV_WINDOW_PER_ROUND");
-        return e ? atoi(e) : 0;
-    }();
-    return v == 0 ? std::is_same<T, int>::value : v == 2;
-}
-
-template <typename T, int W>
-static int window_launch(int n, const int* rp, const int* col, const T* val, const T* invd, const T* b, T* x,
-                         Ctl* ctl, int64_t budget, int backoff_ns, cudaStream_t st, int64_t* launches) {
-    return window_two<T>()
-               ? window_launch_t<T, W, true>(n, rp, col, val, invd, b, x, ctl, budget, backoff_ns, st, launches)
-               : window_launch_t<T, W, false>(n, rp, col, val, invd, b, x, ctl, budget, backoff_ns, st, launches);
-}
-
 template <typename T>
 static int window_dispatch(int n, const int* rp, const int* col, const T* val, const T* invd, const T* b, T* x,
                            Ctl* ctl, int64_t budget, cudaStream_t st, int64_t* launches) {
-    const int bo = window_backoff_ns();
     switch (window_warps()) {
-        case 2: return window_launch<T, 2>(n, rp, col, val, invd, b, x, ctl, budget, bo, st, launches);
-        case 16: return window_launch<T, 16>(n, rp, col, val, invd, b, x, ctl, budget, bo, st, launches);
-        case 8: return window_launch<T, 8>(n, rp, col, val, invd, b, x, ctl, budget, bo, st, launches);
-        default: return window_launch<T, 4>(n, rp, col, val, invd, b, x, ctl, budget, bo, st, launches);
+        case 2: return window_launch<T, 2>(n, rp, col, val, invd, b, x, ctl, budget, st, launches);
+        case 16: return window_launch<T, 16>(n, rp, col, val, invd, b, x, ctl, budget, st, launches);
+        case 8: return window_launch<T, 8>(n, rp, col, val, invd, b, x, ctl, budget, st, launches);
+        default: return window_launch<T, 4>(n, rp, col, val, invd, b, x, ctl, budget, st, launches);
     }
 }
 
-// Warps of the window CTA (SPTRSV_WINDOW_WARPS = 2, 4, 8 or 16) and the sleep of a round that made
-// no progress (SPTRSV_WINDOW_BACKOFF_NS, 0 = poll without sleeping).
+// Warps of the window CTA (SPTRSV_WINDOW_WARPS = 2, 4, 8 or 16).
 int window_warps() {
     static int w = [] {
         const char* e = getenv("SPTRSV_WINDOW_WARPS");
@@ -514,14 +509,6 @@ int window_warps() {
         return (v == 2 || v == 4 || v == 8 || v == 16) ? v : 4;
     }();
     return w;
-}
-int window_backoff_ns() {
-    static int b = [] {
-        const char* e = getenv("SPTRSV_WINDOW_BACKOFF_NS");
-        const int v = e ? atoi(e) : 0;
-        return v < 0 ? 0 : (v > 1000 ? 1000 : v);
-    }();
-    return b;
 }
 
 int launch_window(bool f32, const SolveArgs& a) {

@@ -144,3 +144,25 @@ def test_window_timeout_then_recovers(orc, solver):
     x = solver.solve(b, schedule="syncfree_window")
     ref = orc.base_gauss_upper(rp.astype(np.uint64), col, val, b, 1)
     assert elem_err(x, ref) <= ELEM_TOL
+
+
+@pytest.mark.parametrize("band,p_near", [(4000, 0.5), (64, 0.9)])
+def test_window_unsorted_rows(orc, solver, band, p_near):
+    """Rows whose off-diagonal entries are stored in a shuffled order (the diagonal stays first):
+    far columns then follow near ones, and the rounds must read them from global x."""
+    m = gen.random_upper(120_000, 8.0, p_near, band, band + 3)
+    rp = m.row_ptr.astype(np.int64)
+    col = np.array(m.col, dtype=np.int32)
+    val = np.array(m.val, dtype=np.float64)
+    rng = np.random.default_rng(17)
+    for r in range(m.n):
+        a, e = rp[r] + 1, rp[r + 1]
+        if e - a > 1:
+            perm = a + rng.permutation(e - a)
+            col[a:e] = col[perm]
+            val[a:e] = val[perm]
+    b = gen.uniform(band, m.n)
+    _solve_check(orc, solver, rp, col, val, b, schedule="syncfree_window")
+    lv, ml = orc.levels(rp.astype(np.uint64), col)
+    assert solver.info()["max_level"] == ml
+    assert np.array_equal(solver.levels(), lv)
