@@ -381,8 +381,7 @@ k_window(int n, const int* __restrict__ rp, const int* __restrict__ col, const T
             } else {
                 xm = Pend<T>::fix(scaled ? p : fma(-acc, di, bd));
             }
-            vring[i & RM] = xm;
-            win_st<T>(x + i, xm);
+            vring[i & RM] = xm;  // global x is written once the whole block is done
             done = true;
         };
         if (!done) {
@@ -395,7 +394,9 @@ k_window(int n, const int* __restrict__ rp, const int* __restrict__ col, const T
         // entry, whose column and weight were loaded a round ahead.  (Handing in-block values over
         // by warp shuffles instead -- two shuffles and a select a round -- measured slower on the
         // 2M-row system: 140.5 against 131.0 ms for the solve, 97.2 against 80.4 ms for the
-        // levels, same GPU; so did two entries a round, and an L1 prefetch of the far columns.)
+        // levels, same GPU; so did two entries a round, and an L1 prefetch of the far columns.
+        // Writing each finished row to global x at once, rather than the block's 32 rows in one
+        // coalesced store at its end, cost 131.1 against 118.1 ms.)
         // Registers hold the head (entry k: column c, scaled weight w = -U_ik / U_ii) and the next
         // entry (cn, wn: k-1, an index past the row's start clamped to it and never consumed),
         // loaded a round ahead.
@@ -459,7 +460,9 @@ k_window(int n, const int* __restrict__ rp, const int* __restrict__ col, const T
             cpa_wait_all();  // the warp's own copies in flight end before it returns
             return;
         }
-        // 5. block t done: its ring stores and the reset of block t+W's slots before the flag
+        // 5. block t done: its rows to global x in one coalesced store; those stores, the ring
+        //    stores and the reset of block t+W's slots before the flag
+        if (i >= lo) win_st<T>(x + i, xm);
         __threadfence_block();
         __syncwarp();
         if (lane == 0) vflag[t & (kWinFlags - 1)] = t;
