@@ -82,9 +82,9 @@ def parse():
     ap.add_argument("--batch-steps", type=int, default=10,
                     help="default workload: timed steps of the batched mix measured after the 2M-row system")
     ap.add_argument("--no-batch", action="store_true", help="default workload: skip the nested batched-mix record")
-    ap.add_argument("--panels", default="fp64", choices=["fp64", "tc"],
-                    help="panel products of the exact FP64 supernodal / batched schedules: FP64 FMAs or the tensor "
-                         "cores (BF16 digit slices, FP64-accurate)")
+    ap.add_argument("--panels", default="fp64", choices=["fp64", "tc", "df"],
+                    help="panel products of the exact FP64 supernodal / batched schedules: FP64 FMAs, the tensor "
+                         "cores (BF16 digit slices) or double-FP32 on the FP32 pipes; all FP64-accurate")
     ap.add_argument("--rhs", default="1,8,32,128", help="supernodal: right-hand-side counts (comma list)")
     ap.add_argument("--plain-schedule", default=None, choices=["syncfree_block", "syncfree_window", "syncfree_warp"],
                     help="default workload: the plain FP64 sync-free baseline's schedule")
@@ -825,8 +825,8 @@ def batch_record(args, dist, steps, warmup, with_cpu=True, sample_errors=True):
         "config": {"workload": BATCH_WORKLOAD.format(count=args.count, nmax=args.nmax), "systems": args.count,
                    "rows": int(np.sum(M.n)), "nnz": int(np.sum(M.nnz)), "rhs_columns": int(np.sum(M.rhs)),
                    "rank0_systems": count_l, "schedules": counts, "picked_by": picked_by, "generation_s": t_gen,
-                   "panel_products": "tensor cores (BF16 digit slices, FP64-accurate)" if args.panels == "tc"
-                   else "FP64 FMAs",
+                   "panel_products": {"tc": "tensor cores (BF16 digit slices, FP64-accurate)",
+                                      "df": "double-FP32 on the FP32 pipes (FP64-accurate)"}.get(args.panels, "FP64 FMAs"),
                    "l2": "no flush: the arena (%.1f GB) is far larger than L2" % (fb / 1e9),
                    "parallelism": f"systems sharded over {dist.ws} GPU(s) by LPT on nnz x rhs"},
         "solve_unit": "one system with all its right-hand sides",

@@ -204,8 +204,10 @@ SPTRSV_API int sptrsv_device_sm_count(sptrsv_handle h);
 SPTRSV_API int sptrsv_measure_fp64(int device, double* gfma_per_s, double* dep_fma_cycles);
 /* No counterpart in the reference: the panel products of the exact FP64 supernodal and batched
  * schedules -- 0 = FP64 FMAs (the default), 1 = the tensor cores (tcgen05: BF16 digit slices of
- * G and of the right-hand side, exact FP32 accumulation in TMEM, FP64 combination; FP64-accurate).
- * Applies to partitions and batches built afterwards; returns the previous mode. */
+ * G and of the right-hand side, exact FP32 accumulation in TMEM, FP64 combination; FP64-accurate),
+ * 2 = double-FP32 on the FP32 pipes (G and the right-hand side as scaled FP32 pairs, error-free
+ * products and compensated sums; FP64-accurate).  Applies to partitions and batches built
+ * afterwards; returns the previous mode. */
 SPTRSV_API int sptrsv_set_panels_mode(int mode);
 /* Largest n accepted by sptrsv_solve_noalloc (its reciprocal diagonal lives in a fixed array). */
 #define SPTRSV_NOALLOC_MAX_ROWS (1 << 20)

@@ -72,12 +72,13 @@ def measure_fp64(device=0):
 
 
 def set_panels_mode(mode):
-    """Panel products of the exact FP64 schedules: "fp64" (FP64 FMAs) or "tc" (tensor cores, FP64
-    accurate); applies to partitions and batches built afterwards; returns the previous mode."""
-    rc = _lib.lib().sptrsv_set_panels_mode({"fp64": 0, "tc": 1}[mode])
+    """Panel products of the exact FP64 schedules: "fp64" (FP64 FMAs), "tc" (tensor cores) or "df"
+    (double-FP32 on the FP32 pipes), all FP64-accurate; applies to partitions and batches built
+    afterwards; returns the previous mode."""
+    rc = _lib.lib().sptrsv_set_panels_mode({"fp64": 0, "tc": 1, "df": 2}[mode])
     if rc < 0:
         raise SptrsvError(rc, "set_panels_mode")
-    return ("fp64", "tc")[rc]
+    return ("fp64", "tc", "df")[rc]
 
 
 def candidate(cand_id):

@@ -226,16 +226,18 @@ int Handle::build_csc() {
     return 0;
 }
 
-// FP64 AUTO with one RHS: the one-CTA window kernel on short rows (its lanes hold a row's pending
-// entries in registers; 2M-row system, 8.6 entries per row: 208 against 324 ms for the block
-// kernel), the block kernel on long rows (64 x 64 band factor, 65 entries per row: 2.25 against
-// 3.25 ms).  SPTRSV_AUTO_WINDOW=0 / 1 forces either.
+// FP64 AUTO with one RHS: the one-CTA window kernel up to ~90 entries per row, the block kernel on
+// longer rows, whose many entries per lane the window kernel walks one a round.  Measured on GB300
+// (kernel times, same GPU): random factors of 200k rows with 8.6 / 27 / 54 / 80 / 106 entries per
+// row 11.8 / 28.4 / 54.3 / 96.4 / 123.6 ms against 32.0 / 87.5 / 99.2 / 104.3 / 106.8 ms for the
+// block kernel; 64 x 64 band factor (65 entries per row) 1.33 against 2.26 ms; 2M-row system
+// 118 against 324 ms.  SPTRSV_AUTO_WINDOW=0 / 1 forces either.
 static bool auto_window(double mean_len) {
     static int w = [] {
         const char* e = getenv("SPTRSV_AUTO_WINDOW");
         return e ? (strcmp(e, "1") == 0 ? 1 : 0) : -1;
     }();
-    return w < 0 ? mean_len <= 24.0 : w == 1;
+    return w < 0 ? mean_len <= 90.0 : w == 1;
 }
 
 // Schedule choice from the analysis features (the autotuner overrides it).
@@ -899,7 +901,7 @@ Handle::~Handle() {
                       &level_rows, &stats, &csc_ptr, &csc_row, &csc_val, &scratch, &xw, &bw, &r32, &d32a, &d32b,
                       &norms, &indeg_work, &left, &db, &dx, &flush, &offdiag, &roff, &jmeta, &jbase, &sell, &sell_perm, &sell_len, &sell_ptr,
                       &sn_start, &sn_m, &sn_roff, &sn_rect, &sn_goff, &sn_ld, &sn_colbase, &sn_outbase, &sn_items,
-                      &sn_G, &sn_Ghi, &sn_Glo, &sn_pan, &sn_pitems, &sn_pcnt, &sn_ppart, &sn_gtc, &sn_tcrec, &tune_b, &tune_x};
+                      &sn_G, &sn_Ghi, &sn_Glo, &sn_pan, &sn_pitems, &sn_pcnt, &sn_ppart, &sn_gtc, &sn_tcrec, &sn_ghl, &sn_gexp, &tune_b, &tune_x};
     for (DevBuf* b : bufs) b->release();
     if (ctl) cudaFree(ctl);
     if (ev0) cudaEventDestroy(ev0);

@@ -1085,7 +1085,7 @@ int Batch::build_panels(int s, bool f64) {
     const long long gtot = goff[C];
     // buffers of this system: [bf16 hi, bf16 lo] and/or [f64], then the rectangle columns
     const int k0 = (int)gbufs.size();
-    gbufs.resize(k0 + 5);
+    gbufs.resize(k0 + 7);  // + [4] tensor-core records, [5] double-FP32 G, [6] its row exponents
     if ((rc = gbufs[k0 + 3].ensure(sizeof(int) * ((size_t)roff[C] + 1)))) return rc;
     if (!f64) {
         if ((rc = gbufs[k0].ensure(2 * (size_t)gtot)) || (rc = gbufs[k0 + 1].ensure(2 * (size_t)gtot))) return rc;
@@ -1117,6 +1117,8 @@ int Batch::build_panels(int s, bool f64) {
             if ((int)old.size() == C) {
                 ch.g64 = old[c].g64;
                 ch.gtc = old[c].gtc;
+                ch.ghl = old[c].ghl;
+                ch.gexp = old[c].gexp;
             }
         } else {
             ch.g64 = gbufs[k0 + 2].as<double>() + goff[c];
@@ -1152,6 +1154,25 @@ int Batch::build_panels(int s, bool f64) {
         trec.release();
         if (rc) return rc;
         have_tc[s] = 1;
+    }
+    if (f64 && panels_mode() == 2) {
+        // the double-FP32 schedule: G as scaled FP32 pairs (laid out like g64) and the row exponents,
+        // indexed by the system's row
+        if ((rc = gbufs[k0 + 5].ensure(sizeof(float2) * (size_t)std::max(1LL, gtot))) ||
+            (rc = gbufs[k0 + 6].ensure(sizeof(int) * (size_t)std::max(1, S.n))))
+            return rc;
+        for (int c = 0; c < C; ++c) {
+            pchunks[s][c].ghl = gbufs[k0 + 5].as<float2>() + goff[c];
+            pchunks[s][c].gexp = gbufs[k0 + 6].as<int>() + ss[c];
+        }
+        DevBuf tch;
+        if ((rc = tch.ensure(sizeof(BChunk) * C))) return rc;
+        CUDA_TRY(cudaMemcpyAsync(tch.p, pchunks[s].data(), sizeof(BChunk) * C, cudaMemcpyHostToDevice, st));
+        int64_t lconv = 0;
+        rc = launch_g_df(tch.as<BChunk>(), C, st, &lconv);
+        if (!rc) CUDA_TRY(cudaStreamSynchronize(st));
+        tch.release();
+        if (rc) return rc;
     }
     H.drop_matrix();
     panel_ok[s] = 1;
@@ -1257,6 +1278,7 @@ int Batch::build_lists() {
             steps.push_back(std::move(its));
         }
         for (BChunk b : pchunks[s]) {
+            if (panels_mode() != 2) b.ghl = nullptr;  // double-FP32 products only in that mode
             b.poff = poff;
             b.cbase = cbase;
             cbase += ng;

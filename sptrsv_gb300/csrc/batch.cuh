@@ -12,7 +12,9 @@ constexpr int kP64 = 64;      // columns of G per FP64 panel work item (and rows
 constexpr int kP64Nc = 16;    // right-hand-side columns per pass of an FP64 panel work item
 constexpr int kP64Near = 16;  // columns per block in the nearest solved region
 
-// Right-hand-side columns per work item: 4 up to 16 columns, then 16 (at most kP64Nc).
+// Right-hand-side columns per work item: 4 up to 16 columns, then 16 (at most kP64Nc), so that one
+// item's work on the dependency chain stays short.  (Double-FP32 items of up to 16 columns, one G
+// read for all of them, measured slower on the 512-system mix: 74.9 against 57.5 ms.)
 __host__ __device__ __forceinline__ int p64_group_width(int rhs) { return rhs <= 16 ? 4 : kP64Nc; }
 __host__ __device__ __forceinline__ int p64_groups(int rhs) {
     const int g = p64_group_width(rhs);
@@ -38,6 +40,8 @@ struct BChunk {
     int r0, pw;                // the panel's rows within the chunk
     int cbase;                 // FP64 schedule: first completion counter (one per RHS group)
     unsigned char* gtc;        // tensor-core FP64 schedule: the panel's digit-slice G records (panels_tc.cu)
+    const float2* ghl;         // double-FP32 products: G 2^-e_r as FP32 pairs, laid out like g64 (or null)
+    const int* gexp;           // their row exponents e_r, indexed by the chunk's row
 };
 
 // Column blocks of a panel's G (w own columns, then K - w solved columns): the own part in
@@ -71,6 +75,7 @@ __host__ __device__ __forceinline__ void p64_block(int w, int K, int blk, int& k
 // items carry their group (block | group << 16), poff counts doubles and cbase counters.  One
 // system (sys == nullptr, rhs columns, row-major n x rhs): every item runs for each of the
 // p64_groups(rhs) groups, poff counts per column and cbase per group.  ncnt counters are cleared.
+// Panels that carry double-FP32 copies of G (ghl) are multiplied in double-FP32.
 int launch_panels64(const BSys* sys, int rhs, const double* b, double* x, Ctl* ctl, unsigned* ticket, int64_t budget,
                     const int2* items, unsigned nitems, const BChunk* panels, double* part, int* cnt, int ncnt,
                     int ctas_per_sm, int sm_count, cudaStream_t st, int64_t* launches);
@@ -88,5 +93,8 @@ int tc_groups_host(int rhs);
 // Panel products of the exact FP64 schedules: 0 = FP64 FMAs (default), 1 = tensor cores
 // (SPTRSV_PANELS=tc).
 int panels_mode();
+// Double-FP32 copies of every panel's G (ghl, gexp of each chunk; panels of one chunk share them):
+// one CTA per panel writes its rows.
+int launch_g_df(const BChunk* panels, int npanels, cudaStream_t st, int64_t* launches);
 
 }  // namespace sptrsv

@@ -110,6 +110,7 @@ struct Handle {
     // (panel, block) items, per-panel completion counters, partial sums (sn_prows per column)
     DevBuf sn_pan, sn_pitems, sn_pcnt, sn_ppart;
     DevBuf sn_gtc, sn_tcrec;  // tensor-core schedule: digit-slice G records of every panel block
+    DevBuf sn_ghl, sn_gexp;   // double-FP32 schedule: G as scaled FP32 pairs, row exponents
     bool sn_tc = false;       // the records are built
     bool build_tc = true;     // set_supernodes builds them (off for the batch's scratch handle)
     int sn_npan = 0;

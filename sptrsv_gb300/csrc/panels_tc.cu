@@ -62,7 +62,7 @@ static int g_panels_mode = -1;
 int panels_mode() {
     if (g_panels_mode < 0) {
         const char* e = getenv("SPTRSV_PANELS");
-        g_panels_mode = (e && strcmp(e, "tc") == 0) ? 1 : 0;
+        g_panels_mode = (e && strcmp(e, "tc") == 0) ? 1 : (e && strcmp(e, "df") == 0) ? 2 : 0;
     }
     return g_panels_mode;
 }
@@ -395,7 +395,7 @@ int launch_tc_split(const BChunk* panels, const int2* recs, int nrec, int sm_cou
 }  // namespace sptrsv
 
 extern "C" int sptrsv_set_panels_mode(int mode) {
-    if (mode != 0 && mode != 1) return SPTRSV_ERR_INVALID_ARG;
+    if (mode != 0 && mode != 1 && mode != 2) return SPTRSV_ERR_INVALID_ARG;
     const int prev = sptrsv::panels_mode();
     sptrsv::g_panels_mode = mode;
     return prev;

@@ -415,6 +415,18 @@ int Handle::set_supernodes(int sn, const int* snodes_host) {
         if ((rc = sn_gtc.ensure(tot)) || (rc = sn_tcrec.ensure(sizeof(int2) * recs.size()))) return rc;
         for (size_t p = 0; p < pan.size(); ++p) pan[p].gtc = sn_gtc.as<unsigned char>() + toff[p];
     }
+    // double-FP32 schedule: G as scaled FP32 pairs (laid out like sn_G) and the row exponents,
+    // indexed by the matrix row, converted below
+    const bool df = panels_mode() == 2 && build_tc;
+    if (df) {
+        if ((rc = sn_ghl.ensure(sizeof(float2) * (size_t)std::max(1LL, gtot))) ||
+            (rc = sn_gexp.ensure(sizeof(int) * (size_t)std::max(1, n))))
+            return rc;
+        for (BChunk& c : pan) {
+            c.ghl = sn_ghl.as<float2>() + (c.g64 - sn_G.as<double>());
+            c.gexp = sn_gexp.as<int>() + c.a;
+        }
+    }
     if ((rc = sn_pan.ensure(sizeof(BChunk) * pan.size())) || (rc = sn_pitems.ensure(sizeof(int2) * pit.size())))
         return rc;
     CUDA_TRY(cudaMemcpyAsync(sn_pan.p, pan.data(), sizeof(BChunk) * pan.size(), cudaMemcpyHostToDevice, st));
@@ -425,6 +437,7 @@ int Handle::set_supernodes(int sn, const int* snodes_host) {
             return rc;
         sn_tc = true;
     }
+    if (df && (rc = launch_g_df(sn_pan.as<BChunk>(), (int)pan.size(), st, &launches))) return rc;
     CUDA_TRY(cudaStreamSynchronize(st));
     sn_npan = (int)pan.size();
     sn_npitems = (unsigned)pit.size();
