@@ -272,23 +272,32 @@ k_window(int n, const int* __restrict__ rp, const int* __restrict__ col, const T
         }
         // the lane's entries through one pointer: the staged copy in shared memory, else global
         const int* rcol = staged ? S.col + ds * L::kCap + (s - e0) : col + s;
-        const T* rval = nullptr;
-        if constexpr (!kLevels) rval = staged ? S.val + ds * L::kCap + (s - e0) : val + s;
+        T* rval = nullptr;  // the lane's row values (staged: scaled in place below)
+        if constexpr (!kLevels) rval = staged ? S.val + ds * L::kCap + (s - e0) : const_cast<T*>(val) + s;
         auto ecol = [&](int q) -> int { return rcol[q - s]; };
-        auto eval = [&](int q) -> T {
-            if constexpr (kLevels) return T(0);
-            else return rval[q - s];
-        };
-        T v = T(0), acc = T(0), di = T(0), bd = T(0), vs = T(0), p = T(0);
-        bool scaled = false, fail = false;
+        T acc = T(0), di = T(0), p = T(0);  // levels: acc; solves: p = b_i / U_ii + sum of w_ij x_j
+        bool fail = false;
         if (!done) {
             if constexpr (!kLevels) {
                 di = S.inv[ds * 32 + lane];
-                bd = S.bb[ds * 32 + lane] * di;
+                p = S.bb[ds * 32 + lane] * di;
+                // the staged row values become the weights w_ij = -U_ij / U_ii once, so that a
+                // dependency hop costs one FMA and no round multiplies
+                if (staged)
+                    for (int q = s + 1; q <= k; ++q) rval[q - s] = -rval[q - s] * di;
             }
+        }
+        __syncwarp();
+        // the weight of entry q: staged ones are scaled already, global ones are scaled here
+        auto weight = [&](int q) -> T {
+            if constexpr (kLevels) return T(0);
+            else return staged ? rval[q - s] : -rval[q - s] * di;
+        };
+        T v = T(0);  // the head's weight
+        if (!done) {
             if (k > s) {
                 c = ecol(k);
-                v = eval(k);
+                v = weight(k);
             }
             // far columns (blocks <= t-W-1, all done) from global x, four loads in flight
             while (k > s && c >= far) {
@@ -304,7 +313,7 @@ k_window(int n, const int* __restrict__ rp, const int* __restrict__ col, const T
                     use[q] = use[q - 1] && kq > s;
                     cq[q] = use[q] ? ecol(kq) : 0;
                     use[q] = use[q] && cq[q] >= far;
-                    vq[q] = use[q] ? eval(kq) : T(0);
+                    vq[q] = use[q] ? weight(kq) : T(0);
                 }
 #pragma unroll
                 for (int q = 0; q < 4; ++q) xq[q] = use[q] ? win_ld<T>(x + cq[q]) : T(0);
@@ -331,14 +340,14 @@ k_window(int n, const int* __restrict__ rp, const int* __restrict__ col, const T
                 for (int q = 0; q < 4; ++q) {
                     if (use[q]) {
                         if constexpr (kLevels) acc = max(acc, xq[q]);
-                        else acc = fma(vq[q], xq[q], acc);
+                        else p = fma(vq[q], xq[q], p);
                         ++used;
                     }
                 }
                 k -= used;
                 if (k > s) {
                     c = ecol(k);
-                    v = eval(k);
+                    v = weight(k);
                 }
             }
         }
@@ -349,28 +358,12 @@ k_window(int n, const int* __restrict__ rp, const int* __restrict__ col, const T
         auto walk = [&]() {
             while (k > s) {
                 const T xv = c >= far ? win_ld<T>(x + c) : vring[c & RM];
-                if (WinVal<T>::is_pending(xv)) {
-                    if constexpr (!kLevels) {
-                        if (!scaled) {  // from here on one FMA per term
-                            p = fma(-acc, di, bd);
-                            vs = -v * di;
-                            scaled = true;
-                        }
-                    }
-                    break;
-                }
-                if constexpr (kLevels) {
-                    acc = max(acc, xv);
-                } else {
-                    if (scaled) p = fma(vs, xv, p);
-                    else acc = fma(v, xv, acc);
-                }
+                if (WinVal<T>::is_pending(xv)) break;
+                if constexpr (kLevels) acc = max(acc, xv);
+                else p = fma(v, xv, p);
                 if (--k > s) {
                     c = ecol(k);
-                    v = eval(k);
-                    if constexpr (!kLevels) {
-                        if (scaled) vs = -v * di;
-                    }
+                    v = weight(k);
                 }
             }
         };
@@ -379,7 +372,7 @@ k_window(int n, const int* __restrict__ rp, const int* __restrict__ col, const T
                 xm = T(1) + acc;
                 lmax = max(lmax, xm);
             } else {
-                xm = Pend<T>::fix(scaled ? p : fma(-acc, di, bd));
+                xm = Pend<T>::fix(p);
             }
             vring[i & RM] = xm;  // global x is written once the whole block is done
             done = true;
@@ -396,18 +389,15 @@ k_window(int n, const int* __restrict__ rp, const int* __restrict__ col, const T
         // 2M-row system: 140.5 against 131.0 ms for the solve, 97.2 against 80.4 ms for the
         // levels, same GPU; so did two entries a round, and an L1 prefetch of the far columns.
         // Writing each finished row to global x at once, rather than the block's 32 rows in one
-        // coalesced store at its end, cost 131.1 against 118.1 ms.)
-        // Registers hold the head (entry k: column c, scaled weight w = -U_ik / U_ii) and the next
-        // entry (cn, wn: k-1, an index past the row's start clamped to it and never consumed),
-        // loaded a round ahead.
-        T w = T(0), wn = T(0);
+        // coalesced store at its end, cost 131.1 against 118.1 ms; forming each next weight by a
+        // multiply in the round, rather than scaling the staged row once, 118.2 against 110.8 ms.)
+        // Registers hold the head (entry k: column c, weight w) and the next entry (cn, wn: k-1, an
+        // index past the row's start clamped to it and never consumed), loaded a round ahead.  The
+        // loop is compiled twice: for a staged block its weights are loads, for a block read from
+        // global memory each is scaled as it is loaded.
+        T w = v, wn = T(0);
         int cn = 0;
-        auto weight = [&](int q) -> T {
-            if constexpr (kLevels) return T(0);
-            else return -eval(q) * di;
-        };
         if (!done) {
-            if constexpr (!kLevels) w = vs;
             const int k1 = max(k - 1, s);
             cn = ecol(k1);
             wn = weight(k1);
@@ -415,47 +405,54 @@ k_window(int n, const int* __restrict__ rp, const int* __restrict__ col, const T
         __syncwarp();  // the lanes' ring stores of rows finished above before the rounds' loads
         // the budget's timer starts at the block for short budgets, else at round 31 of the block
         uint64_t t0 = budget < 1000000 ? gtimer() : 0;
-        unsigned cd = 31;  // rounds to the next timer check
-        for (;;) {
-            if (__all_sync(0xffffffffu, done)) break;
-            // The head's value from the ring: rows of this block and of the blocks in flight are
-            // stored there when they finish (the __syncwarp that ends a round orders this warp's
-            // stores before the next round's loads).  A column beyond the ring's reach is read
-            // from global x: rows need not be sorted, so such an entry can follow a near one (rare;
-            // the far loop took the sorted case).  A finished lane's stale column reads a slot whose
-            // value is discarded.
-            T x0;
-            if (__builtin_expect(c >= far, 0)) x0 = win_ld<T>(x + c);
-            else x0 = vring[c & RM];
-            const bool rdy = !done && !WinVal<T>::is_pending(x0);
-            if constexpr (kLevels) acc = rdy ? max(acc, x0) : acc;
-            else p = rdy ? fma(w, x0, p) : p;
-            k -= (int)rdy;
-            c = rdy ? cn : c;
-            if constexpr (!kLevels) w = rdy ? wn : w;
-            {
-                // the entry after the head, for the next round (a repeated load when nothing moved)
-                const int k1 = max(k - 1, s);
-                cn = ecol(k1);
-                wn = weight(k1);
-            }
-            if (rdy && k <= s) finish();
-            __syncwarp();
-            // checked at round 31 of a block (a 32-row chain takes 32 rounds) and every 256 after
-            if (--cd == 0) {
-                cd = 256;
-                if (aborted(ctl)) fail = true;
-                else if (t0 == 0) t0 = gtimer();
-                else if ((int64_t)(gtimer() - t0) > budget) {
-                    record_error(ctl, SPTRSV_ERR_TIMEOUT);
-                    fail = true;
+        auto rounds = [&](auto staged_c) {
+            constexpr bool kStaged = decltype(staged_c)::value;
+            (void)kStaged;  // unused by the level analysis (no weights)
+            unsigned cd = 31;  // rounds to the next timer check
+            for (;;) {
+                if (__all_sync(0xffffffffu, done)) break;
+                // The head's value from the ring: rows of this block and of the blocks in flight
+                // are stored there when they finish (the __syncwarp that ends a round orders this
+                // warp's stores before the next round's loads).  A column beyond the ring's reach
+                // is read from global x: rows need not be sorted, so such an entry can follow a
+                // near one (rare; the far loop took the sorted case).  A finished lane's stale
+                // column reads a slot whose value is discarded.
+                T x0;
+                if (__builtin_expect(c >= far, 0)) x0 = win_ld<T>(x + c);
+                else x0 = vring[c & RM];
+                const bool rdy = !done && !WinVal<T>::is_pending(x0);
+                if constexpr (kLevels) acc = rdy ? max(acc, x0) : acc;
+                else p = rdy ? fma(w, x0, p) : p;
+                k -= (int)rdy;
+                c = rdy ? cn : c;
+                if constexpr (!kLevels) w = rdy ? wn : w;
+                {
+                    // the entry after the head, for the next round (a repeated load when nothing
+                    // moved)
+                    const int k1 = max(k - 1, s);
+                    cn = ecol(k1);
+                    if constexpr (!kLevels) wn = kStaged ? rval[k1 - s] : -rval[k1 - s] * di;
                 }
-                if (__any_sync(0xffffffffu, fail)) {
-                    fail = true;
-                    break;
+                if (rdy && k <= s) finish();
+                __syncwarp();
+                // checked at round 31 of a block (a 32-row chain takes 32 rounds) and every 256 after
+                if (--cd == 0) {
+                    cd = 256;
+                    if (aborted(ctl)) fail = true;
+                    else if (t0 == 0) t0 = gtimer();
+                    else if ((int64_t)(gtimer() - t0) > budget) {
+                        record_error(ctl, SPTRSV_ERR_TIMEOUT);
+                        fail = true;
+                    }
+                    if (__any_sync(0xffffffffu, fail)) {
+                        fail = true;
+                        break;
+                    }
                 }
             }
-        }
+        };
+        if (staged) rounds(std::true_type{});
+        else rounds(std::false_type{});
         if (__any_sync(0xffffffffu, fail)) {
             cpa_wait_all();  // the warp's own copies in flight end before it returns
             return;
