@@ -45,6 +45,7 @@
 #include <type_traits>
 #include "common.cuh"
 #include "kernels.cuh"
+namespace sptrsv { int window_backoff_ns(); int window_warps(); }
 
 namespace sptrsv {
 
@@ -390,7 +391,9 @@ k_window(int n, const int* __restrict__ rp, const int* __restrict__ col, const T
         // levels, same GPU; so did two entries a round, and an L1 prefetch of the far columns.
         // Writing each finished row to global x at once, rather than the block's 32 rows in one
         // coalesced store at its end, cost 131.1 against 118.1 ms; forming each next weight by a
-        // multiply in the round, rather than scaling the staged row once, 118.2 against 110.8 ms.)
+        // multiply in the round, rather than scaling the staged row once, 118.2 against 110.8 ms;
+        // one round per loop pass instead of two (one vote, one timer countdown per pass), 110.8
+        // against 107.0 ms and 79.9 against 76.2 ms for the levels.)
         // Registers hold the head (entry k: column c, weight w) and the next entry (cn, wn: k-1, an
         // index past the row's start clamped to it and never consumed), loaded a round ahead.  The
         // loop is compiled twice: for a staged block its weights are loads, for a block read from
@@ -408,9 +411,7 @@ k_window(int n, const int* __restrict__ rp, const int* __restrict__ col, const T
         auto rounds = [&](auto staged_c) {
             constexpr bool kStaged = decltype(staged_c)::value;
             (void)kStaged;  // unused by the level analysis (no weights)
-            unsigned cd = 31;  // rounds to the next timer check
-            for (;;) {
-                if (__all_sync(0xffffffffu, done)) break;
+            auto step = [&]() {
                 // The head's value from the ring: rows of this block and of the blocks in flight
                 // are stored there when they finish (the __syncwarp that ends a round orders this
                 // warp's stores before the next round's loads).  A column beyond the ring's reach
@@ -433,10 +434,25 @@ k_window(int n, const int* __restrict__ rp, const int* __restrict__ col, const T
                     cn = ecol(k1);
                     if constexpr (!kLevels) wn = kStaged ? rval[k1 - s] : -rval[k1 - s] * di;
                 }
-                if (rdy && k <= s) finish();
+                {
+                    // the row's completion without a branch: value, ring store, flag
+                    const bool fin = rdy && k <= s;
+                    T xf;
+                    if constexpr (kLevels) xf = T(1) + acc;
+                    else xf = Pend<T>::fix(p);
+                    xm = fin ? xf : xm;
+                    if constexpr (kLevels) lmax = fin ? max(lmax, xf) : lmax;
+                    if (fin) vring[i & RM] = xf;
+                    done = done || fin;
+                }
                 __syncwarp();
-                // checked at round 31 of a block (a 32-row chain takes 32 rounds) and every 256 after
-                if (--cd == 0) {
+            };
+            int cd = 31;  // rounds to the next timer check (two per loop pass)
+            for (;;) {
+                if (__all_sync(0xffffffffu, done)) break;
+                step();
+                step();  // harmless when every lane finished in the first
+                if ((cd -= 2) <= 0) {
                     cd = 256;
                     if (aborted(ctl)) fail = true;
                     else if (t0 == 0) t0 = gtimer();
