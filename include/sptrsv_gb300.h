@@ -221,10 +221,9 @@ SPTRSV_API int sptrsv_set_panels_mode(int mode);
  * is allocated: the spin control block and the reciprocal diagonal live in one fixed device
  * array of SPTRSV_NOALLOC_MAX_ROWS * 8 + 256 bytes that every GPU loading this library holds
  * until the process exits.  n above SPTRSV_NOALLOC_MAX_ROWS returns SPTRSV_ERR_TOO_LARGE.
- * The first call on a device looks up that device's array address (cudaGetSymbolAddress), so
- * make the first call before any stream capture starts.  The matrix is checked first (same
- * statuses as sptrsv_analyse_*).  The call is synchronous: it returns the solve's status after
- * the stream has drained.  All calls in a process share the array and each rewrites it: the
+ * The matrix is checked first (same statuses as sptrsv_analyse_*).  The call is synchronous: it
+ * returns the solve's status after the stream has drained, so it cannot be captured into a CUDA
+ * graph.  All calls in a process share the array and each rewrites it: the
  * library holds one lock for the whole of each call, so calls made from several host threads
  * run one after another whatever stream they name.  The array keeps the last call's contents;
  * each call clears what must start at zero. */

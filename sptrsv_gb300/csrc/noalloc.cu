@@ -11,10 +11,9 @@
 // (SPTRSV_NOALLOC_MAX_ROWS * 8 bytes + 256) until the process exits.
 //
 // Host code must not pass `g_noalloc_scratch` itself to a kernel -- on the host that name is
-// only a stand-in, not a device address.  The device address is looked up once per device,
-// with that device current, by cudaGetSymbolAddress on the first call made on that device, so
-// that first call should come before any stream capture begins (after cudaDeviceReset the
-// cached address is stale, as is every other device object of the library).  All calls share
+// only a stand-in, not a device address.  Every call looks the device address up with
+// cudaGetSymbolAddress on the current device.  The call synchronises its stream, so it cannot be
+// captured into a CUDA graph.  All calls share
 // the one array and it keeps the previous call's contents: each call clears the control block
 // and rewrites the reciprocal diagonal for its rows before the solve.  A call runs in two
 // phases on its stream (checks, then the solve), so every call in the process holds one lock
@@ -58,18 +57,14 @@ __global__ void k_noalloc_prepare(int n, int nnz, const int* __restrict__ rp, co
 }
 
 static std::mutex g_noalloc_mu;
-static NoallocScratch* g_noalloc_addr[64];  // device address of the array, per device
 
-// Caller holds g_noalloc_mu.
-static int noalloc_scratch(int device, NoallocScratch** out) {
-    if (device < 0 || device >= 64) return SPTRSV_ERR_INVALID_ARG;
-    if (!g_noalloc_addr[device]) {
-        void* p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || !p) return set_cuda_error(e, "cudaGetSymbolAddress");
-        g_noalloc_addr[device] = static_cast<NoallocScratch*>(p);
-    }
-    *out = g_noalloc_addr[device];
+// The array's device address on the current device, looked up on every call (cheap next to the
+// call's two stream synchronisations, and never stale after a cudaDeviceReset reloads the module).
+static int noalloc_scratch(NoallocScratch** out) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) return set_cuda_error(e, "cudaGetSymbolAddress");
+    *out = static_cast<NoallocScratch*>(p);
     return 0;
 }
 
@@ -85,7 +80,7 @@ extern "C" int sptrsv_solve_noalloc(int n, int nnz, const int* d_row_ptr, const 
     // one call at a time in this process: the checks and the solve both use the shared array
     std::lock_guard<std::mutex> lk(g_noalloc_mu);
     NoallocScratch* s = nullptr;
-    int rc = noalloc_scratch(device, &s);
+    int rc = noalloc_scratch(&s);
     if (rc) return rc;
     int sm_count = 0;
     CUDA_TRY(cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, device));
