@@ -154,7 +154,7 @@ int Handle::ensure_levels() {
     const int sgrid = sm_count * 4;
     CUDA_TRY(cudaMemsetAsync(levels.p, 0, sizeof(int) * (size_t)n, st));
     if (levels_kernel() == 0) {
-        if ((rc = launch_window_levels(n, rp, col, levels.as<int>(), ctl, kDefaultBudgetNs, st, &launches))) return rc;
+        if ((rc = launch_window_levels(n, nnz, rp, col, levels.as<int>(), ctl, kDefaultBudgetNs, st, &launches))) return rc;
     } else {
         k_levels<<<sm_count * 2, 256, 0, st>>>(n, rp, col, levels.as<int>(), ctl, kDefaultBudgetNs);
         ++launches;
@@ -377,6 +377,7 @@ int Handle::enqueue(const sptrsv_opts& o, const double* b, double* x, int rhs, i
     a.budget = o.spin_budget_ns;
     a.sm_count = sm_count;
     a.warps = resident_warps(o);
+    a.nnz = nnz;
     a.st = st;
     a.launches = &launches;
     if (o.precision == SPTRSV_PREC_FP64) {

@@ -61,6 +61,7 @@ struct SolveArgs {
     int64_t budget;
     int sm_count;
     int warps;           // resident warps to launch (0 = full occupancy)
+    long long nnz;       // entries of U (0 = unknown); the window kernel sizes its CTA by it
     cudaStream_t st;
     int64_t* launches;
 };
@@ -73,7 +74,8 @@ int launch_push_csc(const SolveArgs& a, const int* cp, const int* crow, const do
 int launch_levelset(bool f32, const SolveArgs& a, int max_level, const int* lptr, const int* lrows);
 // window.cu: one CTA walks the rows in 32-row blocks with recent x in a shared-memory ring
 int launch_window(bool f32, const SolveArgs& a);
-int launch_window_levels(int n, const int* rp, const int* col, int* level, Ctl* ctl, int64_t budget, cudaStream_t st,
+int launch_window_levels(int n, long long nnz, const int* rp, const int* col, int* level, Ctl* ctl, int64_t budget,
+                         cudaStream_t st,
                          int64_t* launches);
 int window_warps();
 int launch_transpose(bool to_row_major, const double* src, double* dst, int n, int rhs, cudaStream_t st,

@@ -1324,6 +1324,7 @@ int launch_exact_inner(const RefineArgs& a, int schedule, int rows_per_warp, int
     s.budget = a.budget;
     s.sm_count = a.sm_count;
     s.warps = warps;
+    s.nnz = a.nnz;
     s.st = a.st;
     s.launches = a.launches;
     if (schedule == SPTRSV_SCHED_LEVELSET) return launch_levelset(true, s, max_level, lptr, lrows);

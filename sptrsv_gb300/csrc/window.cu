@@ -289,12 +289,21 @@ k_window(int n, const int* __restrict__ rp, const int* __restrict__ col, const T
             }
         }
         __syncwarp();
-        // the weight of entry q: staged ones are scaled already, global ones are scaled here
+        // xm is this lane's value once its row is finished.
+        T xm = WinVal<T>::pending();
+        // The block's rows, compiled twice: a staged block's weights are loads, a block read from
+        // global memory has each weight scaled as it is loaded.
+        auto block_rows = [&](auto staged_c) {
+        constexpr bool kStaged = decltype(staged_c)::value;
+        (void)kStaged;  // the level analysis has no weights
         auto weight = [&](int q) -> T {
             if constexpr (kLevels) return T(0);
-            else return staged ? rval[q - s] : -rval[q - s] * di;
+            else if constexpr (kStaged) return rval[q - s];
+            else return -rval[q - s] * di;
         };
         T v = T(0);  // the head's weight
+        T p2 = T(0);  // a second accumulator for the setup's FMAs (two chains instead of one)
+        (void)p2;
         if (!done) {
             if (k > s) {
                 c = ecol(k);
@@ -341,6 +350,7 @@ k_window(int n, const int* __restrict__ rp, const int* __restrict__ col, const T
                 for (int q = 0; q < 4; ++q) {
                     if (use[q]) {
                         if constexpr (kLevels) acc = max(acc, xq[q]);
+                        else if (q & 1) p2 = fma(vq[q], xq[q], p2);
                         else p = fma(vq[q], xq[q], p);
                         ++used;
                     }
@@ -353,19 +363,23 @@ k_window(int n, const int* __restrict__ rp, const int* __restrict__ col, const T
             }
         }
         // the rest: one walk over what is ready, then lockstep rounds over the remaining entries.
-        // xm is this lane's value once its row is finished.
-        T xm = WinVal<T>::pending();
-        // walk right to left consuming ready entries; stops at the first pending one
+        // walk right to left consuming ready entries (into the two accumulators by the entry's
+        // parity); stops at the first pending one
         auto walk = [&]() {
             while (k > s) {
                 const T xv = c >= far ? win_ld<T>(x + c) : vring[c & RM];
                 if (WinVal<T>::is_pending(xv)) break;
                 if constexpr (kLevels) acc = max(acc, xv);
+                else if (k & 1) p2 = fma(v, xv, p2);
                 else p = fma(v, xv, p);
                 if (--k > s) {
                     c = ecol(k);
                     v = weight(k);
                 }
+            }
+            if constexpr (!kLevels) {
+                p += p2;
+                p2 = T(0);
             }
         };
         auto finish = [&]() {
@@ -393,12 +407,15 @@ k_window(int n, const int* __restrict__ rp, const int* __restrict__ col, const T
         // coalesced store at its end, cost 131.1 against 118.1 ms; forming each next weight by a
         // multiply in the round, rather than scaling the staged row once, 118.2 against 110.8 ms;
         // one round per loop pass instead of two (one vote, one timer countdown per pass), 110.8
-        // against 107.0 ms and 79.9 against 76.2 ms for the levels.)
+        // against 107.0 ms and 79.9 against 76.2 ms for the levels; four per pass, 99.7 and
+        // 73.4 ms.  With the setup specialised for staged blocks and two FMA chains in it, eight
+        // warps take 77.1 and 44.7 ms.)
         // Registers hold the head (entry k: column c, weight w) and the next entry (cn, wn: k-1, an
         // index past the row's start clamped to it and never consumed), loaded a round ahead.  The
         // loop is compiled twice: for a staged block its weights are loads, for a block read from
-        // global memory each is scaled as it is loaded.
+        // global memory each is scaled as it is loaded (see block_rows).
         T w = v, wn = T(0);
+        (void)w;
         int cn = 0;
         if (!done) {
             const int k1 = max(k - 1, s);
@@ -408,9 +425,7 @@ k_window(int n, const int* __restrict__ rp, const int* __restrict__ col, const T
         __syncwarp();  // the lanes' ring stores of rows finished above before the rounds' loads
         // the budget's timer starts at the block for short budgets, else at round 31 of the block
         uint64_t t0 = budget < 1000000 ? gtimer() : 0;
-        auto rounds = [&](auto staged_c) {
-            constexpr bool kStaged = decltype(staged_c)::value;
-            (void)kStaged;  // unused by the level analysis (no weights)
+        auto rounds = [&]() {
             auto step = [&]() {
                 // The head's value from the ring: rows of this block and of the blocks in flight
                 // are stored there when they finish (the __syncwarp that ends a round orders this
@@ -432,7 +447,7 @@ k_window(int n, const int* __restrict__ rp, const int* __restrict__ col, const T
                     // moved)
                     const int k1 = max(k - 1, s);
                     cn = ecol(k1);
-                    if constexpr (!kLevels) wn = kStaged ? rval[k1 - s] : -rval[k1 - s] * di;
+                    wn = weight(k1);
                 }
                 {
                     // the row's completion without a branch: value, ring store, flag
@@ -447,12 +462,14 @@ k_window(int n, const int* __restrict__ rp, const int* __restrict__ col, const T
                 }
                 __syncwarp();
             };
-            int cd = 31;  // rounds to the next timer check (two per loop pass)
+            int cd = 31;  // rounds to the next timer check (four per loop pass)
             for (;;) {
                 if (__all_sync(0xffffffffu, done)) break;
                 step();
-                step();  // harmless when every lane finished in the first
-                if ((cd -= 2) <= 0) {
+                step();  // harmless when every lane finished in an earlier one
+                step();
+                step();
+                if ((cd -= 4) <= 0) {
                     cd = 256;
                     if (aborted(ctl)) fail = true;
                     else if (t0 == 0) t0 = gtimer();
@@ -467,8 +484,10 @@ k_window(int n, const int* __restrict__ rp, const int* __restrict__ col, const T
                 }
             }
         };
-        if (staged) rounds(std::true_type{});
-        else rounds(std::false_type{});
+        rounds();
+        };
+        if (staged) block_rows(std::true_type{});
+        else block_rows(std::false_type{});
         if (__any_sync(0xffffffffu, fail)) {
             cpa_wait_all();  // the warp's own copies in flight end before it returns
             return;
@@ -506,10 +525,26 @@ static int window_launch(int n, const int* rp, const int* col, const T* val, con
     return 0;
 }
 
+// Warps of the window CTA: SPTRSV_WINDOW_WARPS = 2, 4, 8 or 16 forces one; otherwise 8 while a
+// 32-row block's entries (at the matrix's mean row length) fill at most 90 % of the 8-warp staging
+// buffer, else 4 (more warps hide more of each block's setup behind the other warps' rounds, but
+// leave less staging space per warp).  Measured on the 2M-row system (8.6 entries per row, same
+// GPU): the solve 124.7 / 77.1 / 92.7 ms and the levels 74.4 / 44.7 / 52.7 ms at 4 / 8 / 16 warps;
+// on 200k-row random factors the solve at 8 warps 7.7 / 12.4 / 15.8 ms against 12.4 / 17.4 /
+// 21.8 ms at 4 with 8.6 / 15.5 / 21.7 entries per row, and 51.2 against 25.9 ms with 27.4 (whose
+// blocks no longer fit 8 warps' buffers).
 template <typename T>
-static int window_dispatch(int n, const int* rp, const int* col, const T* val, const T* invd, const T* b, T* x,
-                           Ctl* ctl, int64_t budget, cudaStream_t st, int64_t* launches) {
-    switch (window_warps()) {
+static int window_pick_warps(int n, long long nnz) {
+    const int forced = window_warps();
+    if (forced) return forced;
+    if (n <= 0 || nnz <= 0) return 4;
+    return 32.0 * (double)nnz / n <= 0.9 * WinLayout<T, 8>::kCap ? 8 : 4;
+}
+
+template <typename T>
+static int window_dispatch(int n, long long nnz, const int* rp, const int* col, const T* val, const T* invd,
+                           const T* b, T* x, Ctl* ctl, int64_t budget, cudaStream_t st, int64_t* launches) {
+    switch (window_pick_warps<T>(n, nnz)) {
         case 2: return window_launch<T, 2>(n, rp, col, val, invd, b, x, ctl, budget, st, launches);
         case 16: return window_launch<T, 16>(n, rp, col, val, invd, b, x, ctl, budget, st, launches);
         case 8: return window_launch<T, 8>(n, rp, col, val, invd, b, x, ctl, budget, st, launches);
@@ -517,12 +552,12 @@ static int window_dispatch(int n, const int* rp, const int* col, const T* val, c
     }
 }
 
-// Warps of the window CTA (SPTRSV_WINDOW_WARPS = 2, 4, 8 or 16).
+// SPTRSV_WINDOW_WARPS (2, 4, 8 or 16), or 0 when unset.
 int window_warps() {
     static int w = [] {
         const char* e = getenv("SPTRSV_WINDOW_WARPS");
-        const int v = e ? atoi(e) : 4;
-        return (v == 2 || v == 4 || v == 8 || v == 16) ? v : 4;
+        const int v = e ? atoi(e) : 0;
+        return (v == 2 || v == 4 || v == 8 || v == 16) ? v : 0;
     }();
     return w;
 }
@@ -530,15 +565,15 @@ int window_warps() {
 int launch_window(bool f32, const SolveArgs& a) {
     if (a.rhs != 1) return SPTRSV_ERR_UNSUPPORTED;
     if (f32)
-        return window_dispatch<float>(a.n, a.rp, a.col, (const float*)a.val, (const float*)a.invd, (const float*)a.b,
-                                      (float*)a.x, a.ctl, a.budget, a.st, a.launches);
-    return window_dispatch<double>(a.n, a.rp, a.col, (const double*)a.val, (const double*)a.invd,
+        return window_dispatch<float>(a.n, a.nnz, a.rp, a.col, (const float*)a.val, (const float*)a.invd,
+                                      (const float*)a.b, (float*)a.x, a.ctl, a.budget, a.st, a.launches);
+    return window_dispatch<double>(a.n, a.nnz, a.rp, a.col, (const double*)a.val, (const double*)a.invd,
                                    (const double*)a.b, (double*)a.x, a.ctl, a.budget, a.st, a.launches);
 }
 
-int launch_window_levels(int n, const int* rp, const int* col, int* level, Ctl* ctl, int64_t budget, cudaStream_t st,
-                         int64_t* launches) {
-    return window_dispatch<int>(n, rp, col, nullptr, nullptr, nullptr, level, ctl, budget, st, launches);
+int launch_window_levels(int n, long long nnz, const int* rp, const int* col, int* level, Ctl* ctl, int64_t budget,
+                         cudaStream_t st, int64_t* launches) {
+    return window_dispatch<int>(n, nnz, rp, col, nullptr, nullptr, nullptr, level, ctl, budget, st, launches);
 }
 
 }  // namespace sptrsv
