@@ -46,6 +46,7 @@
 #include "common.cuh"
 #include "kernels.cuh"
 namespace sptrsv { int window_backoff_ns(); int window_warps(); }
+namespace sptrsv { int window_backoff_ns(); int window_warps(); }
 
 namespace sptrsv {
 
@@ -409,7 +410,7 @@ k_window(int n, const int* __restrict__ rp, const int* __restrict__ col, const T
         // one round per loop pass instead of two (one vote, one timer countdown per pass), 110.8
         // against 107.0 ms and 79.9 against 76.2 ms for the levels; four per pass, 99.7 and
         // 73.4 ms.  With the setup specialised for staged blocks and two FMA chains in it, eight
-        // warps take 77.1 and 44.7 ms.)
+        // warps take 77.1 and 44.7 ms; eight rounds per pass, 73.6 and 40.4 ms.)
         // Registers hold the head (entry k: column c, weight w) and the next entry (cn, wn: k-1, an
         // index past the row's start clamped to it and never consumed), loaded a round ahead.  The
         // loop is compiled twice: for a staged block its weights are loads, for a block read from
@@ -462,14 +463,18 @@ k_window(int n, const int* __restrict__ rp, const int* __restrict__ col, const T
                 }
                 __syncwarp();
             };
-            int cd = 31;  // rounds to the next timer check (four per loop pass)
+            int cd = 31;  // rounds to the next timer check (eight per loop pass)
             for (;;) {
                 if (__all_sync(0xffffffffu, done)) break;
                 step();
                 step();  // harmless when every lane finished in an earlier one
                 step();
                 step();
-                if ((cd -= 4) <= 0) {
+                step();
+                step();
+                step();
+                step();
+                if ((cd -= 8) <= 0) {
                     cd = 256;
                     if (aborted(ctl)) fail = true;
                     else if (t0 == 0) t0 = gtimer();
