@@ -220,6 +220,91 @@ k_window(int n, const int* __restrict__ rp, const int* __restrict__ col, const T
 
     int lmax = 0;  // levels: largest level of this lane's rows
     int j = 0;     // this warp's block count
+    // The lane's state for the warp's next block, prepared at the end of the block before it (in
+    // the prologue for the first): its staged row scaled to the weights w_ij = -U_ij / U_ii (a
+    // dependency hop then costs one FMA and no round multiplies), and its far columns -- rows of
+    // blocks finished long before, read from global x -- folded into the partial sum.  So a block
+    // starts with its walk over the ring.
+    int nk = 0;                   // the entry to consume next
+    T np = T(0), nacc = T(0);     // partial sums: b_i / U_ii + far terms (solves); max (levels)
+    bool nfail = false;           // a far value never arrived (not expected): the lane gives up
+    auto prepare = [&](int u, int jj) {
+        const int ds_u = jj & 1;
+        const int top = win_top(n, u), lo = win_lo(n, u);
+        const int* rS = S.rp + (jj % 3) * L::kRpSlot;
+        const int e0 = rS[0];
+        const bool staged = rS[top - lo] - e0 <= L::kCap;
+        const int i = top - 1 - lane;
+        const int far = top + reach;
+        nk = e0;
+        np = nacc = T(0);
+        nfail = false;
+        if (i < lo) return;
+        const int s = rS[i - lo];
+        int k = rS[i - lo + 1] - 1;
+        const int* rcol = staged ? S.col + ds_u * L::kCap + (s - e0) : col + s;
+        T* rval = nullptr;
+        T di = T(0), p = T(0), p2 = T(0), acc = T(0);
+        if constexpr (!kLevels) {
+            rval = staged ? S.val + ds_u * L::kCap + (s - e0) : const_cast<T*>(val) + s;
+            di = S.inv[ds_u * 32 + lane];
+            p = S.bb[ds_u * 32 + lane] * di;
+            if (staged)
+                for (int q = s + 1; q <= k; ++q) rval[q - s] = -rval[q - s] * di;
+        }
+        auto weight = [&](int q) -> T {
+            if constexpr (kLevels) return T(0);
+            else return staged ? rval[q - s] : -rval[q - s] * di;
+        };
+        // far columns (blocks <= u-W-1, done before block u-W started), four loads in flight
+        int c = k > s ? rcol[k - s] : 0;
+        bool fail = false;
+        while (k > s && c >= far) {
+            int cq[4];
+            T vq[4], xq[4];
+            bool use[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int kq = k - q;
+                use[q] = (q == 0 || use[q - 1]) && kq > s;
+                cq[q] = use[q] ? rcol[kq - s] : 0;
+                use[q] = use[q] && cq[q] >= far;
+                vq[q] = use[q] ? weight(kq) : T(0);
+            }
+#pragma unroll
+            for (int q = 0; q < 4; ++q) xq[q] = use[q] ? win_ld<T>(x + cq[q]) : T(0);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                // not expected: those blocks are done.  Wait all the same, bounded like every wait.
+                if (use[q] && !fail && WinVal<T>::is_pending(xq[q])) {
+                    xq[q] = win_wait<T>(x + cq[q], ctl, budget);
+                    fail = WinVal<T>::is_pending(xq[q]);
+                }
+            }
+            if (fail) break;
+            int used = 0;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                if (use[q]) {
+                    if constexpr (kLevels) acc = max(acc, xq[q]);
+                    else if (q & 1) p2 = fma(vq[q], xq[q], p2);
+                    else p = fma(vq[q], xq[q], p);
+                    ++used;
+                }
+            }
+            k -= used;
+            if (k > s) c = rcol[k - s];
+        }
+        nk = k;
+        np = p + p2;
+        nacc = acc;
+        nfail = fail;
+    };
+    if (warp < nblk) {
+        cpa_wait_all();
+        __syncwarp();
+        prepare(warp, 0);
+    }
     for (int t = warp; t < nblk; t += W, ++j) {
         // 1. start condition: blocks t-W-1 ... t-2W+1 done (lane q checks block t-W-1-q)
         {
@@ -270,26 +355,20 @@ k_window(int n, const int* __restrict__ rp, const int* __restrict__ col, const T
         int s = e0, k = e0, c = 0;  // a lane without a row (short last block) reads entry e0 harmlessly
         if (!done) {
             s = rS[i - lo];
-            k = rS[i - lo + 1] - 1;
+            k = nk;  // prepared: the far columns are folded in already
         }
         // the lane's entries through one pointer: the staged copy in shared memory, else global
         const int* rcol = staged ? S.col + ds * L::kCap + (s - e0) : col + s;
         T* rval = nullptr;  // the lane's row values (staged: scaled in place below)
         if constexpr (!kLevels) rval = staged ? S.val + ds * L::kCap + (s - e0) : const_cast<T*>(val) + s;
         auto ecol = [&](int q) -> int { return rcol[q - s]; };
-        T acc = T(0), di = T(0), p = T(0);  // levels: acc; solves: p = b_i / U_ii + sum of w_ij x_j
-        bool fail = false;
-        if (!done) {
-            if constexpr (!kLevels) {
-                di = S.inv[ds * 32 + lane];
-                p = S.bb[ds * 32 + lane] * di;
-                // the staged row values become the weights w_ij = -U_ij / U_ii once, so that a
-                // dependency hop costs one FMA and no round multiplies
-                if (staged)
-                    for (int q = s + 1; q <= k; ++q) rval[q - s] = -rval[q - s] * di;
-            }
+        // levels: acc; solves: p = b_i / U_ii + sum of w_ij x_j (the prepared part so far)
+        T acc = nacc, di = T(0), p = np;
+        bool fail = nfail;
+        if (fail) done = true;  // the lane gives up: no rounds, no publication; the warp returns
+        if constexpr (!kLevels) {
+            if (!done) di = S.inv[ds * 32 + lane];
         }
-        __syncwarp();
         // xm is this lane's value once its row is finished.
         T xm = WinVal<T>::pending();
         // The block's rows, compiled twice: a staged block's weights are loads, a block read from
@@ -309,58 +388,6 @@ k_window(int n, const int* __restrict__ rp, const int* __restrict__ col, const T
             if (k > s) {
                 c = ecol(k);
                 v = weight(k);
-            }
-            // far columns (blocks <= t-W-1, all done) from global x, four loads in flight
-            while (k > s && c >= far) {
-                int cq[4];
-                T vq[4], xq[4];
-                bool use[4];
-                cq[0] = c;
-                vq[0] = v;
-                use[0] = true;
-#pragma unroll
-                for (int q = 1; q < 4; ++q) {
-                    const int kq = k - q;
-                    use[q] = use[q - 1] && kq > s;
-                    cq[q] = use[q] ? ecol(kq) : 0;
-                    use[q] = use[q] && cq[q] >= far;
-                    vq[q] = use[q] ? weight(kq) : T(0);
-                }
-#pragma unroll
-                for (int q = 0; q < 4; ++q) xq[q] = use[q] ? win_ld<T>(x + cq[q]) : T(0);
-                bool bad = false;
-#pragma unroll
-                for (int q = 0; q < 4; ++q) bad |= use[q] && WinVal<T>::is_pending(xq[q]);
-                if (bad) {
-                    // not expected: the start condition has every block at or beyond `far` done.
-                    // Wait all the same, bounded like every other wait.
-#pragma unroll
-                    for (int q = 0; q < 4; ++q) {
-                        if (use[q] && !fail && WinVal<T>::is_pending(xq[q])) {
-                            xq[q] = win_wait<T>(x + cq[q], ctl, budget);
-                            fail = WinVal<T>::is_pending(xq[q]);
-                        }
-                    }
-                    if (fail) {
-                        done = true;  // the lane gives up: no rounds, no publication; the warp returns
-                        break;
-                    }
-                }
-                int used = 0;
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    if (use[q]) {
-                        if constexpr (kLevels) acc = max(acc, xq[q]);
-                        else if (q & 1) p2 = fma(vq[q], xq[q], p2);
-                        else p = fma(vq[q], xq[q], p);
-                        ++used;
-                    }
-                }
-                k -= used;
-                if (k > s) {
-                    c = ecol(k);
-                    v = weight(k);
-                }
             }
         }
         // the rest: one walk over what is ready, then lockstep rounds over the remaining entries.
@@ -410,7 +437,9 @@ k_window(int n, const int* __restrict__ rp, const int* __restrict__ col, const T
         // one round per loop pass instead of two (one vote, one timer countdown per pass), 110.8
         // against 107.0 ms and 79.9 against 76.2 ms for the levels; four per pass, 99.7 and
         // 73.4 ms.  With the setup specialised for staged blocks and two FMA chains in it, eight
-        // warps take 77.1 and 44.7 ms; eight rounds per pass, 73.6 and 40.4 ms.)
+        // warps take 77.1 and 44.7 ms; eight rounds per pass, 73.6 and 40.4 ms; each block
+        // prepared (its row scaled, its far columns folded in) at the end of the warp's block
+        // before it, 68.0 and 41.4 ms.)
         // Registers hold the head (entry k: column c, weight w) and the next entry (cn, wn: k-1, an
         // index past the row's start clamped to it and never consumed), loaded a round ahead.  The
         // loop is compiled twice: for a staged block its weights are loads, for a block read from
@@ -503,6 +532,12 @@ k_window(int n, const int* __restrict__ rp, const int* __restrict__ col, const T
         __threadfence_block();
         __syncwarp();
         if (lane == 0) vflag[t & (kWinFlags - 1)] = t;
+        // 6. the warp's next block: its data (staged at this block's start) has landed
+        if (t + W < nblk) {
+            cpa_wait_all();
+            __syncwarp();
+            prepare(t + W, j + 1);
+        }
     }
     cpa_wait_all();  // no copy left in flight when the warp exits
     if constexpr (kLevels) {
