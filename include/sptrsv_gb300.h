@@ -209,6 +209,30 @@ SPTRSV_API int sptrsv_measure_fp64(int device, double* gfma_per_s, double* dep_f
  * products and compensated sums; FP64-accurate).  Applies to partitions and batches built
  * afterwards; returns the previous mode. */
 SPTRSV_API int sptrsv_set_panels_mode(int mode);
+
+/* No counterpart in the reference, whose factors come from an external sparse Cholesky: the step
+ * upstream of the solve, a multifrontal supernodal Cholesky A = U^T U of a symmetric positive
+ * definite n x n matrix on the GPU.  A is host CSR (int64 row pointer) already in the elimination
+ * order; every row must hold its entries at and right of the diagonal (a full symmetric pattern
+ * or the upper triangle).  The elimination is given as nf fronts in a postorder: front t pivots
+ * rows front_start[t] .. front_start[t+1]-1 (the ranges tile 0 .. n-1 in order) and hands its
+ * update matrix to front_parent[t] > t (-1 for a root).  The host finds every front's row set;
+ * the GPU assembles each front (A's entries, its children's update matrices), factors its pivot
+ * columns and forms its update matrix in FP64 (blocked in 64-column panels).  On success *factor
+ * holds U in the solver's CSR layout (diagonal first, columns ascending) and the supernode
+ * partition: each front's pivots in pieces of at most max_width rows, each piece a dense triangle
+ * plus one shared set of columns, as sptrsv_set_supernodes takes it.  SPTRSV_ERR_ZERO_PIVOT when a
+ * pivot is not positive (A not positive definite); SPTRSV_ERR_INVALID_ARG for a tree whose
+ * updates reach rows no later front pivots. */
+SPTRSV_API int sptrsv_factor_multifrontal(int device, int n, const int64_t* a_row_ptr, const int* a_col,
+                                          const double* a_val, int nf, const int* front_start,
+                                          const int* front_parent, int max_width, void** factor);
+/* Sizes of a factor: n, entries of U, supernodes. */
+SPTRSV_API int sptrsv_factor_info(void* factor, int* n, int64_t* nnz, int* num_supernodes);
+/* Copies U (row_ptr[n+1], col[nnz], val[nnz]) and the partition (supernodes[num_supernodes+1]);
+ * any pointer may be NULL. */
+SPTRSV_API int sptrsv_factor_copy(void* factor, int64_t* row_ptr, int* col, double* val, int* supernodes);
+SPTRSV_API void sptrsv_factor_free(void* factor);
 /* Largest n accepted by sptrsv_solve_noalloc (its reciprocal diagonal lives in a fixed array). */
 #define SPTRSV_NOALLOC_MAX_ROWS (1 << 20)
 

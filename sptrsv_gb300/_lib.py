@@ -92,6 +92,10 @@ C_API = {
     "sptrsv_get_csc": ([c_vp, i32, i32, f64], c_int),
     "sptrsv_measure_fp64": ([c_int, ctypes.POINTER(c_dbl), ctypes.POINTER(c_dbl)], c_int),
     "sptrsv_set_panels_mode": ([c_int], c_int),
+    "sptrsv_factor_multifrontal": ([c_int, c_int, i64, i32, f64, c_int, i32, i32, c_int, ctypes.POINTER(c_vp)], c_int),
+    "sptrsv_factor_info": ([c_vp, _c_int_p, ctypes.POINTER(c_i64), _c_int_p], c_int),
+    "sptrsv_factor_copy": ([c_vp, i64, i32, f64, i32], c_int),
+    "sptrsv_factor_free": ([c_vp], None),
     "sptrsv_get_level_buckets": ([c_vp, i32, i32], c_int),
     "sptrsv_get_level_tasks": ([c_vp, c_int, i32], c_int),
     "sptrsv_solve": ([c_vp, ctypes.POINTER(Opts), c_vp, c_vp, c_int, c_int], c_int),

@@ -239,6 +239,63 @@ def laplace3d_nd_cholesky(g=40, leaf=8, max_width=400):
     return m
 
 
+def laplace3d_nd_matrix(g=40, leaf=8):
+    """The 7-point 3D Laplacian (diag 6, off -1) on a g^3 grid in the nested-dissection elimination
+    order of laplace3d_nd_cholesky, as CSR holding every row's entries at and right of its diagonal,
+    with that dissection's fronts: (row_ptr, col, val, front_start, front_parent, order)."""
+    order, nodes = _nd_tree(g, leaf)
+    n = g ** 3
+    inv = np.empty(n, dtype=np.int64)
+    inv[order] = np.arange(n)
+    z, rem = np.divmod(order, g * g)
+    y, x = np.divmod(rem, g)
+    rows, cols = [np.arange(n)], [np.arange(n)]
+    for dz, dy, dx in ((1, 0, 0), (-1, 0, 0), (0, 1, 0), (0, -1, 0), (0, 0, 1), (0, 0, -1)):
+        zz, yy, xx = z + dz, y + dy, x + dx
+        ok = (zz >= 0) & (zz < g) & (yy >= 0) & (yy < g) & (xx >= 0) & (xx < g)
+        i = np.nonzero(ok)[0]
+        j = inv[(zz[ok] * g + yy[ok]) * g + xx[ok]]
+        up = j > i
+        rows.append(i[up])
+        cols.append(j[up])
+    r = np.concatenate(rows)
+    c = np.concatenate(cols)
+    srt = np.lexsort((c, r))
+    r, c = r[srt], c[srt]
+    val = np.where(r == c, 6.0, -1.0)
+    row_ptr = np.zeros(n + 1, dtype=np.int64)
+    np.add.at(row_ptr, r + 1, 1)
+    row_ptr = np.cumsum(row_ptr)
+    front_start = np.array([f0 for f0, _, _ in nodes] + [n], dtype=np.int32)
+    front_parent = np.array([par for _, _, par in nodes], dtype=np.int32)
+    return row_ptr, c.astype(np.int32), val, front_start, front_parent, order
+
+
+def laplace3d_nd_cholesky_gpu(g=40, leaf=8, max_width=400, device=0):
+    """The factor of laplace3d_nd_cholesky (same order, fronts and supernodes) computed by the
+    library's GPU multifrontal Cholesky (sptrsv_factor_multifrontal)."""
+    row_ptr, col, val, fs, fp, order = laplace3d_nd_matrix(g, leaf)
+    L = _lib.lib()
+    h = ctypes.c_void_p()
+    rc = L.sptrsv_factor_multifrontal(int(device), len(row_ptr) - 1, row_ptr, col, val, len(fs) - 1, fs, fp,
+                                      int(max_width), ctypes.byref(h))
+    if rc:
+        raise RuntimeError("sptrsv_factor_multifrontal: status %d" % rc)
+    try:
+        n, nnz, nsn = ctypes.c_int(), ctypes.c_int64(), ctypes.c_int()
+        L.sptrsv_factor_info(h, ctypes.byref(n), ctypes.byref(nnz), ctypes.byref(nsn))
+        rp = np.empty(n.value + 1, dtype=np.int64)
+        cl = np.empty(nnz.value, dtype=np.int32)
+        vl = np.empty(nnz.value, dtype=np.float64)
+        sn = np.empty(nsn.value + 1, dtype=np.int32)
+        L.sptrsv_factor_copy(h, rp, cl, vl, sn)
+    finally:
+        L.sptrsv_factor_free(h)
+    m = Csr(rp, cl, vl, sn)
+    m.perm = order
+    return m
+
+
 def supernodal_case(g=40, rhs=1, seed=3):
     """The supernodal workload: 40^3 3D Laplacian factor under nested dissection, B ~ U[-1,1]."""
     m = laplace3d_nd_cholesky(g)

@@ -573,3 +573,25 @@ def test_dropin_base_gauss_lower_rejects_upper(golden):
     col, val = golden["csr_6_upper/col"], golden["csr_6_upper/val"]
     x = np.zeros(6)
     assert sp.base_gauss_lower(6, val.copy(), rp.copy(), col.copy(), x, np.ones(6)) < 0
+
+
+@pytest.mark.parametrize("p_near", [0.0, 0.9])
+@pytest.mark.parametrize("warps", [None, 32, 100_000])
+def test_levelset_grids(orc, solver, p_near, warps):
+    """The level-set solve on one CTA (its barrier the CTA barrier) and on one CTA per SM (the grid
+    barrier through L2), and as the analysis' cost model picks, on a wide DAG (every column far:
+    few wide levels) and a narrow one (near columns: many narrow levels), one and three RHS.  The
+    all-far matrix has tiny solution components, so the elementwise bound is the larger of 1e-10
+    and ten times the reordering floor (the serial solve against itself summed in reverse) on the
+    same inputs; every grid must also give the same x."""
+    m = gen.random_upper(100_000, 5.0, p_near, 64, 13)
+    solver.analyse(m.row_ptr, m.col, m.val)
+    rpu = m.row_ptr.astype(np.uint64)
+    for rhs in (1, 3):
+        b = gen.uniform(60 + rhs, m.n * rhs)
+        ref = orc.base_gauss_upper(rpu, m.col, m.val, b, rhs)
+        floor = elem_err(orc.base_gauss_upper_rev(rpu, m.col, m.val, b, rhs), ref)
+        x = solver.solve(b, rhs=rhs, schedule="levelset", resident_warps=warps)
+        assert elem_err(x, ref) <= max(ELEM_TOL, 10 * floor), (rhs, warps, floor)
+        assert orc.rel_residual(rpu, m.col, m.val, x, b, rhs) <= RES_TOL
+        assert np.array_equal(x, solver.solve(b, rhs=rhs, schedule="levelset", resident_warps=32))

@@ -93,3 +93,13 @@ def test_nd40_full(orc, nd40, solver, rhs):
         else:
             assert err <= (bound if prec == "fp64" else max(1e-8, FLOOR_FACTOR * floor)), (name, report)
     print("nd40 rhs=%d" % rhs, report)
+
+
+def test_nd40_gpu_factor_matches(nd40):
+    """The full workload's factor from the GPU multifrontal Cholesky (sptrsv_factor_multifrontal)
+    against the host generator's: same pattern and partition, values to 1e-12 of the largest."""
+    f = gen.laplace3d_nd_cholesky_gpu(40)
+    assert np.array_equal(f.row_ptr, nd40.row_ptr) and np.array_equal(f.col, nd40.col)
+    assert np.array_equal(f.snodes, nd40.snodes)
+    assert np.max(np.abs(f.val - nd40.val)) <= 1e-12 * np.max(np.abs(nd40.val))
+
