@@ -39,6 +39,9 @@ Other workloads (their own JSON line, same keys where they apply):
                          sync-free, serial CPU.
   --workload dropin      the reference-signature base_gauss_upper on the 64 x 64 and 256 x 256
                          grid Laplacian factors and the 2M-row system, against the serial CPU solve.
+  --workload factor      the step upstream of the supernodal solve: the GPU multifrontal Cholesky
+                         of the 40^3 nested-dissection 3D Laplacian (sptrsv_factor_multifrontal),
+                         beside the host generator's numpy/scipy factor of the same fronts.
 """
 import argparse
 import csv
@@ -73,10 +76,13 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=2_000_000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="irregular2m", choices=["irregular2m", "batch", "supernodal", "dropin"],
+    ap.add_argument("--workload", default="irregular2m",
+                    choices=["irregular2m", "batch", "supernodal", "dropin", "factor"],
                     help="irregular2m: the 2M-row single solve (default); batch: the 512-system uneven mix; "
                          "supernodal: the 40^3 nested-dissection factor at 1/8/32/128 right-hand sides; "
-                         "dropin: the reference-signature base_gauss_upper on three systems")
+                         "dropin: the reference-signature base_gauss_upper on three systems; "
+                         "factor: the GPU multifrontal Cholesky that produces the supernodal factor")
+    ap.add_argument("--grid", type=int, default=40, help="factor: side of the 3D Laplacian grid")
     ap.add_argument("--count", type=int, default=512, help="batch: number of systems")
     ap.add_argument("--nmax", type=int, default=200_000, help="batch: largest n")
     ap.add_argument("--batch-steps", type=int, default=10,
@@ -1017,6 +1023,71 @@ def run_dropin(args, dist):
                       "rows": rows}), flush=True)
 
 
+def run_factor(args, dist):
+    """The multifrontal Cholesky A = U^T U of the 7-point 3D Laplacian on a grid^3 grid under
+    nested dissection (8^3 leaves, supernodes <= 400 rows) through sptrsv_factor_multifrontal:
+    wall time of the call (host symbolic step + GPU numeric step, U left on the device; best of
+    `steps` after `warmup` calls), the two steps apart, the copy of U to host memory timed apart
+    (sptrsv_factor_copy), and the factor's FLOPs (sum over columns of L of c_j^2, c_j the
+    column's entries) over the numeric step against the measured FP64 pipe.  Beside it the host
+    generator's factor of the same matrix and fronts (numpy/scipy dense fronts, LAPACK on the
+    host's OpenBLAS) timed once, and the largest difference between the two factors."""
+    import ctypes
+    import sptrsv_gb300 as sp
+    from sptrsv_gb300 import gen
+    if dist.rank != 0:
+        return
+    L = sp._lib.lib()
+    g = args.grid
+    rp, col, val, fs, fp, _ = gen.laplace3d_nd_matrix(g)
+    n = len(rp) - 1
+    times = []
+    for k in range(max(3, args.warmup) + args.steps):
+        h = ctypes.c_void_p()
+        t0 = time.perf_counter()
+        rc = L.sptrsv_factor_multifrontal(dist.local, n, rp, col, val, len(fs) - 1, fs, fp, 400, ctypes.byref(h))
+        wall = time.perf_counter() - t0
+        if rc:
+            raise SystemExit("sptrsv_factor_multifrontal: " + sp.status_string(rc))
+        sym, num = ctypes.c_double(), ctypes.c_double()
+        L.sptrsv_factor_times(h, ctypes.byref(sym), ctypes.byref(num))
+        nn, nnz, nsn = ctypes.c_int(), ctypes.c_int64(), ctypes.c_int()
+        L.sptrsv_factor_info(h, ctypes.byref(nn), ctypes.byref(nnz), ctypes.byref(nsn))
+        urp = np.empty(n + 1, dtype=np.int64)
+        ucol = np.empty(nnz.value, dtype=np.int32)
+        uval = np.empty(nnz.value, dtype=np.float64)
+        t0 = time.perf_counter()
+        L.sptrsv_factor_copy(h, urp, ucol, uval, np.empty(nsn.value + 1, dtype=np.int32))
+        copy = time.perf_counter() - t0
+        if k >= max(3, args.warmup):
+            times.append((wall, sym.value, num.value, copy))
+        L.sptrsv_factor_free(h)
+    wall, sym, num, copy = min(times)
+    c = np.diff(urp).astype(np.float64)
+    flops = float((c * c).sum())
+    pipe = fp64_pipe(dist.local)
+    rec = {"workload": f"factor: 7-point 3D Laplacian, {g}^3 grid, nested dissection (8^3 leaves), fronts "
+                       f"{len(fs) - 1}, supernodes <= 400 rows",
+           "metric": "factor wall seconds (host symbolic + GPU numeric, U on the device)", "unit": "s",
+           "higher_is_better": False,
+           "n": n, "nnz_A": int(rp[-1]), "nnz_U": int(nnz.value), "supernodes": int(nsn.value),
+           "steps": len(times), "value": wall, "symbolic_s": sym, "numeric_s": num, "copy_to_host_s": copy,
+           "all_wall_s": [t[0] for t in times],
+           "flops": flops, "numeric_gflop_per_s": flops / num / 1e9,
+           "frac_of_measured_fp64": flops / num / 1e9 / (2.0 * pipe["gfma_per_s"]),
+           "measured_fp64_gfma_per_s": pipe["gfma_per_s"]}
+    if not args.no_cpu_baseline:
+        t0 = time.perf_counter()
+        hm = gen.laplace3d_nd_cholesky(g)
+        rec["cpu_baseline"] = {"value": time.perf_counter() - t0, "unit": "s", "kind": "port",
+                               "cores": int(os.environ.get("OPENBLAS_NUM_THREADS", os.cpu_count())),
+                               "sample": f"gen.laplace3d_nd_cholesky({g}): the same fronts as dense numpy/scipy "
+                                         "blocks (LAPACK/BLAS on numpy's OpenBLAS), one run"}
+        rec["max_abs_diff_vs_host"] = float(np.max(np.abs(hm.val - uval)))
+        rec["max_abs_U"] = float(np.max(np.abs(uval)))
+    print(json.dumps(rec), flush=True)
+
+
 def apply_options(args):
     """Process-wide choices the command line makes before anything is built."""
     global PLAIN_SCHEDULE
@@ -1040,6 +1111,8 @@ def main():
             run_supernodal(args, dist)
         elif args.workload == "dropin":
             run_dropin(args, dist)
+        elif args.workload == "factor":
+            run_factor(args, dist)
         else:
             run_ours(args, dist)
     finally:

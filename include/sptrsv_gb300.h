@@ -218,8 +218,9 @@ SPTRSV_API int sptrsv_set_panels_mode(int mode);
  * rows front_start[t] .. front_start[t+1]-1 (the ranges tile 0 .. n-1 in order) and hands its
  * update matrix to front_parent[t] > t (-1 for a root).  The host finds every front's row set;
  * the GPU assembles each front (A's entries, its children's update matrices), factors its pivot
- * columns and forms its update matrix in FP64 (blocked in 64-column panels).  On success *factor
- * holds U in the solver's CSR layout (diagonal first, columns ascending) and the supernode
+ * columns and forms its update matrix in FP64 (blocked in 64-column panels), every front of one
+ * tree height in the same launches.  On success *factor holds U on the device in the solver's CSR
+ * layout (diagonal first, columns ascending), its row pointer on the host, and the supernode
  * partition: each front's pivots in pieces of at most max_width rows, each piece a dense triangle
  * plus one shared set of columns, as sptrsv_set_supernodes takes it.  SPTRSV_ERR_ZERO_PIVOT when a
  * pivot is not positive (A not positive definite); SPTRSV_ERR_INVALID_ARG for a tree whose
@@ -230,8 +231,15 @@ SPTRSV_API int sptrsv_factor_multifrontal(int device, int n, const int64_t* a_ro
 /* Sizes of a factor: n, entries of U, supernodes. */
 SPTRSV_API int sptrsv_factor_info(void* factor, int* n, int64_t* nnz, int* num_supernodes);
 /* Copies U (row_ptr[n+1], col[nnz], val[nnz]) and the partition (supernodes[num_supernodes+1]);
- * any pointer may be NULL. */
+ * any pointer may be NULL.  U lives on the device: col and val are copied from there. */
 SPTRSV_API int sptrsv_factor_copy(void* factor, int64_t* row_ptr, int* col, double* val, int* supernodes);
+/* U where the factor keeps it on its device: int32 row pointer, columns, values, valid until
+ * sptrsv_factor_free -- what sptrsv_analyse_device takes, so the solve can follow the factor
+ * without a trip through host memory.  SPTRSV_ERR_TOO_LARGE when U has 2^31 entries or more. */
+SPTRSV_API int sptrsv_factor_device(void* factor, const int** d_row_ptr, const int** d_col, const double** d_val);
+/* Host wall time of the factor's two steps in seconds: the symbolic step on the host and the
+ * numeric step on the GPU (uploads, every front's kernels, the copy of U back); either may be NULL. */
+SPTRSV_API int sptrsv_factor_times(void* factor, double* symbolic_s, double* numeric_s);
 SPTRSV_API void sptrsv_factor_free(void* factor);
 /* Largest n accepted by sptrsv_solve_noalloc (its reciprocal diagonal lives in a fixed array). */
 #define SPTRSV_NOALLOC_MAX_ROWS (1 << 20)

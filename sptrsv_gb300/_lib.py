@@ -95,6 +95,8 @@ C_API = {
     "sptrsv_factor_multifrontal": ([c_int, c_int, i64, i32, f64, c_int, i32, i32, c_int, ctypes.POINTER(c_vp)], c_int),
     "sptrsv_factor_info": ([c_vp, _c_int_p, ctypes.POINTER(c_i64), _c_int_p], c_int),
     "sptrsv_factor_copy": ([c_vp, i64, i32, f64, i32], c_int),
+    "sptrsv_factor_device": ([c_vp, ctypes.POINTER(c_vp), ctypes.POINTER(c_vp), ctypes.POINTER(c_vp)], c_int),
+    "sptrsv_factor_times": ([c_vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)], c_int),
     "sptrsv_factor_free": ([c_vp], None),
     "sptrsv_get_level_buckets": ([c_vp, i32, i32], c_int),
     "sptrsv_get_level_tasks": ([c_vp, c_int, i32], c_int),

@@ -6,34 +6,79 @@
 // Symbolic step (host): front t pivots rows f0 .. f1-1 and hands its update matrix to its parent.
 // Its row set is S_t = [f0, f1) followed, sorted, by every row >= f1 adjacent in A to one of its
 // pivots or in one of its children's update sets.  U's pattern follows: row f0 + k holds S_t[k:].
-// Numeric step (GPU, fronts in the given postorder): the dense front F_t (|S_t| x |S_t|, column
-// major, lower triangle) gets A's entries and its children's update matrices (extend-add), then a
-// blocked right-looking Cholesky over its first w = f1 - f0 columns in 64-column panels: the
-// panel's diagonal tile factored by one CTA, the rows below it solved against that tile, the
-// trailing lower triangle updated by a tiled FP64 rank-64 product.  Running the trailing updates
-// over the whole front leaves the Schur complement -- the update matrix for the parent -- in
-// F_t[w:, w:].  Column f0 + k of L = U^T is F_t[k:, k], copied into U's row f0 + k.
+// Numeric step (GPU, by tree level): a front's height is 0 for a leaf and one more than its
+// highest child otherwise; the fronts of one height are independent, so each step below is one
+// launch over every front of the level (a work list of fronts and a prefix of their CTA counts).
+// The dense front F_t (|S_t| x |S_t|, column major, lower triangle) gets A's entries and its
+// children's update matrices (extend-add, the children in order), then a blocked right-looking
+// Cholesky over its first w = f1 - f0 columns in 64-column panels: the panel's diagonal tile
+// factored by one CTA, the rows below it solved against that tile, the trailing lower triangle
+// updated by a tiled FP64 rank-64 product.  Running the trailing updates over the whole front
+// leaves the Schur complement -- the update matrix for the parent -- in F_t[w:, w:].  Column
+// f0 + k of L = U^T is F_t[k:, k], copied into U's row f0 + k.  The fronts of a level share one
+// region of a single arena, reused once the level's parents have taken their update matrices;
+// every entry sees the same operations in the same order as a front-by-front run.
 #include <algorithm>
+#include <chrono>
 #include <cstdint>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 #include "common.cuh"
 #include "sptrsv_gb300.h"
 
 namespace sptrsv {
 
-constexpr int kFb = 64;  // panel width and update tile
+constexpr int kFb = 64;       // panel width and update tile
+constexpr int kTrsmRows = 16;  // rows per CTA of the panel solve
 
-// F[idx[q]] = v[q]: A's entries of one front.
-__global__ void k_fr_scatter(double* __restrict__ F, const int64_t* __restrict__ idx, const double* __restrict__ v,
-                             int count) {
-    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < count; q += gridDim.x * blockDim.x) F[idx[q]] = v[q];
+// Where the fronts live: front t is F = arena + foff[t], fm[t] x fm[t], pivots fstart[t] ..
+// fstart[t+1]-1.
+struct FrontTab {
+    const int* fstart;
+    const int* fm;
+    const int64_t* foff;
+};
+
+// The work item of CTA b in a launch over nlist fronts with CTA prefix counts: the largest f with
+// prefix[f] <= b (every listed front has at least one CTA).
+__device__ __forceinline__ int fr_item(const int* __restrict__ prefix, int nlist, int b) {
+    int lo = 0, hi = nlist - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (prefix[mid] <= b) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
 }
 
-// F[map[r] + map[s] m] += C[(wc + r) + (wc + s) mc] for s <= r < nu: a child's update matrix
-// (the lower triangle of its front past its pivots) added into the parent front.
-__global__ void k_fr_extend_add(double* __restrict__ F, int m, const double* __restrict__ C, int mc, int wc,
-                                const int* __restrict__ map, int nu) {
+// (i, j), j <= i, of the e-th entry of a lower triangle walked row by row.
+__device__ __forceinline__ void fr_tri(int e, int& i, int& j) {
+    i = (int)((sqrtf(8.0f * e + 1.0f) - 1.0f) * 0.5f);
+    while ((i + 1) * (i + 2) / 2 <= e) ++i;
+    while (i * (i + 1) / 2 > e) --i;
+    j = e - i * (i + 1) / 2;
+}
+
+// arena[idx[q]] = v[q]: A's entries of a level's fronts (idx already holds each front's offset).
+__global__ void k_fr_scatter(double* __restrict__ arena, const int64_t* __restrict__ idx,
+                             const double* __restrict__ v, long long count) {
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < count;
+         q += (long long)gridDim.x * blockDim.x)
+        arena[idx[q]] = v[q];
+}
+
+// F_p[map[r] + map[s] m] += C[(wc + r) + (wc + s) mc] for s <= r < nu: child c = child[blockIdx.y]
+// adds its update matrix (the lower triangle of its front past its pivots) into its parent p.
+// One launch takes at most one child of each parent, so no two CTAs add into the same entry.
+__global__ void k_fr_extend_add(double* __restrict__ arena, FrontTab ft, const int* __restrict__ child,
+                                const int* __restrict__ parent, const int* __restrict__ maps,
+                                const int64_t* __restrict__ map_start) {
+    const int c = child[blockIdx.y], p = parent[c];
+    const int wc = ft.fstart[c + 1] - ft.fstart[c], mc = ft.fm[c], nu = mc - wc, m = ft.fm[p];
+    const double* C = arena + ft.foff[c];
+    double* F = arena + ft.foff[p];
+    const int* map = maps + map_start[c];
     const long long total = (long long)nu * nu;
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
          e += (long long)gridDim.x * blockDim.x) {
@@ -43,29 +88,46 @@ __global__ void k_fr_extend_add(double* __restrict__ F, int m, const double* __r
     }
 }
 
-// Cholesky of the kb x kb diagonal tile at (k0, k0), lower, in place (one CTA of 256 threads).
-// A pivot that is not positive (or not finite) sets *bad and the factor is not used.
-__global__ void __launch_bounds__(256) k_fr_potrf(double* __restrict__ F, int m, int k0, int kb, int* bad) {
+// Cholesky of the kb x kb diagonal tile at (k0, k0) of front list[blockIdx.x], lower, in place
+// (one CTA of 256 threads per front).  A pivot that is not positive (or not finite) sets *bad and
+// the factor is not used.  The chain that orders the columns is one reciprocal square root per
+// column (thread 0; the column is scaled by it and its diagonal is d * rsqrt(d)); the rank-1
+// update of the rest walks the entries of its lower triangle only, from a table of (row, column)
+// pairs, so no lane idles on the upper half.
+__global__ void __launch_bounds__(256) k_fr_potrf(double* __restrict__ arena, FrontTab ft,
+                                                  const int* __restrict__ list, int k0, int* bad) {
     __shared__ double T[kFb][kFb + 1];
+    __shared__ int pairs[kFb * (kFb + 1) / 2];  // e = i (i + 1) / 2 + c  ->  i << 8 | c, c <= i
+    __shared__ double rs;
+    const int t = list[blockIdx.x];
+    double* F = arena + ft.foff[t];
+    const int m = ft.fm[t], kb = min(kFb, ft.fstart[t + 1] - ft.fstart[t] - k0);
     for (int e = threadIdx.x; e < kb * kb; e += blockDim.x) {
         const int r = e % kb, c = e / kb;
         T[r][c] = r >= c ? F[(size_t)(k0 + r) + (size_t)(k0 + c) * m] : 0.0;
+    }
+    for (int e = threadIdx.x; e < kFb * (kFb + 1) / 2; e += blockDim.x) {
+        int i, c;
+        fr_tri(e, i, c);
+        pairs[e] = i << 8 | c;
     }
     __syncthreads();
     for (int j = 0; j < kb; ++j) {
         if (threadIdx.x == 0) {
             const double d = T[j][j];
             if (!(d > 0.0) || !isfinite(d)) atomicExch(bad, 1);
-            T[j][j] = sqrt(d > 0.0 ? d : 1.0);
+            const double r = rsqrt(d > 0.0 ? d : 1.0);
+            T[j][j] = (d > 0.0 ? d : 1.0) * r;
+            rs = r;
         }
         __syncthreads();
-        const double inv = 1.0 / T[j][j];
-        for (int i = j + 1 + threadIdx.x; i < kb; i += blockDim.x) T[i][j] *= inv;
+        const double r = rs;
+        for (int i = j + 1 + threadIdx.x; i < kb; i += blockDim.x) T[i][j] *= r;
         __syncthreads();
-        const int rest = kb - j - 1;
-        for (int e = threadIdx.x; e < rest * rest; e += blockDim.x) {
-            const int i = j + 1 + e % rest, c = j + 1 + e / rest;
-            if (i >= c) T[i][c] = fma(-T[i][j], T[c][j], T[i][c]);
+        const int rest = kb - j - 1, np = rest * (rest + 1) / 2;
+        for (int e = threadIdx.x; e < np; e += blockDim.x) {
+            const int pr = pairs[e], i = j + 1 + (pr >> 8), c = j + 1 + (pr & 255);
+            T[i][c] = fma(-T[i][j], T[c][j], T[i][c]);
         }
         __syncthreads();
     }
@@ -75,40 +137,73 @@ __global__ void __launch_bounds__(256) k_fr_potrf(double* __restrict__ F, int m,
     }
 }
 
-// Rows r0 .. m-1 of the panel (columns k0 .. k0+kb-1): X L^T = B with L the factored tile, one
-// thread per row, four partial sums per element so that the FP64 chain is a quarter as long.
-__global__ void __launch_bounds__(256) k_fr_trsm(double* __restrict__ F, int m, int k0, int kb, int r0) {
+// Rows r0 .. m-1 of the panel (columns k0 .. k0+kb-1, r0 = k0 + kb) of each listed front:
+// X L^T = B with L the factored tile.  kTrsmRows rows per CTA, eight lanes per row (one warp
+// holds four rows).  The columns go in blocks of eight: lane q first forms its column's sum over
+// the blocks already solved (the row's solved values and L's rows come from shared memory, four
+// partial sums), then the block's 8 x 8 triangle is solved across the eight lanes by shuffles.
+// A row's 2,016 FMAs are spread over eight lanes, and the dependent chain is eight short blocks.
+__global__ void __launch_bounds__(kTrsmRows * 8) k_fr_trsm(double* __restrict__ arena, FrontTab ft,
+                                                           const int* __restrict__ list,
+                                                           const int* __restrict__ prefix, int nlist, int k0) {
     __shared__ double L[kFb][kFb + 1];
-    for (int e = threadIdx.x; e < kb * kb; e += blockDim.x) {
-        const int r = e % kb, c = e / kb;
-        L[r][c] = r >= c ? F[(size_t)(k0 + r) + (size_t)(k0 + c) * m] : 0.0;
+    __shared__ double X[kTrsmRows][kFb + 1];
+    __shared__ double dinv[kFb];
+    const int f = fr_item(prefix, nlist, blockIdx.x), t = list[f];
+    double* F = arena + ft.foff[t];
+    const int m = ft.fm[t], kb = min(kFb, ft.fstart[t + 1] - ft.fstart[t] - k0);
+    const int row0 = k0 + kb + (blockIdx.x - prefix[f]) * kTrsmRows;
+    for (int e = threadIdx.x; e < kFb * kFb; e += blockDim.x) {
+        const int r = e % kFb, c = e / kFb;
+        L[r][c] = r < kb && c <= r ? F[(size_t)(k0 + r) + (size_t)(k0 + c) * m] : 0.0;
+    }
+    for (int e = threadIdx.x; e < kTrsmRows * kb; e += blockDim.x) {
+        const int rr = e % kTrsmRows, c = e / kTrsmRows;
+        X[rr][c] = row0 + rr < m ? F[(size_t)(row0 + rr) + (size_t)(k0 + c) * m] : 0.0;
     }
     __syncthreads();
-    const int r = r0 + blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= m) return;
-    double x[kFb];
-    for (int j = 0; j < kb; ++j) {
-        double s0 = F[(size_t)r + (size_t)(k0 + j) * m], s1 = 0.0, s2 = 0.0, s3 = 0.0;
-        int c = 0;
-        for (; c + 3 < j; c += 4) {
-            s0 = fma(-x[c], L[j][c], s0);
-            s1 = fma(-x[c + 1], L[j][c + 1], s1);
-            s2 = fma(-x[c + 2], L[j][c + 2], s2);
-            s3 = fma(-x[c + 3], L[j][c + 3], s3);
+    if (threadIdx.x < kFb) dinv[threadIdx.x] = threadIdx.x < kb ? 1.0 / L[threadIdx.x][threadIdx.x] : 0.0;
+    __syncthreads();
+    const int g = threadIdx.x >> 3, q = threadIdx.x & 7;
+    const unsigned full = 0xffffffffu;
+    for (int j0 = 0; j0 < kb; j0 += 8) {
+        const int c = j0 + q;
+        double s0 = c < kb ? X[g][c] : 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+        for (int p = 0; p < j0; p += 4) {
+            s0 = fma(-X[g][p], L[c][p], s0);
+            s1 = fma(-X[g][p + 1], L[c][p + 1], s1);
+            s2 = fma(-X[g][p + 2], L[c][p + 2], s2);
+            s3 = fma(-X[g][p + 3], L[c][p + 3], s3);
         }
-        for (; c < j; ++c) s0 = fma(-x[c], L[j][c], s0);
-        x[j] = ((s0 + s1) + (s2 + s3)) / L[j][j];
+        double s = (s0 + s1) + (s2 + s3), x = 0.0;
+#pragma unroll
+        for (int p = 0; p < 8; ++p) {
+            const double xp = __shfl_sync(full, s * dinv[j0 + p], p, 8);
+            if (q == p) x = xp;
+            if (q > p) s = fma(-xp, L[c][j0 + p], s);
+        }
+        if (c < kb) X[g][c] = x;
+        __syncwarp();
     }
-    for (int j = 0; j < kb; ++j) F[(size_t)r + (size_t)(k0 + j) * m] = x[j];
+    __syncthreads();
+    for (int e = threadIdx.x; e < kTrsmRows * kb; e += blockDim.x) {
+        const int rr = e % kTrsmRows, c = e / kTrsmRows;
+        if (row0 + rr < m) F[(size_t)(row0 + rr) + (size_t)(k0 + c) * m] = X[rr][c];
+    }
 }
 
-// The trailing lower triangle F[r0:, r0:] -= P P^T with P = F[r0:, k0:k0+kb]: one 64 x 64 output
-// tile per CTA (tiles above the diagonal skip), 256 threads of 4 x 4 outputs each.
-__global__ void __launch_bounds__(256) k_fr_syrk(double* __restrict__ F, int m, int k0, int kb, int r0) {
-    const int ti = blockIdx.x, tj = blockIdx.y;
-    if (tj > ti) return;
+// The trailing lower triangle F[r0:, r0:] -= P P^T with P = F[r0:, k0:k0+kb] of each listed
+// front: one 64 x 64 output tile per CTA (the CTA's item is the tile's index in the lower
+// triangle of tiles), 256 threads of 4 x 4 outputs each.
+__global__ void __launch_bounds__(256) k_fr_syrk(double* __restrict__ arena, FrontTab ft, const int* __restrict__ list,
+                                                 const int* __restrict__ prefix, int nlist, int k0) {
+    const int f = fr_item(prefix, nlist, blockIdx.x), t = list[f];
+    double* F = arena + ft.foff[t];
+    const int m = ft.fm[t], kb = min(kFb, ft.fstart[t + 1] - ft.fstart[t] - k0), r0 = k0 + kb;
+    int ti, tj;
+    fr_tri(blockIdx.x - prefix[f], ti, tj);
     extern __shared__ double fr_sm[];
-    double* A = fr_sm;                  // [kFb][kFb + 1]: rows of tile ti
+    double* A = fr_sm;                    // [kFb][kFb + 1]: rows of tile ti
     double* B = fr_sm + kFb * (kFb + 1);  // [kFb][kFb + 1]: rows of tile tj
     const int rA = r0 + ti * kFb, rB = r0 + tj * kFb;
     for (int e = threadIdx.x; e < kFb * kb; e += blockDim.x) {
@@ -143,20 +238,43 @@ __global__ void __launch_bounds__(256) k_fr_syrk(double* __restrict__ F, int m, 
     }
 }
 
-// U's values of one front: row f0 + k (k < w) = F[k:, k].
-__global__ void k_fr_copy_rows(const double* __restrict__ F, int m, int w, const int64_t* __restrict__ rp, int f0,
-                               double* __restrict__ uval) {
-    const int k = blockIdx.x;
-    if (k >= w) return;
-    const int64_t base = rp[f0 + k];
-    for (int r = k + threadIdx.x; r < m; r += blockDim.x) uval[base + (r - k)] = F[(size_t)r + (size_t)k * m];
+// U's rows of the listed fronts: one CTA per pivot, row f0 + k (k < w) holds columns S_t[k:]
+// (rows = the fronts' row sets, front t's at rows + soff[t]) with values F[k:, k].
+__global__ void k_fr_copy_rows(const double* __restrict__ arena, FrontTab ft, const int* __restrict__ list,
+                               const int* __restrict__ prefix, int nlist, const int* __restrict__ rows,
+                               const int64_t* __restrict__ soff, const int64_t* __restrict__ rp,
+                               int* __restrict__ ucol, double* __restrict__ uval) {
+    const int f = fr_item(prefix, nlist, blockIdx.x), t = list[f], k = blockIdx.x - prefix[f];
+    const double* F = arena + ft.foff[t];
+    const int* S = rows + soff[t];
+    const int m = ft.fm[t];
+    const int64_t base = rp[ft.fstart[t] + k];
+    for (int r = k + threadIdx.x; r < m; r += blockDim.x) {
+        ucol[base + (r - k)] = S[r];
+        uval[base + (r - k)] = F[(size_t)r + (size_t)k * m];
+    }
 }
 
+// U lives on the device (the factor owns it); the host copies are made when first asked for.
 struct Factor {
-    int n = 0;
+    int n = 0, device = 0;
     std::vector<int64_t> rp;
-    std::vector<int> col, snodes;
-    std::vector<double> val;
+    std::vector<int> snodes;
+    int* d_rp32 = nullptr;  // int32 row pointer, when nnz < 2^31 (what sptrsv_analyse_device takes)
+    int* d_col = nullptr;
+    double* d_val = nullptr;
+    double symbolic_s = 0.0, numeric_s = 0.0;  // host wall time of the two steps
+    ~Factor() {
+        if (d_rp32 || d_col || d_val) {
+            int cur = 0;
+            cudaGetDevice(&cur);
+            cudaSetDevice(device);
+            cudaFree(d_rp32);
+            cudaFree(d_col);
+            cudaFree(d_val);
+            cudaSetDevice(cur);
+        }
+    }
 };
 
 }  // namespace sptrsv
@@ -183,17 +301,15 @@ extern "C" int sptrsv_factor_multifrontal(int device, int n, const int64_t* a_rp
     for (int64_t e = 0; e < annz; ++e)
         if (a_col[e] < 0 || a_col[e] >= n) return SPTRSV_ERR_COL_RANGE;
     // ---- symbolic: row sets, index maps, U's pattern, supernodes
-    std::vector<int> front_of(n);
-    for (int t = 0; t < nf; ++t)
-        for (int i = front_start[t]; i < front_start[t + 1]; ++i) front_of[i] = t;
+    const auto t_begin = std::chrono::steady_clock::now();
     std::vector<std::vector<int>> children(nf), S(nf);
     for (int t = 0; t < nf; ++t)
         if (front_parent[t] >= 0) children[front_parent[t]].push_back(t);
-    std::vector<int64_t> a_idx_off(nf + 1, 0), map_off(nf + 1, 0);
+    std::vector<int64_t> a_idx_off(nf + 1, 0), map_start(nf, 0);
     std::vector<int64_t> a_idx;
     std::vector<double> a_v;
     std::vector<int> maps;
-    std::vector<int> mark(n, -1);
+    std::vector<int> mark(n, -1), posmap(n, 0);  // posmap: a row's place in the current front
     for (int t = 0; t < nf; ++t) {
         const int f0 = front_start[t], f1 = front_start[t + 1];
         std::vector<int> below;
@@ -222,10 +338,9 @@ extern "C" int sptrsv_factor_multifrontal(int device, int n, const int64_t* a_rp
         for (int p = f0; p < f1; ++p) St.push_back(p);
         St.insert(St.end(), below.begin(), below.end());
         const int m = (int)St.size();
-        auto pos = [&](int q) -> int {
-            if (q < f1) return q - f0;
-            return (f1 - f0) + (int)(std::lower_bound(below.begin(), below.end(), q) - below.begin());
-        };
+        if (front_parent[t] < 0 && m != f1 - f0) return SPTRSV_ERR_INVALID_ARG;  // an update nobody takes
+        for (size_t k = 0; k < below.size(); ++k) posmap[below[k]] = (f1 - f0) + (int)k;
+        auto pos = [&](int q) -> int { return q < f1 ? q - f0 : posmap[q]; };
         // A's lower-triangle entries of the pivot columns
         for (int p = f0; p < f1; ++p)
             for (int64_t e = a_rp[p]; e < a_rp[p + 1]; ++e) {
@@ -238,9 +353,9 @@ extern "C" int sptrsv_factor_multifrontal(int device, int n, const int64_t* a_rp
         // the children's update rows within this front
         for (int c : children[t]) {
             const int wc = front_start[c + 1] - front_start[c];
+            map_start[c] = (int64_t)maps.size();
             for (size_t k = wc; k < S[c].size(); ++k) maps.push_back(pos(S[c][k]));
         }
-        map_off[t + 1] = (int64_t)maps.size();
     }
     Factor* fct = new Factor;
     fct->n = n;
@@ -250,28 +365,147 @@ extern "C" int sptrsv_factor_multifrontal(int device, int n, const int64_t* a_rp
         for (int k = 0; k < w; ++k) fct->rp[f0 + k + 1] = m - k;
     }
     for (int i = 0; i < n; ++i) fct->rp[i + 1] += fct->rp[i];
-    fct->col.resize(fct->rp[n]);
-    for (int t = 0; t < nf; ++t) {
-        const int f0 = front_start[t], w = front_start[t + 1] - f0;
-        for (int k = 0; k < w; ++k) std::copy(S[t].begin() + k, S[t].end(), fct->col.begin() + fct->rp[f0 + k]);
-    }
+    fct->device = device;
     fct->snodes.push_back(0);
     for (int t = 0; t < nf; ++t) {
         const int f0 = front_start[t], f1 = front_start[t + 1], w = f1 - f0;
         const int pieces = (w + max_width - 1) / max_width, step = (w + pieces - 1) / pieces;
         for (int a = f0; a < f1; a += step) fct->snodes.push_back(std::min(f1, a + step));
     }
-    fct->val.resize(fct->rp[n]);
-    // ---- numeric on the GPU
+    // ---- schedule: levels by height, one arena region per level, the launches' work lists
+    std::vector<int> height(nf, 0), fm(nf);
+    for (int t = 0; t < nf; ++t) {
+        fm[t] = (int)S[t].size();
+        if (front_parent[t] >= 0) height[front_parent[t]] = std::max(height[front_parent[t]], height[t] + 1);
+    }
+    const int H = *std::max_element(height.begin(), height.end()) + 1;
+    std::vector<std::vector<int>> level(H);
+    for (int t = 0; t < nf; ++t) level[height[t]].push_back(t);
+    // a level's region lives from its own step to its parents' extend-add; first fit over the
+    // regions still live when the level starts
+    struct Region {
+        int64_t off, size;
+        int last;
+    };
+    std::vector<Region> live;  // by offset
+    std::vector<int64_t> foff(nf), lvl_off(H), lvl_size(H);
+    int64_t arena_size = 0;
+    for (int h = 0; h < H; ++h) {
+        int64_t size = 0;
+        int last = h;
+        for (int t : level[h]) {
+            foff[t] = size;
+            size += ((int64_t)fm[t] * fm[t] + 31) / 32 * 32;  // 256-byte aligned fronts
+            if (front_parent[t] >= 0) last = std::max(last, height[front_parent[t]]);
+        }
+        live.erase(std::remove_if(live.begin(), live.end(), [&](const Region& r) { return r.last < h; }), live.end());
+        int64_t at = 0;
+        size_t k = 0;
+        for (; k < live.size() && live[k].off - at < size; ++k) at = live[k].off + live[k].size;
+        live.insert(live.begin() + k, Region{at, size, last});
+        lvl_off[h] = at;
+        lvl_size[h] = size;
+        arena_size = std::max(arena_size, at + size);
+        for (int t : level[h]) foff[t] += at;
+    }
+    // A's entries by level, each index already offset to its front
+    std::vector<int64_t> sc_idx, lvl_a(H + 1, 0);
+    std::vector<double> sc_v;
+    sc_idx.reserve(a_idx.size());
+    sc_v.reserve(a_v.size());
+    for (int h = 0; h < H; ++h) {
+        for (int t : level[h])
+            for (int64_t q = a_idx_off[t]; q < a_idx_off[t + 1]; ++q) {
+                sc_idx.push_back(foff[t] + a_idx[q]);
+                sc_v.push_back(a_v[q]);
+            }
+        lvl_a[h + 1] = (int64_t)sc_idx.size();
+    }
+    std::vector<int64_t>().swap(a_idx);
+    std::vector<double>().swap(a_v);
+    std::vector<int> rows;  // every front's row set, U's column indices
+    std::vector<int64_t> soff(nf);
+    for (int t = 0; t < nf; ++t) {
+        soff[t] = (int64_t)rows.size();
+        rows.insert(rows.end(), S[t].begin(), S[t].end());
+    }
+    enum { kExtend, kPotrf, kTrsm, kSyrk, kCopy };
+    struct Launch {
+        int kind, k0, nlist, total;  // total: CTAs (kExtend: CTAs per child)
+        int64_t list;                // offset of the list in sched; the CTA prefix (nlist + 1) follows it
+    };
+    std::vector<int> sched;
+    std::vector<std::vector<Launch>> launches(H);
+    auto add = [&](int h, int kind, int k0, const std::vector<int>& lst, const std::vector<int>& cnt, int total) {
+        if (lst.empty()) return;
+        Launch L{kind, k0, (int)lst.size(), total, (int64_t)sched.size()};
+        sched.insert(sched.end(), lst.begin(), lst.end());
+        if (!cnt.empty()) {
+            int acc = 0;
+            for (int c : cnt) {
+                sched.push_back(acc);
+                acc += c;
+            }
+            sched.push_back(acc);
+            L.total = acc;
+        }
+        launches[h].push_back(L);
+    };
+    for (int h = 0; h < H; ++h) {
+        // extend-add: the r-th children of the level's fronts in one launch, r = 0, 1, ...
+        for (size_t r = 0;; ++r) {
+            std::vector<int> kids;
+            long long most = 0;
+            bool any = false;
+            for (int t : level[h]) {
+                if (r >= children[t].size()) continue;
+                any = true;
+                const int c = children[t][r], nu = fm[c] - (front_start[c + 1] - front_start[c]);
+                if (nu <= 0) continue;
+                kids.push_back(c);
+                most = std::max(most, (long long)nu * nu);
+            }
+            if (!any) break;
+            const int gx = (int)std::min<long long>(1024, (most + 255) / 256);
+            for (size_t a = 0; a < kids.size(); a += 65535)
+                add(h, kExtend, 0, std::vector<int>(kids.begin() + a, kids.begin() + std::min(kids.size(), a + 65535)),
+                    {}, gx);
+        }
+        int panels = 0;
+        for (int t : level[h]) panels = std::max(panels, (front_start[t + 1] - front_start[t] + kFb - 1) / kFb);
+        for (int p = 0; p < panels; ++p) {
+            const int k0 = p * kFb;
+            std::vector<int> fac, upd, n_trsm, n_syrk;
+            for (int t : level[h]) {
+                const int w = front_start[t + 1] - front_start[t];
+                if (w <= k0) continue;
+                fac.push_back(t);
+                const int r0 = k0 + std::min(kFb, w - k0), rest = fm[t] - r0;
+                if (rest <= 0) continue;
+                upd.push_back(t);
+                n_trsm.push_back((rest + kTrsmRows - 1) / kTrsmRows);
+                const int tiles = (rest + kFb - 1) / kFb;
+                n_syrk.push_back(tiles * (tiles + 1) / 2);
+            }
+            add(h, kPotrf, k0, fac, {}, (int)fac.size());
+            add(h, kTrsm, k0, upd, n_trsm, 0);
+            add(h, kSyrk, k0, upd, n_syrk, 0);
+        }
+        std::vector<int> widths;
+        for (int t : level[h]) widths.push_back(front_start[t + 1] - front_start[t]);
+        add(h, kCopy, 0, level[h], widths, 0);
+    }
+    const auto t_symbolic = std::chrono::steady_clock::now();
+    fct->symbolic_s = std::chrono::duration<double>(t_symbolic - t_begin).count();
+    // ---- numeric on the GPU: one stream, one arena
     int rc = 0;
     cudaStream_t st = nullptr;
-    int64_t* d_aidx = nullptr;
-    double* d_av = nullptr;
-    int* d_maps = nullptr;
-    int64_t* d_rp = nullptr;
-    double* d_uval = nullptr;
+    int *d_sched = nullptr, *d_fstart = nullptr, *d_fm = nullptr, *d_parent = nullptr, *d_maps = nullptr;
+    int64_t *d_foff = nullptr, *d_mapstart = nullptr, *d_scidx = nullptr, *d_rp = nullptr, *d_soff = nullptr;
+    int* d_rows = nullptr;
+    double *d_scv = nullptr, *d_arena = nullptr;
+    const int64_t unnz = fct->rp[n];
     int* d_bad = nullptr;
-    std::vector<double*> F(nf, nullptr);
     auto fail = [&](cudaError_t e, const char* what) {
         if (!rc) rc = set_cuda_error(e, what);
     };
@@ -285,69 +519,77 @@ extern "C" int sptrsv_factor_multifrontal(int device, int n, const int64_t* a_rp
         if (!ck(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "stream")) break;
         if (!ck(cudaFuncSetAttribute(k_fr_syrk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)syrk_smem), "attr"))
             break;
-        if (!ck(cudaMallocAsync((void**)&d_aidx, sizeof(int64_t) * std::max<size_t>(1, a_idx.size()), st), "alloc")) break;
-        if (!ck(cudaMallocAsync((void**)&d_av, sizeof(double) * std::max<size_t>(1, a_v.size()), st), "alloc")) break;
-        if (!ck(cudaMallocAsync((void**)&d_maps, sizeof(int) * std::max<size_t>(1, maps.size()), st), "alloc")) break;
-        if (!ck(cudaMallocAsync((void**)&d_rp, sizeof(int64_t) * (n + 1), st), "alloc")) break;
-        if (!ck(cudaMallocAsync((void**)&d_uval, sizeof(double) * std::max<int64_t>(1, fct->rp[n]), st), "alloc")) break;
-        if (!ck(cudaMallocAsync((void**)&d_bad, sizeof(int), st), "alloc")) break;
-        if (!ck(cudaMemsetAsync(d_bad, 0, sizeof(int), st), "memset")) break;
-        if (!a_idx.empty() &&
-            (!ck(cudaMemcpyAsync(d_aidx, a_idx.data(), sizeof(int64_t) * a_idx.size(), cudaMemcpyHostToDevice, st), "h2d") ||
-             !ck(cudaMemcpyAsync(d_av, a_v.data(), sizeof(double) * a_v.size(), cudaMemcpyHostToDevice, st), "h2d")))
+        int sm_count = 0;
+        if (!ck(cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, device), "attr")) break;
+        auto up = [&](auto** d, const auto* h, size_t count) {
+            using E = std::remove_pointer_t<std::remove_pointer_t<decltype(d)>>;
+            if (!ck(cudaMallocAsync((void**)d, sizeof(E) * std::max<size_t>(1, count), st), "alloc")) return false;
+            return count == 0 || ck(cudaMemcpyAsync(*d, h, sizeof(E) * count, cudaMemcpyHostToDevice, st), "h2d");
+        };
+        if (!up(&d_sched, sched.data(), sched.size()) || !up(&d_fstart, front_start, (size_t)nf + 1) ||
+            !up(&d_fm, fm.data(), (size_t)nf) || !up(&d_parent, front_parent, (size_t)nf) ||
+            !up(&d_maps, maps.data(), maps.size()) || !up(&d_foff, foff.data(), (size_t)nf) ||
+            !up(&d_mapstart, map_start.data(), (size_t)nf) || !up(&d_scidx, sc_idx.data(), sc_idx.size()) ||
+            !up(&d_scv, sc_v.data(), sc_v.size()) || !up(&d_rp, fct->rp.data(), (size_t)n + 1) ||
+            !up(&d_rows, rows.data(), rows.size()) || !up(&d_soff, soff.data(), (size_t)nf))
             break;
-        if (!maps.empty() &&
-            !ck(cudaMemcpyAsync(d_maps, maps.data(), sizeof(int) * maps.size(), cudaMemcpyHostToDevice, st), "h2d"))
+        // U's arrays outlive the call (plain cudaMalloc: the factor frees them, on any stream)
+        if (!ck(cudaMalloc((void**)&fct->d_col, sizeof(int) * std::max<int64_t>(1, unnz)), "alloc U") ||
+            !ck(cudaMalloc((void**)&fct->d_val, sizeof(double) * std::max<int64_t>(1, unnz)), "alloc U"))
             break;
-        if (!ck(cudaMemcpyAsync(d_rp, fct->rp.data(), sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice, st), "h2d")) break;
-        for (int t = 0; t < nf && !rc; ++t) {
-            const int f0 = front_start[t], w = front_start[t + 1] - f0, m = (int)S[t].size();
-            if (!ck(cudaMallocAsync((void**)&F[t], sizeof(double) * (size_t)m * m, st), "front alloc")) break;
-            if (!ck(cudaMemsetAsync(F[t], 0, sizeof(double) * (size_t)m * m, st), "front memset")) break;
-            const int na = (int)(a_idx_off[t + 1] - a_idx_off[t]);
-            if (na > 0) k_fr_scatter<<<(na + 255) / 256, 256, 0, st>>>(F[t], d_aidx + a_idx_off[t], d_av + a_idx_off[t], na);
-            int64_t mo = map_off[t];
-            for (int c : children[t]) {
-                const int wc = front_start[c + 1] - front_start[c], mc = (int)S[c].size(), nu = mc - wc;
-                if (nu > 0) {
-                    const long long tot = (long long)nu * nu;
-                    const int g = (int)std::min<long long>(65535, (tot + 255) / 256);
-                    k_fr_extend_add<<<g, 256, 0, st>>>(F[t], m, F[c], mc, wc, d_maps + mo, nu);
+        if (unnz < ((int64_t)1 << 31)) {
+            std::vector<int> rp32(fct->rp.begin(), fct->rp.end());
+            if (!ck(cudaMalloc((void**)&fct->d_rp32, sizeof(int) * (n + 1)), "alloc U") ||
+                !ck(cudaMemcpyAsync(fct->d_rp32, rp32.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, st),
+                    "h2d"))
+                break;
+        }
+        if (!ck(cudaMallocAsync((void**)&d_arena, sizeof(double) * std::max<int64_t>(1, arena_size), st), "arena") ||
+            !ck(cudaMallocAsync((void**)&d_bad, sizeof(int), st), "alloc") ||
+            !ck(cudaMemsetAsync(d_bad, 0, sizeof(int), st), "memset"))
+            break;
+        const FrontTab ft{d_fstart, d_fm, d_foff};
+        for (int h = 0; h < H && !rc; ++h) {
+            if (!ck(cudaMemsetAsync(d_arena + lvl_off[h], 0, sizeof(double) * lvl_size[h], st), "memset")) break;
+            const long long na = lvl_a[h + 1] - lvl_a[h];
+            if (na > 0) {
+                const int g = (int)std::min<long long>((long long)sm_count * 8, (na + 255) / 256);
+                k_fr_scatter<<<g, 256, 0, st>>>(d_arena, d_scidx + lvl_a[h], d_scv + lvl_a[h], na);
+            }
+            for (const Launch& L : launches[h]) {
+                const int* lst = d_sched + L.list;
+                const int* pre = lst + L.nlist;
+                switch (L.kind) {
+                    case kExtend:
+                        k_fr_extend_add<<<dim3(L.total, L.nlist), 256, 0, st>>>(d_arena, ft, lst, d_parent, d_maps,
+                                                                                 d_mapstart);
+                        break;
+                    case kPotrf: k_fr_potrf<<<L.nlist, 256, 0, st>>>(d_arena, ft, lst, L.k0, d_bad); break;
+                    case kTrsm:
+                        k_fr_trsm<<<L.total, kTrsmRows * 8, 0, st>>>(d_arena, ft, lst, pre, L.nlist, L.k0);
+                        break;
+                    case kSyrk:
+                        k_fr_syrk<<<L.total, 256, syrk_smem, st>>>(d_arena, ft, lst, pre, L.nlist, L.k0);
+                        break;
+                    default:
+                        k_fr_copy_rows<<<L.total, 256, 0, st>>>(d_arena, ft, lst, pre, L.nlist, d_rows, d_soff, d_rp,
+                                                                fct->d_col, fct->d_val);
+                        break;
                 }
-                mo += nu;
-                if (!ck(cudaFreeAsync(F[c], st), "front free")) break;
-                F[c] = nullptr;
             }
-            for (int k0 = 0; k0 < w && !rc; k0 += kFb) {
-                const int kb = std::min(kFb, w - k0), r0 = k0 + kb;
-                k_fr_potrf<<<1, 256, 0, st>>>(F[t], m, k0, kb, d_bad);
-                if (r0 < m) {
-                    k_fr_trsm<<<(m - r0 + 255) / 256, 256, 0, st>>>(F[t], m, k0, kb, r0);
-                    const int tiles = (m - r0 + kFb - 1) / kFb;
-                    k_fr_syrk<<<dim3(tiles, tiles), 256, syrk_smem, st>>>(F[t], m, k0, kb, r0);
-                }
-                ck(cudaGetLastError(), "front kernels");
-            }
-            k_fr_copy_rows<<<w, 256, 0, st>>>(F[t], m, w, d_rp, f0, d_uval);
-            ck(cudaGetLastError(), "front copy");
-            if (front_parent[t] < 0) {
-                ck(cudaFreeAsync(F[t], st), "front free");
-                F[t] = nullptr;
-            }
+            ck(cudaGetLastError(), "front kernels");
         }
         if (rc) break;
         int bad = 0;
-        if (!ck(cudaMemcpyAsync(fct->val.data(), d_uval, sizeof(double) * fct->val.size(), cudaMemcpyDeviceToHost, st),
-                "d2h") ||
-            !ck(cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, st), "d2h") ||
+        if (!ck(cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, st), "d2h") ||
             !ck(cudaStreamSynchronize(st), "sync"))
             break;
         if (bad) rc = SPTRSV_ERR_ZERO_PIVOT;  // not positive definite in this order
     } while (false);
     if (st) {
-        for (double* p : F)
-            if (p) cudaFreeAsync(p, st);
-        for (void* p : {(void*)d_aidx, (void*)d_av, (void*)d_maps, (void*)d_rp, (void*)d_uval, (void*)d_bad})
+        for (void* p : {(void*)d_sched, (void*)d_fstart, (void*)d_fm, (void*)d_parent, (void*)d_maps, (void*)d_foff,
+                        (void*)d_mapstart, (void*)d_scidx, (void*)d_scv, (void*)d_rp, (void*)d_rows, (void*)d_soff,
+                        (void*)d_arena, (void*)d_bad})
             if (p) cudaFreeAsync(p, st);
         cudaStreamSynchronize(st);
         cudaStreamDestroy(st);
@@ -356,6 +598,7 @@ extern "C" int sptrsv_factor_multifrontal(int device, int n, const int64_t* a_rp
         delete fct;
         return rc;
     }
+    fct->numeric_s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_symbolic).count();
     *out = fct;
     return 0;
 }
@@ -373,9 +616,34 @@ extern "C" int sptrsv_factor_copy(void* f, int64_t* row_ptr, int* col, double* v
     if (!f) return SPTRSV_ERR_INVALID_ARG;
     const Factor* F = static_cast<const Factor*>(f);
     if (row_ptr) std::memcpy(row_ptr, F->rp.data(), sizeof(int64_t) * F->rp.size());
-    if (col) std::memcpy(col, F->col.data(), sizeof(int) * F->col.size());
-    if (val) std::memcpy(val, F->val.data(), sizeof(double) * F->val.size());
     if (supernodes) std::memcpy(supernodes, F->snodes.data(), sizeof(int) * F->snodes.size());
+    const int64_t nnz = F->rp[F->n];
+    if (!col && !val) return 0;
+    int cur = 0;
+    CUDA_TRY(cudaGetDevice(&cur));
+    CUDA_TRY(cudaSetDevice(F->device));
+    cudaError_t e = cudaSuccess;
+    if (col) e = cudaMemcpy(col, F->d_col, sizeof(int) * nnz, cudaMemcpyDeviceToHost);
+    if (val && e == cudaSuccess) e = cudaMemcpy(val, F->d_val, sizeof(double) * nnz, cudaMemcpyDeviceToHost);
+    cudaSetDevice(cur);
+    return e == cudaSuccess ? 0 : set_cuda_error(e, "factor copy");
+}
+
+extern "C" int sptrsv_factor_device(void* f, const int** d_row_ptr, const int** d_col, const double** d_val) {
+    if (!f) return SPTRSV_ERR_INVALID_ARG;
+    const Factor* F = static_cast<const Factor*>(f);
+    if (!F->d_rp32) return SPTRSV_ERR_TOO_LARGE;  // 2^31 entries or more: no int32 row pointer
+    if (d_row_ptr) *d_row_ptr = F->d_rp32;
+    if (d_col) *d_col = F->d_col;
+    if (d_val) *d_val = F->d_val;
+    return 0;
+}
+
+extern "C" int sptrsv_factor_times(void* f, double* symbolic_s, double* numeric_s) {
+    if (!f) return SPTRSV_ERR_INVALID_ARG;
+    const Factor* F = static_cast<const Factor*>(f);
+    if (symbolic_s) *symbolic_s = F->symbolic_s;
+    if (numeric_s) *numeric_s = F->numeric_s;
     return 0;
 }
 
