@@ -20,12 +20,14 @@
 // every entry sees the same operations in the same order as a front-by-front run.
 #include <algorithm>
 #include <chrono>
+#include <cstdlib>
 #include <cstdint>
 #include <cstring>
 #include <type_traits>
 #include <vector>
 #include "common.cuh"
 #include "sptrsv_gb300.h"
+#include "tc.cuh"
 
 namespace sptrsv {
 
@@ -226,16 +228,233 @@ __global__ void __launch_bounds__(256) k_fr_syrk(double* __restrict__ arena, Fro
 #pragma unroll
             for (int v = 0; v < 4; ++v) acc[u][v] = fma(a[u], b[v], acc[u][v]);
     }
+    // the 16 outputs are read first, then written (no load waits behind a store)
+    double cur[4][4];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
-        const int row = rA + ty * 4 + u;
-        if (row >= m) continue;
+    for (int u = 0; u < 4; ++u)
 #pragma unroll
         for (int v = 0; v < 4; ++v) {
-            const int colx = rB + tx * 4 + v;
-            if (colx < m && colx <= row) F[(size_t)row + (size_t)colx * m] -= acc[u][v];
+            const int row = rA + ty * 4 + u, colx = rB + tx * 4 + v;
+            cur[u][v] = row < m && colx <= row ? F[(size_t)row + (size_t)colx * m] : 0.0;
+        }
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            const int row = rA + ty * 4 + u, colx = rB + tx * 4 + v;
+            if (row < m && colx <= row) F[(size_t)row + (size_t)colx * m] = cur[u][v] - acc[u][v];
+        }
+}
+
+// ---- the trailing update on the tensor cores
+// C -= P P^T with P the panel's rows below its diagonal tile (K = kb <= 64 columns), FP64-accurate
+// from BF16 digit slices (the fixed-point split product of Ozaki, Ogita, Oishi and Rump, 2012, in
+// tc.cuh): every row i of P is 2^e_i times eight signed 7-bit digit vectors d_1..d_8, so
+// (P P^T)_ij = 2^(e_i + e_j) sum_{p,q} 2^(-7(p+q)) (d_p[i] . d_q[j]).  Pairs with p + q <= 9 are
+// formed (the rest lie below FP64 rounding); the products of one digit diagonal k = p + q share a
+// TMEM accumulator, at most eight 64-term sums of products below 2^14: integers below 2^23, exact
+// in FP32.  The epilogue packs diagonals 2..5 and 6..9 into two integers below 2^44 (exact in
+// int64, then exact as FP64, built by integer operations with the scale in the exponent) and
+// subtracts them from C -- two FP64-pipe operations per output instead of the 64 FMAs of the FP64
+// tile (k_fr_syrk).
+constexpr int kTcBlk = 64;                                  // rows per digit block
+constexpr int kTcSlice = kTcBlk * kFb * 2;                  // one digit slice of a block (K = 64), bytes
+constexpr int kTcRec = tc::kDigits * kTcSlice + kTcBlk * 4;  // a block: eight slices, then row exponents
+constexpr int kTcM = 128, kTcN = 64;                        // output tile: 128 rows x 64 columns
+constexpr size_t kTcSmem = (size_t)tc::kDigits * (kTcM + kTcN) * kFb * 2 + (kTcM + kTcN) * 4 + 128;
+constexpr int kTcMinRest = 256;                             // fronts with fewer rows below use k_fr_syrk
+
+// Digit blocks of the listed fronts' panel rows below the diagonal tile: CTA b of front f makes
+// block b (rows r0 + 64 b ..) in buf at (prefix[f] + b) * kTcRec; rows past the front are zero.
+__global__ void __launch_bounds__(256) k_fr_split(const double* __restrict__ arena, FrontTab ft,
+                                                  const int* __restrict__ list, const int* __restrict__ prefix,
+                                                  int nlist, int k0, unsigned char* __restrict__ buf) {
+    __shared__ double P[kTcBlk][kFb + 1];
+    __shared__ int s_exp[kTcBlk];
+    const int f = fr_item(prefix, nlist, blockIdx.x), t = list[f], b = blockIdx.x - prefix[f];
+    const double* F = arena + ft.foff[t];
+    const int m = ft.fm[t], kb = min(kFb, ft.fstart[t + 1] - ft.fstart[t] - k0);
+    const int row0 = k0 + kb + b * kTcBlk;
+    unsigned char* rec = buf + (size_t)blockIdx.x * kTcRec;
+    if (threadIdx.x < kTcBlk) s_exp[threadIdx.x] = tc::kExpZero;
+    for (int e = threadIdx.x; e < kTcBlk * kFb; e += blockDim.x) {
+        const int rr = e % kTcBlk, c = e / kTcBlk;
+        P[rr][c] = row0 + rr < m && c < kb ? F[(size_t)(row0 + rr) + (size_t)(k0 + c) * m] : 0.0;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < kTcBlk * kFb; e += blockDim.x) {
+        const int rr = e % kTcBlk, c = e / kTcBlk;
+        if (P[rr][c] != 0.0) atomicMax(&s_exp[rr], tc::exp_bound(P[rr][c]));
+    }
+    __syncthreads();
+    // element i of the tile layout: (k & 7) fastest, then (r & 7), (k >> 3), (r >> 3), so that a
+    // warp writes 64 consecutive bytes of every slice
+    for (int i = threadIdx.x; i < kTcBlk * kFb; i += blockDim.x) {
+        const int k = (i & 7) | ((i >> 6) & 7) << 3, rr = ((i >> 3) & 7) | (i >> 9) << 3;
+        float d[tc::kDigits];
+        tc::digits(P[rr][k], s_exp[rr], d);
+#pragma unroll
+        for (int q = 0; q < tc::kDigits; ++q)
+            reinterpret_cast<__nv_bfloat16*>(rec + q * kTcSlice)[i] = __float2bfloat16(d[q]);
+    }
+    if (threadIdx.x < kTcBlk) reinterpret_cast<int*>(rec + tc::kDigits * kTcSlice)[threadIdx.x] = s_exp[threadIdx.x];
+}
+
+// X 2^s as an FP64 value for an integer 0 < |X| < 2^53 -- exact, so built from X's bits with
+// integer operations (sign, leading-bit position, the 52 bits below it, the exponent with s
+// added) instead of a conversion and a multiply on the FP64 pipe; ldexp where the result would not
+// be a normal number.
+__device__ __forceinline__ double fr_exact(long long X, int s) {
+    const unsigned long long a = (unsigned long long)(X < 0 ? -X : X);
+    const int lz = __clzll((long long)a);
+    const int ex = (63 - lz) + s + 1023;
+    if (ex < 1 || ex > 2046) return ldexp((double)X, s);
+    const unsigned long long mant = (a << (lz - 11)) & 0xFFFFFFFFFFFFFull;
+    return __longlong_as_double((long long)((X < 0 ? 1ull << 63 : 0ull) | ((unsigned long long)ex << 52) | mant));
+}
+
+// One 128 x 64 tile (row block I, column block J; 64 J <= 128 I + 127) of each listed front's
+// trailing lower triangle: bulk copies of the digit blocks (A: blocks 2I, 2I+1; B: block J), 144
+// MMAs of 128 x 64 x 16 by one thread into eight accumulators, then every thread one row of the
+// tile.  Waits are bounded; a timeout records SPTRSV_ERR_TIMEOUT in ctl and the tile is skipped
+// after the copies and MMAs this CTA started have drained.
+__global__ void __launch_bounds__(128, 1) k_fr_syrk_tc(double* __restrict__ arena, FrontTab ft,
+                                                       const int* __restrict__ list, const int* __restrict__ prefix,
+                                                       int nlist, const int* __restrict__ sprefix, int k0,
+                                                       const unsigned char* __restrict__ buf, Ctl* ctl,
+                                                       int64_t budget) {
+    extern __shared__ __align__(128) unsigned char fr_tc[];
+    unsigned char* sA = fr_tc;                                          // 8 slices x 128 rows x 64
+    unsigned char* sB = fr_tc + (size_t)tc::kDigits * kTcM * kFb * 2;   // 8 slices x 64 rows x 64
+    int* sAe = reinterpret_cast<int*>(sB + (size_t)tc::kDigits * kTcN * kFb * 2);
+    int* sBe = sAe + kTcM;
+    __shared__ __align__(8) uint64_t barL, barM;
+    __shared__ uint32_t s_tmem;
+    __shared__ int s_ok;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int f = fr_item(prefix, nlist, blockIdx.x), t = list[f];
+    double* F = arena + ft.foff[t];
+    const int m = ft.fm[t], kb = min(kFb, ft.fstart[t + 1] - ft.fstart[t] - k0), r0 = k0 + kb;
+    const int nJ = (m - r0 + kTcN - 1) / kTcN;
+    int e = blockIdx.x - prefix[f], I = 0;
+    for (;;) {
+        const int c = min(2 * I + 2, nJ);
+        if (e < c) break;
+        e -= c;
+        ++I;
+    }
+    const int J = e;
+    const unsigned char* blocks = buf + (size_t)sprefix[f] * kTcRec;
+    if (warp == 0) tc::tmem_alloc(&s_tmem, tc::kDigits * kTcN);
+    if (tid == 0) {
+        tc::mbar_init(&barL, 1);
+        tc::mbar_init(&barM, 1);
+    }
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    const uint32_t tmem = s_tmem;
+    if (tid == 0) {
+        constexpr unsigned kSlA = kTcM * kFb * 2, kSlB = kTcN * kFb * 2;
+        tc::mbar_expect_tx(&barL, tc::kDigits * (kSlA + kSlB) + (kTcM + kTcN) * 4);
+        for (int h = 0; h < 2; ++h) {
+            const unsigned char* rec = blocks + (size_t)(2 * I + h) * kTcRec;
+            for (int q = 0; q < tc::kDigits; ++q)
+                tc::bulk_g2s(sA + q * kSlA + h * kTcSlice, rec + q * kTcSlice, kTcSlice, &barL);
+            tc::bulk_g2s(sAe + kTcBlk * h, rec + tc::kDigits * kTcSlice, kTcBlk * 4, &barL);
+        }
+        const unsigned char* rec = blocks + (size_t)J * kTcRec;
+        tc::bulk_g2s(sB, rec, tc::kDigits * kTcSlice, &barL);
+        tc::bulk_g2s(sBe, rec + tc::kDigits * kTcSlice, kTcBlk * 4, &barL);
+        bool ok = tc::mbar_wait(&barL, 0, ctl, budget);
+        if (ok) {
+            tc::fence_after();
+            const uint32_t id = tc::idesc_bf16_f32(kTcM, kTcN), a0 = tc::smem(sA), b0 = tc::smem(sB);
+            for (int k = 2; k <= 9; ++k) {
+                uint32_t acc = 0;
+                for (int p = max(1, k - tc::kDigits); p <= min(tc::kDigits, k - 1); ++p) {
+                    const int q = k - p;
+                    for (int ks = 0; ks < kFb / 16; ++ks) {
+                        const uint64_t da = tc::desc(a0 + (p - 1) * kSlA + ks * 256, 128, kFb * 16);
+                        const uint64_t db = tc::desc(b0 + (q - 1) * kSlB + ks * 256, 128, kFb * 16);
+                        tc::mma_bf16(tmem + (uint32_t)(k - 2) * kTcN, da, db, id, acc);
+                        acc = 1;
+                    }
+                }
+            }
+            tc::mma_commit(&barM);
+        } else {
+            tc::mbar_drain(&barL, 0, budget);  // the copies this CTA started end first
+        }
+        s_ok = ok;
+    }
+    __syncthreads();
+    if (s_ok) {
+        // this thread's row of the tile: its C entries are read 16 at a time, each chunk's loads
+        // issued before the previous chunk's stores (the first while the MMAs run)
+        const int R = 32 * warp + lane, row = r0 + I * kTcM + R, ei = sAe[R];
+        const bool live = row < m && ei != tc::kExpZero;
+        const double* crow = F + (size_t)(live ? row : 0);
+        auto load_chunk = [&](int c0, double* cv) {
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                const int col = r0 + J * kTcN + c0 + j;
+                cv[j] = live && col <= row ? crow[(size_t)col * m] : 0.0;
+            }
+        };
+        double cv[16];
+        load_chunk(0, cv);
+        const bool got = tc::mbar_wait(&barM, 0, ctl, budget);
+        if (!got) tc::mbar_drain(&barM, 0, budget);
+        tc::fence_after();
+#pragma unroll 1
+        for (int c0 = 0; c0 < kTcN; c0 += 16) {
+            double nx[16];
+            if (c0 + 16 < kTcN) load_chunk(c0 + 16, nx);
+            long long th[16], tl[16];
+#pragma unroll
+            for (int j = 0; j < 16; ++j) th[j] = tl[j] = 0;
+            // diagonals 2..5, then 6..9: four loads in flight per wait
+#pragma unroll
+            for (int half = 0; half < 2; ++half) {
+                uint32_t v[4][16];
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                    tc::tmem_ld16_async(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(4 * half + u) * kTcN + c0,
+                                        v[u]);
+                tc::tmem_wait_ld();
+#pragma unroll
+                for (int u = 0; u < 4; ++u) tc::tmem_regs_after_wait(v[u]);
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) {
+                        const long long a = (long long)__float2int_rn(__uint_as_float(v[u][j]));
+                        if (half == 0) th[j] += a * (1ll << (7 * (3 - u)));  // diagonal k = 2 + u
+                        else tl[j] += a * (1ll << (7 * (3 - u)));            // diagonal k = 6 + u
+                    }
+            }
+            if (got && live) {
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    const int col = r0 + J * kTcN + c0 + j, ej = sBe[c0 + j];
+                    if (col > row || ej == tc::kExpZero) continue;
+                    // sum_k acc_k 2^(-7k) = th 2^-35 + tl 2^-63, each part exact in FP64
+                    double v = cv[j];
+                    if (tl[j]) v -= fr_exact(tl[j], ei + ej - 63);
+                    if (th[j]) v -= fr_exact(th[j], ei + ej - 35);
+                    F[(size_t)row + (size_t)col * m] = v;
+                }
+            }
+            if (c0 + 16 < kTcN) {
+#pragma unroll
+                for (int j = 0; j < 16; ++j) cv[j] = nx[j];
+            }
         }
     }
+    tc::fence_before();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tmem, tc::kDigits * kTcN);
 }
 
 // U's rows of the listed fronts: one CTA per pivot, row f0 + k (k < w) holds columns S_t[k:]
@@ -429,16 +648,22 @@ extern "C" int sptrsv_factor_multifrontal(int device, int n, const int64_t* a_rp
         soff[t] = (int64_t)rows.size();
         rows.insert(rows.end(), S[t].begin(), S[t].end());
     }
-    enum { kExtend, kPotrf, kTrsm, kSyrk, kCopy };
+    enum { kExtend, kPotrf, kTrsm, kSyrk, kSplit, kSyrkTc, kCopy };
     struct Launch {
         int kind, k0, nlist, total;  // total: CTAs (kExtend: CTAs per child)
         int64_t list;                // offset of the list in sched; the CTA prefix (nlist + 1) follows it
+        int64_t aux;                 // kSyrkTc: offset of the matching kSplit launch's list
     };
+    // the trailing updates of fronts with at least kTcMinRest rows below the panel go to the tensor
+    // cores unless SPTRSV_FACTOR_UPDATE=fp64
+    const char* upd_env = getenv("SPTRSV_FACTOR_UPDATE");
+    const bool use_tc = !(upd_env && std::strcmp(upd_env, "fp64") == 0);
+    int64_t tc_blocks_max = 0;
     std::vector<int> sched;
     std::vector<std::vector<Launch>> launches(H);
     auto add = [&](int h, int kind, int k0, const std::vector<int>& lst, const std::vector<int>& cnt, int total) {
         if (lst.empty()) return;
-        Launch L{kind, k0, (int)lst.size(), total, (int64_t)sched.size()};
+        Launch L{kind, k0, (int)lst.size(), total, (int64_t)sched.size(), 0};
         sched.insert(sched.end(), lst.begin(), lst.end());
         if (!cnt.empty()) {
             int acc = 0;
@@ -475,7 +700,7 @@ extern "C" int sptrsv_factor_multifrontal(int device, int n, const int64_t* a_rp
         for (int t : level[h]) panels = std::max(panels, (front_start[t + 1] - front_start[t] + kFb - 1) / kFb);
         for (int p = 0; p < panels; ++p) {
             const int k0 = p * kFb;
-            std::vector<int> fac, upd, n_trsm, n_syrk;
+            std::vector<int> fac, upd, n_trsm, upd64, n_syrk, updtc, n_split, n_tc;
             for (int t : level[h]) {
                 const int w = front_start[t + 1] - front_start[t];
                 if (w <= k0) continue;
@@ -484,12 +709,29 @@ extern "C" int sptrsv_factor_multifrontal(int device, int n, const int64_t* a_rp
                 if (rest <= 0) continue;
                 upd.push_back(t);
                 n_trsm.push_back((rest + kTrsmRows - 1) / kTrsmRows);
-                const int tiles = (rest + kFb - 1) / kFb;
-                n_syrk.push_back(tiles * (tiles + 1) / 2);
+                if (use_tc && rest >= kTcMinRest) {
+                    const int nI = (rest + kTcM - 1) / kTcM, nJ = (rest + kTcN - 1) / kTcN;
+                    int tiles = 0;
+                    for (int i = 0; i < nI; ++i) tiles += std::min(2 * i + 2, nJ);
+                    updtc.push_back(t);
+                    n_split.push_back(2 * nI);
+                    n_tc.push_back(tiles);
+                } else {
+                    const int tiles = (rest + kFb - 1) / kFb;
+                    upd64.push_back(t);
+                    n_syrk.push_back(tiles * (tiles + 1) / 2);
+                }
             }
             add(h, kPotrf, k0, fac, {}, (int)fac.size());
             add(h, kTrsm, k0, upd, n_trsm, 0);
-            add(h, kSyrk, k0, upd, n_syrk, 0);
+            if (!updtc.empty()) {
+                add(h, kSplit, k0, updtc, n_split, 0);
+                const int64_t split_list = launches[h].back().list;
+                tc_blocks_max = std::max<int64_t>(tc_blocks_max, launches[h].back().total);
+                add(h, kSyrkTc, k0, updtc, n_tc, 0);
+                launches[h].back().aux = split_list;
+            }
+            add(h, kSyrk, k0, upd64, n_syrk, 0);
         }
         std::vector<int> widths;
         for (int t : level[h]) widths.push_back(front_start[t + 1] - front_start[t]);
@@ -506,6 +748,8 @@ extern "C" int sptrsv_factor_multifrontal(int device, int n, const int64_t* a_rp
     double *d_scv = nullptr, *d_arena = nullptr;
     const int64_t unnz = fct->rp[n];
     int* d_bad = nullptr;
+    unsigned char* d_tcbuf = nullptr;
+    Ctl* d_ctl = nullptr;
     auto fail = [&](cudaError_t e, const char* what) {
         if (!rc) rc = set_cuda_error(e, what);
     };
@@ -517,7 +761,8 @@ extern "C" int sptrsv_factor_multifrontal(int device, int n, const int64_t* a_rp
     do {
         if (!ck(cudaSetDevice(device), "cudaSetDevice")) break;
         if (!ck(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "stream")) break;
-        if (!ck(cudaFuncSetAttribute(k_fr_syrk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)syrk_smem), "attr"))
+        if (!ck(cudaFuncSetAttribute(k_fr_syrk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)syrk_smem), "attr") ||
+            !ck(cudaFuncSetAttribute(k_fr_syrk_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem), "attr"))
             break;
         int sm_count = 0;
         if (!ck(cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, device), "attr")) break;
@@ -546,7 +791,12 @@ extern "C" int sptrsv_factor_multifrontal(int device, int n, const int64_t* a_rp
         }
         if (!ck(cudaMallocAsync((void**)&d_arena, sizeof(double) * std::max<int64_t>(1, arena_size), st), "arena") ||
             !ck(cudaMallocAsync((void**)&d_bad, sizeof(int), st), "alloc") ||
-            !ck(cudaMemsetAsync(d_bad, 0, sizeof(int), st), "memset"))
+            !ck(cudaMemsetAsync(d_bad, 0, sizeof(int), st), "memset") ||
+            !ck(cudaMallocAsync((void**)&d_ctl, sizeof(Ctl), st), "alloc") ||
+            !ck(cudaMemsetAsync(d_ctl, 0, sizeof(Ctl), st), "memset"))
+            break;
+        if (tc_blocks_max > 0 &&
+            !ck(cudaMallocAsync((void**)&d_tcbuf, (size_t)tc_blocks_max * kTcRec, st), "digit blocks"))
             break;
         const FrontTab ft{d_fstart, d_fm, d_foff};
         for (int h = 0; h < H && !rc; ++h) {
@@ -571,6 +821,14 @@ extern "C" int sptrsv_factor_multifrontal(int device, int n, const int64_t* a_rp
                     case kSyrk:
                         k_fr_syrk<<<L.total, 256, syrk_smem, st>>>(d_arena, ft, lst, pre, L.nlist, L.k0);
                         break;
+                    case kSplit:
+                        k_fr_split<<<L.total, 256, 0, st>>>(d_arena, ft, lst, pre, L.nlist, L.k0, d_tcbuf);
+                        break;
+                    case kSyrkTc:
+                        k_fr_syrk_tc<<<L.total, 128, kTcSmem, st>>>(d_arena, ft, lst, pre, L.nlist,
+                                                                     d_sched + L.aux + L.nlist, L.k0, d_tcbuf, d_ctl,
+                                                                     kDefaultBudgetNs);
+                        break;
                     default:
                         k_fr_copy_rows<<<L.total, 256, 0, st>>>(d_arena, ft, lst, pre, L.nlist, d_rows, d_soff, d_rp,
                                                                 fct->d_col, fct->d_val);
@@ -580,16 +838,18 @@ extern "C" int sptrsv_factor_multifrontal(int device, int n, const int64_t* a_rp
             ck(cudaGetLastError(), "front kernels");
         }
         if (rc) break;
-        int bad = 0;
+        int bad = 0, status = 0;
         if (!ck(cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, st), "d2h") ||
+            !ck(cudaMemcpyAsync(&status, &d_ctl->status, sizeof(int), cudaMemcpyDeviceToHost, st), "d2h") ||
             !ck(cudaStreamSynchronize(st), "sync"))
             break;
-        if (bad) rc = SPTRSV_ERR_ZERO_PIVOT;  // not positive definite in this order
+        if (status) rc = status;              // a bounded wait of the tensor-core update gave up
+        else if (bad) rc = SPTRSV_ERR_ZERO_PIVOT;  // not positive definite in this order
     } while (false);
     if (st) {
         for (void* p : {(void*)d_sched, (void*)d_fstart, (void*)d_fm, (void*)d_parent, (void*)d_maps, (void*)d_foff,
                         (void*)d_mapstart, (void*)d_scidx, (void*)d_scv, (void*)d_rp, (void*)d_rows, (void*)d_soff,
-                        (void*)d_arena, (void*)d_bad})
+                        (void*)d_arena, (void*)d_bad, (void*)d_tcbuf, (void*)d_ctl})
             if (p) cudaFreeAsync(p, st);
         cudaStreamSynchronize(st);
         cudaStreamDestroy(st);

@@ -177,3 +177,39 @@ def test_factor_device_arrays_feed_the_solver():
         assert np.linalg.norm(Um @ x_dev - b) <= 1e-12 * np.linalg.norm(b)
     finally:
         L.sptrsv_factor_free(h)
+
+
+def _scaled_spd(n, seed, spread=20):
+    """A dense SPD matrix D S D: S random and diagonally dominant, D powers of two in
+    2^-spread .. 2^spread (U(D S D) = U(S) D, so every column of U keeps S's relative accuracy)."""
+    rng = np.random.default_rng(seed)
+    R = rng.uniform(-1, 1, (n, n))
+    S = (R + R.T) / 2
+    S += np.diag(np.sum(np.abs(S), axis=1) + 1.0)
+    d = np.ldexp(1.0, rng.integers(-spread, spread + 1, n))
+    return S, d
+
+
+@pytest.mark.parametrize("update", ["tc", "fp64"])
+def test_factor_wide_trailing_updates(update, monkeypatch):
+    # a 100-pivot front (panels of 64 and 36 columns) over a 600-row root: 600 and 536 rows below
+    # the panels, the tensor-core update's range (and its K padding), with rows scaled over 40 binades
+    if update == "fp64":
+        monkeypatch.setenv("SPTRSV_FACTOR_UPDATE", "fp64")
+    S, d = _scaled_spd(700, 8)
+    A = S * d[:, None] * d[None, :]
+    U, _ = _factor_dense(A, [0, 100, 700], [1, -1])
+    Us = np.linalg.cholesky(S).T
+    assert np.max(np.abs(U / d[None, :] - Us)) <= 1e-12 * np.max(np.abs(Us))
+
+
+def test_factor_update_forms_agree(monkeypatch):
+    # the 24^3 nested-dissection factor by both trailing-update forms, and against the host factor
+    tc_form = gen.laplace3d_nd_cholesky_gpu(24)
+    monkeypatch.setenv("SPTRSV_FACTOR_UPDATE", "fp64")
+    fp64_form = gen.laplace3d_nd_cholesky_gpu(24)
+    monkeypatch.delenv("SPTRSV_FACTOR_UPDATE")
+    host = gen.laplace3d_nd_cholesky(24)
+    _same_factor(tc_form, host)
+    _same_factor(fp64_form, host)
+    assert np.max(np.abs(tc_form.val - fp64_form.val)) <= 1e-13 * np.max(np.abs(host.val))
