@@ -1073,9 +1073,14 @@ def run_factor(args, dist):
            "n": n, "nnz_A": int(rp[-1]), "nnz_U": int(nnz.value), "supernodes": int(nsn.value),
            "steps": len(times), "value": wall, "symbolic_s": sym, "numeric_s": num, "copy_to_host_s": copy,
            "all_wall_s": [t[0] for t in times],
+           "update_form": ("FP64 FMAs" if os.environ.get("SPTRSV_FACTOR_UPDATE") == "fp64" else
+                           "tensor cores (BF16 digit slices, FP64-accurate) for fronts with >= 256 rows below "
+                           "the panel, FP64 FMAs for the rest"),
            "flops": flops, "numeric_gflop_per_s": flops / num / 1e9,
            "frac_of_measured_fp64": flops / num / 1e9 / (2.0 * pipe["gfma_per_s"]),
-           "measured_fp64_gfma_per_s": pipe["gfma_per_s"]}
+           "measured_fp64_gfma_per_s": pipe["gfma_per_s"],
+           "rate_note": "FLOPs of the FP64 factorisation (sum of c_j^2) over the numeric step; with the "
+                        "tensor-core updates this is an FP64-equivalent rate and can exceed the FP64 pipe"}
     if not args.no_cpu_baseline:
         t0 = time.perf_counter()
         hm = gen.laplace3d_nd_cholesky(g)

@@ -92,10 +92,12 @@ __global__ void k_fr_extend_add(double* __restrict__ arena, FrontTab ft, const i
 
 // Cholesky of the kb x kb diagonal tile at (k0, k0) of front list[blockIdx.x], lower, in place
 // (one CTA of 256 threads per front).  A pivot that is not positive (or not finite) sets *bad and
-// the factor is not used.  The chain that orders the columns is one reciprocal square root per
-// column (thread 0; the column is scaled by it and its diagonal is d * rsqrt(d)); the rank-1
-// update of the rest walks the entries of its lower triangle only, from a table of (row, column)
-// pairs, so no lane idles on the upper half.
+// the factor is not used.  Column j is scaled by the reciprocal square root of its pivot (its
+// diagonal becomes d * rsqrt(d)), then the rest of the tile takes its rank-1 update.  The next
+// pivot is final as soon as its own update is made, so warp 7 makes that one update and the next
+// reciprocal root while warps 0-6 update the other entries of the rest's lower triangle (from a
+// table of (row, column) pairs: no lane idles on the upper half): the square root is off the
+// chain of columns, which is one scale and one update step per column.
 __global__ void __launch_bounds__(256) k_fr_potrf(double* __restrict__ arena, FrontTab ft,
                                                   const int* __restrict__ list, int k0, int* bad) {
     __shared__ double T[kFb][kFb + 1];
@@ -104,6 +106,7 @@ __global__ void __launch_bounds__(256) k_fr_potrf(double* __restrict__ arena, Fr
     const int t = list[blockIdx.x];
     double* F = arena + ft.foff[t];
     const int m = ft.fm[t], kb = min(kFb, ft.fstart[t + 1] - ft.fstart[t] - k0);
+    constexpr int kUpd = 224;  // threads of warps 0-6
     for (int e = threadIdx.x; e < kb * kb; e += blockDim.x) {
         const int r = e % kb, c = e / kb;
         T[r][c] = r >= c ? F[(size_t)(k0 + r) + (size_t)(k0 + c) * m] : 0.0;
@@ -114,22 +117,29 @@ __global__ void __launch_bounds__(256) k_fr_potrf(double* __restrict__ arena, Fr
         pairs[e] = i << 8 | c;
     }
     __syncthreads();
+    // the root of pivot j: its reciprocal to rs, the root itself in place
+    auto root = [&](int j) {
+        const double d = T[j][j];
+        if (!(d > 0.0) || !isfinite(d)) atomicExch(bad, 1);
+        const double dd = d > 0.0 ? d : 1.0, r = rsqrt(dd);
+        T[j][j] = dd * r;
+        rs = r;
+    };
+    if (threadIdx.x == kUpd) root(0);
+    __syncthreads();
     for (int j = 0; j < kb; ++j) {
-        if (threadIdx.x == 0) {
-            const double d = T[j][j];
-            if (!(d > 0.0) || !isfinite(d)) atomicExch(bad, 1);
-            const double r = rsqrt(d > 0.0 ? d : 1.0);
-            T[j][j] = (d > 0.0 ? d : 1.0) * r;
-            rs = r;
-        }
-        __syncthreads();
         const double r = rs;
         for (int i = j + 1 + threadIdx.x; i < kb; i += blockDim.x) T[i][j] *= r;
         __syncthreads();
         const int rest = kb - j - 1, np = rest * (rest + 1) / 2;
-        for (int e = threadIdx.x; e < np; e += blockDim.x) {
-            const int pr = pairs[e], i = j + 1 + (pr >> 8), c = j + 1 + (pr & 255);
-            T[i][c] = fma(-T[i][j], T[c][j], T[i][c]);
+        if (threadIdx.x < kUpd) {
+            for (int e = 1 + threadIdx.x; e < np; e += kUpd) {
+                const int pr = pairs[e], i = j + 1 + (pr >> 8), c = j + 1 + (pr & 255);
+                T[i][c] = fma(-T[i][j], T[c][j], T[i][c]);
+            }
+        } else if (threadIdx.x == kUpd && rest > 0) {
+            T[j + 1][j + 1] = fma(-T[j + 1][j], T[j + 1][j], T[j + 1][j + 1]);
+            root(j + 1);
         }
         __syncthreads();
     }
@@ -260,9 +270,14 @@ __global__ void __launch_bounds__(256) k_fr_syrk(double* __restrict__ arena, Fro
 constexpr int kTcBlk = 64;                                  // rows per digit block
 constexpr int kTcSlice = kTcBlk * kFb * 2;                  // one digit slice of a block (K = 64), bytes
 constexpr int kTcRec = tc::kDigits * kTcSlice + kTcBlk * 4;  // a block: eight slices, then row exponents
-constexpr int kTcM = 128, kTcN = 64;                        // output tile: 128 rows x 64 columns
-constexpr size_t kTcSmem = (size_t)tc::kDigits * (kTcM + kTcN) * kFb * 2 + (kTcM + kTcN) * 4 + 128;
+constexpr int kTcM = 128, kTcN = 32;                        // output tile: 128 rows x 32 columns
+constexpr int kTcChunk = 4;                                 // tiles per CTA (128 columns), one A block
+constexpr int kTcEpiWarps = 8;                              // epilogue warps; warp 8 loads and issues
+constexpr unsigned kTcSlA = kTcM * kFb * 2, kTcSlB = kTcN * kFb * 2;  // one digit slice of A / of B
+constexpr size_t kTcSmem = (size_t)tc::kDigits * (kTcSlA + 2 * kTcSlB) + (kTcM + kTcChunk * kTcN) * 4 + 128;
 constexpr int kTcMinRest = 256;                             // fronts with fewer rows below use k_fr_syrk
+// CTAs of one front's tensor-core update: row block I takes min(I + 1, chunks) chunks of tiles
+__host__ __device__ __forceinline__ int tc_ctas_of_block(int I, int nchunks) { return I + 1 < nchunks ? I + 1 : nchunks; }
 
 // Digit blocks of the listed fronts' panel rows below the diagonal tile: CTA b of front f makes
 // block b (rows r0 + 64 b ..) in buf at (prefix[f] + b) * kTcRec; rows past the front are zero.
@@ -313,114 +328,140 @@ __device__ __forceinline__ double fr_exact(long long X, int s) {
     return __longlong_as_double((long long)((X < 0 ? 1ull << 63 : 0ull) | ((unsigned long long)ex << 52) | mant));
 }
 
-// One 128 x 64 tile (row block I, column block J; 64 J <= 128 I + 127) of each listed front's
-// trailing lower triangle: bulk copies of the digit blocks (A: blocks 2I, 2I+1; B: block J), 144
-// MMAs of 128 x 64 x 16 by one thread into eight accumulators, then every thread one row of the
-// tile.  Waits are bounded; a timeout records SPTRSV_ERR_TIMEOUT in ctl and the tile is skipped
-// after the copies and MMAs this CTA started have drained.
-__global__ void __launch_bounds__(128, 1) k_fr_syrk_tc(double* __restrict__ arena, FrontTab ft,
-                                                       const int* __restrict__ list, const int* __restrict__ prefix,
-                                                       int nlist, const int* __restrict__ sprefix, int k0,
-                                                       const unsigned char* __restrict__ buf, Ctl* ctl,
-                                                       int64_t budget) {
+// Tiles 4c .. 4c+3 (32 columns each, those with a part on or below the diagonal) of row block I
+// (128 rows) of each listed front's trailing lower triangle.  Warp 8 is the producer: bulk copies
+// of the A digit blocks (2I, 2I+1, kept for the whole chunk) and, per tile, of the B digits (half
+// a block) into one of two buffers, then 144 MMAs of 128 x 32 x 16 by one thread into one of two
+// TMEM accumulator sets (eight digit diagonals x 32 columns each).  Warps 0-7 are the epilogue:
+// warp w reads TMEM lanes 32 (w % 4) .. + 31 and columns 16 (w / 4) .. + 15 of the tile, so the
+// MMAs of tile n + 1 run while tile n's outputs are formed and written.  Barriers: A (once), B
+// and MMA per buffer (phase = use of the buffer), epilogue-done per TMEM set (256 arrivals).  All
+// waits are bounded; a timeout records SPTRSV_ERR_TIMEOUT in ctl, which every waiter polls.
+__global__ void __launch_bounds__(32 * (kTcEpiWarps + 1), 1)
+    k_fr_syrk_tc(double* __restrict__ arena, FrontTab ft, const int* __restrict__ list,
+                 const int* __restrict__ prefix, int nlist, const int* __restrict__ sprefix, int k0,
+                 const unsigned char* __restrict__ buf, Ctl* ctl, int64_t budget) {
     extern __shared__ __align__(128) unsigned char fr_tc[];
-    unsigned char* sA = fr_tc;                                          // 8 slices x 128 rows x 64
-    unsigned char* sB = fr_tc + (size_t)tc::kDigits * kTcM * kFb * 2;   // 8 slices x 64 rows x 64
-    int* sAe = reinterpret_cast<int*>(sB + (size_t)tc::kDigits * kTcN * kFb * 2);
-    int* sBe = sAe + kTcM;
-    __shared__ __align__(8) uint64_t barL, barM;
+    unsigned char* sA = fr_tc;                                      // 8 slices x 128 rows x 64
+    unsigned char* sB = fr_tc + (size_t)tc::kDigits * kTcSlA;       // 2 buffers x 8 slices x 32 rows x 64
+    int* sAe = reinterpret_cast<int*>(sB + 2 * (size_t)tc::kDigits * kTcSlB);
+    int* sBe = sAe + kTcM;                                          // the chunk's columns
+    __shared__ __align__(8) uint64_t barA, barB[2], barM[2], barE[2];
     __shared__ uint32_t s_tmem;
-    __shared__ int s_ok;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int f = fr_item(prefix, nlist, blockIdx.x), t = list[f];
     double* F = arena + ft.foff[t];
     const int m = ft.fm[t], kb = min(kFb, ft.fstart[t + 1] - ft.fstart[t] - k0), r0 = k0 + kb;
-    const int nJ = (m - r0 + kTcN - 1) / kTcN;
+    const int nJ = (m - r0 + kTcN - 1) / kTcN, nC = (nJ + kTcChunk - 1) / kTcChunk;
     int e = blockIdx.x - prefix[f], I = 0;
     for (;;) {
-        const int c = min(2 * I + 2, nJ);
+        const int c = tc_ctas_of_block(I, nC);
         if (e < c) break;
         e -= c;
         ++I;
     }
-    const int J = e;
+    const int J0 = e * kTcChunk, nt = min(kTcChunk, min(4 * I + 4, nJ) - J0);  // tiles J0 .. J0+nt-1
     const unsigned char* blocks = buf + (size_t)sprefix[f] * kTcRec;
-    if (warp == 0) tc::tmem_alloc(&s_tmem, tc::kDigits * kTcN);
+    if (warp == 0) tc::tmem_alloc(&s_tmem, 2 * tc::kDigits * kTcN);
     if (tid == 0) {
-        tc::mbar_init(&barL, 1);
-        tc::mbar_init(&barM, 1);
+        tc::mbar_init(&barA, 1);
+        for (int b = 0; b < 2; ++b) {
+            tc::mbar_init(&barB[b], 1);
+            tc::mbar_init(&barM[b], 1);
+            tc::mbar_init(&barE[b], 32 * kTcEpiWarps);
+        }
     }
     tc::fence_before();
     __syncthreads();
     tc::fence_after();
     const uint32_t tmem = s_tmem;
-    if (tid == 0) {
-        constexpr unsigned kSlA = kTcM * kFb * 2, kSlB = kTcN * kFb * 2;
-        tc::mbar_expect_tx(&barL, tc::kDigits * (kSlA + kSlB) + (kTcM + kTcN) * 4);
-        for (int h = 0; h < 2; ++h) {
-            const unsigned char* rec = blocks + (size_t)(2 * I + h) * kTcRec;
-            for (int q = 0; q < tc::kDigits; ++q)
-                tc::bulk_g2s(sA + q * kSlA + h * kTcSlice, rec + q * kTcSlice, kTcSlice, &barL);
-            tc::bulk_g2s(sAe + kTcBlk * h, rec + tc::kDigits * kTcSlice, kTcBlk * 4, &barL);
-        }
-        const unsigned char* rec = blocks + (size_t)J * kTcRec;
-        tc::bulk_g2s(sB, rec, tc::kDigits * kTcSlice, &barL);
-        tc::bulk_g2s(sBe, rec + tc::kDigits * kTcSlice, kTcBlk * 4, &barL);
-        bool ok = tc::mbar_wait(&barL, 0, ctl, budget);
-        if (ok) {
-            tc::fence_after();
-            const uint32_t id = tc::idesc_bf16_f32(kTcM, kTcN), a0 = tc::smem(sA), b0 = tc::smem(sB);
-            for (int k = 2; k <= 9; ++k) {
-                uint32_t acc = 0;
-                for (int p = max(1, k - tc::kDigits); p <= min(tc::kDigits, k - 1); ++p) {
-                    const int q = k - p;
-                    for (int ks = 0; ks < kFb / 16; ++ks) {
-                        const uint64_t da = tc::desc(a0 + (p - 1) * kSlA + ks * 256, 128, kFb * 16);
-                        const uint64_t db = tc::desc(b0 + (q - 1) * kSlB + ks * 256, 128, kFb * 16);
-                        tc::mma_bf16(tmem + (uint32_t)(k - 2) * kTcN, da, db, id, acc);
-                        acc = 1;
+    if (warp == kTcEpiWarps) {
+        if (lane == 0) {
+            // A (two blocks) and the exponents of the chunk's B rows, then the first two B tiles
+            tc::mbar_expect_tx(&barA, tc::kDigits * kTcSlA + kTcM * 4 + nt * kTcN * 4);
+            for (int h = 0; h < 2; ++h) {
+                const unsigned char* rec = blocks + (size_t)(2 * I + h) * kTcRec;
+                for (int q = 0; q < tc::kDigits; ++q)
+                    tc::bulk_g2s(sA + q * kTcSlA + h * kTcSlice, rec + q * kTcSlice, kTcSlice, &barA);
+                tc::bulk_g2s(sAe + kTcBlk * h, rec + tc::kDigits * kTcSlice, kTcBlk * 4, &barA);
+            }
+            for (int n = 0; n < nt; ++n) {
+                const int J = J0 + n;
+                tc::bulk_g2s(sBe + n * kTcN, blocks + (size_t)(J >> 1) * kTcRec + tc::kDigits * kTcSlice + (J & 1) * kTcN * 4,
+                             kTcN * 4, &barA);
+            }
+            int loads[2] = {0, 0}, commits[2] = {0, 0};  // uses of each buffer's barriers
+            auto load_b = [&](int n) {  // B digits of tile n into buffer n & 1
+                const int J = J0 + n, b = n & 1;
+                ++loads[b];
+                const unsigned char* rec = blocks + (size_t)(J >> 1) * kTcRec + (J & 1) * kTcSlB;
+                tc::mbar_expect_tx(&barB[b], tc::kDigits * kTcSlB);
+                for (int q = 0; q < tc::kDigits; ++q)
+                    tc::bulk_g2s(sB + ((size_t)b * tc::kDigits + q) * kTcSlB, rec + q * kTcSlice, kTcSlB, &barB[b]);
+            };
+            load_b(0);
+            if (nt > 1) load_b(1);
+            bool ok = tc::mbar_wait(&barA, 0, ctl, budget);
+            const uint32_t id = tc::idesc_bf16_f32(kTcM, kTcN), a0 = tc::smem(sA);
+            for (int n = 0; n < nt && ok; ++n) {
+                const int b = n & 1;
+                const unsigned ph = (n >> 1) & 1;
+                ok = tc::mbar_wait(&barB[b], ph, ctl, budget);
+                if (ok && n >= 2) ok = tc::mbar_wait(&barE[b], ph ^ 1, ctl, budget);  // tile n-2 read out
+                if (!ok) break;
+                tc::fence_after();
+                const uint32_t b0 = tc::smem(sB + (size_t)b * tc::kDigits * kTcSlB), d0 = tmem + (uint32_t)b * tc::kDigits * kTcN;
+                for (int k = 2; k <= 9; ++k) {
+                    uint32_t acc = 0;
+                    for (int p = max(1, k - tc::kDigits); p <= min(tc::kDigits, k - 1); ++p) {
+                        const int q = k - p;
+                        for (int ks = 0; ks < kFb / 16; ++ks) {
+                            const uint64_t da = tc::desc(a0 + (p - 1) * kTcSlA + ks * 256, 128, kFb * 16);
+                            const uint64_t db = tc::desc(b0 + (q - 1) * kTcSlB + ks * 256, 128, kFb * 16);
+                            tc::mma_bf16(d0 + (uint32_t)(k - 2) * kTcN, da, db, id, acc);
+                            acc = 1;
+                        }
                     }
                 }
+                tc::mma_commit(&barM[b]);
+                ++commits[b];
+                if (n + 2 < nt) {  // buffer b again for tile n + 2 once these MMAs have read it
+                    ok = tc::mbar_wait(&barM[b], ph, ctl, budget);
+                    if (ok) load_b(n + 2);
+                }
             }
-            tc::mma_commit(&barM);
-        } else {
-            tc::mbar_drain(&barL, 0, budget);  // the copies this CTA started end first
+            // nothing of ours left in flight: the last phase of every barrier this thread armed
+            // completes (a barrier's earlier phases completed before its later ones were armed)
+            tc::mbar_drain(&barA, 0, budget);
+            for (int b = 0; b < 2; ++b) {
+                if (loads[b]) tc::mbar_drain(&barB[b], (loads[b] - 1) & 1, budget);
+                if (commits[b]) tc::mbar_drain(&barM[b], (commits[b] - 1) & 1, budget);
+            }
         }
-        s_ok = ok;
-    }
-    __syncthreads();
-    if (s_ok) {
-        // this thread's row of the tile: its C entries are read 16 at a time, each chunk's loads
-        // issued before the previous chunk's stores (the first while the MMAs run)
-        const int R = 32 * warp + lane, row = r0 + I * kTcM + R, ei = sAe[R];
+    } else {
+        // epilogue: row R of the tile, columns c0 .. c0+15 of each 32-column tile
+        const int R = 32 * (warp & 3) + lane, c0 = 16 * (warp >> 2), row = r0 + I * kTcM + R;
+        bool ok = tc::mbar_wait(&barA, 0, ctl, budget);
+        const int ei = ok ? sAe[R] : tc::kExpZero;
         const bool live = row < m && ei != tc::kExpZero;
         const double* crow = F + (size_t)(live ? row : 0);
-        auto load_chunk = [&](int c0, double* cv) {
+        for (int n = 0; n < nt; ++n) {
+            const int b = n & 1, colb = r0 + (J0 + n) * kTcN + c0;
+            double cv[16];
 #pragma unroll
-            for (int j = 0; j < 16; ++j) {
-                const int col = r0 + J * kTcN + c0 + j;
-                cv[j] = live && col <= row ? crow[(size_t)col * m] : 0.0;
-            }
-        };
-        double cv[16];
-        load_chunk(0, cv);
-        const bool got = tc::mbar_wait(&barM, 0, ctl, budget);
-        if (!got) tc::mbar_drain(&barM, 0, budget);
-        tc::fence_after();
-#pragma unroll 1
-        for (int c0 = 0; c0 < kTcN; c0 += 16) {
-            double nx[16];
-            if (c0 + 16 < kTcN) load_chunk(c0 + 16, nx);
+            for (int j = 0; j < 16; ++j) cv[j] = live && colb + j <= row ? crow[(size_t)(colb + j) * m] : 0.0;
+            if (ok) ok = tc::mbar_wait(&barM[b], (n >> 1) & 1, ctl, budget);
+            tc::fence_after();
             long long th[16], tl[16];
 #pragma unroll
             for (int j = 0; j < 16; ++j) th[j] = tl[j] = 0;
-            // diagonals 2..5, then 6..9: four loads in flight per wait
 #pragma unroll
             for (int half = 0; half < 2; ++half) {
                 uint32_t v[4][16];
 #pragma unroll
                 for (int u = 0; u < 4; ++u)
-                    tc::tmem_ld16_async(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(4 * half + u) * kTcN + c0,
+                    tc::tmem_ld16_async(tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)b * tc::kDigits * kTcN +
+                                            (uint32_t)(4 * half + u) * kTcN + c0,
                                         v[u]);
                 tc::tmem_wait_ld();
 #pragma unroll
@@ -434,10 +475,12 @@ __global__ void __launch_bounds__(128, 1) k_fr_syrk_tc(double* __restrict__ aren
                         else tl[j] += a * (1ll << (7 * (3 - u)));            // diagonal k = 6 + u
                     }
             }
-            if (got && live) {
+            tc::fence_before();
+            tc::mbar_arrive(&barE[b]);  // this thread is done with TMEM set b
+            if (ok && live) {
 #pragma unroll
                 for (int j = 0; j < 16; ++j) {
-                    const int col = r0 + J * kTcN + c0 + j, ej = sBe[c0 + j];
+                    const int col = colb + j, ej = sBe[n * kTcN + c0 + j];
                     if (col > row || ej == tc::kExpZero) continue;
                     // sum_k acc_k 2^(-7k) = th 2^-35 + tl 2^-63, each part exact in FP64
                     double v = cv[j];
@@ -446,15 +489,11 @@ __global__ void __launch_bounds__(128, 1) k_fr_syrk_tc(double* __restrict__ aren
                     F[(size_t)row + (size_t)col * m] = v;
                 }
             }
-            if (c0 + 16 < kTcN) {
-#pragma unroll
-                for (int j = 0; j < 16; ++j) cv[j] = nx[j];
-            }
         }
     }
     tc::fence_before();
     __syncthreads();
-    if (warp == 0) tc::tmem_dealloc(tmem, tc::kDigits * kTcN);
+    if (warp == 0) tc::tmem_dealloc(tmem, 2 * tc::kDigits * kTcN);
 }
 
 // U's rows of the listed fronts: one CTA per pivot, row f0 + k (k < w) holds columns S_t[k:]
@@ -711,8 +750,9 @@ extern "C" int sptrsv_factor_multifrontal(int device, int n, const int64_t* a_rp
                 n_trsm.push_back((rest + kTrsmRows - 1) / kTrsmRows);
                 if (use_tc && rest >= kTcMinRest) {
                     const int nI = (rest + kTcM - 1) / kTcM, nJ = (rest + kTcN - 1) / kTcN;
-                    int tiles = 0;
-                    for (int i = 0; i < nI; ++i) tiles += std::min(2 * i + 2, nJ);
+                    const int nC = (nJ + kTcChunk - 1) / kTcChunk;
+                    int tiles = 0;  // CTAs
+                    for (int i = 0; i < nI; ++i) tiles += tc_ctas_of_block(i, nC);
                     updtc.push_back(t);
                     n_split.push_back(2 * nI);
                     n_tc.push_back(tiles);
@@ -825,7 +865,7 @@ extern "C" int sptrsv_factor_multifrontal(int device, int n, const int64_t* a_rp
                         k_fr_split<<<L.total, 256, 0, st>>>(d_arena, ft, lst, pre, L.nlist, L.k0, d_tcbuf);
                         break;
                     case kSyrkTc:
-                        k_fr_syrk_tc<<<L.total, 128, kTcSmem, st>>>(d_arena, ft, lst, pre, L.nlist,
+                        k_fr_syrk_tc<<<L.total, 32 * (kTcEpiWarps + 1), kTcSmem, st>>>(d_arena, ft, lst, pre, L.nlist,
                                                                      d_sched + L.aux + L.nlist, L.k0, d_tcbuf, d_ctl,
                                                                      kDefaultBudgetNs);
                         break;
