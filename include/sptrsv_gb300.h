@@ -219,7 +219,8 @@ SPTRSV_API int sptrsv_set_panels_mode(int mode);
  * update matrix to front_parent[t] > t (-1 for a root).  The host finds every front's row set;
  * the GPU assembles each front (A's entries, its children's update matrices), factors its pivot
  * columns and forms its update matrix in FP64 (blocked in 64-column panels), every front of one
- * tree height in the same launches.  On success *factor holds U on the device in the solver's CSR
+ * tree height in the same launches.  Trailing updates with at least 256 rows go to the tensor
+ * cores as FP64-accurate BF16 digit products (environment SPTRSV_FACTOR_UPDATE=fp64: FP64 FMAs).  On success *factor holds U on the device in the solver's CSR
  * layout (diagonal first, columns ascending), its row pointer on the host, and the supernode
  * partition: each front's pivots in pieces of at most max_width rows, each piece a dense triangle
  * plus one shared set of columns, as sptrsv_set_supernodes takes it.  SPTRSV_ERR_ZERO_PIVOT when a
