@@ -62,12 +62,14 @@ __device__ __forceinline__ void fr_tri(int e, int& i, int& j) {
     j = e - i * (i + 1) / 2;
 }
 
-// arena[idx[q]] = v[q]: A's entries of a level's fronts (idx already holds each front's offset).
-__global__ void k_fr_scatter(double* __restrict__ arena, const int64_t* __restrict__ idx,
-                             const double* __restrict__ v, long long count) {
-    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < count;
-         q += (long long)gridDim.x * blockDim.x)
-        arena[idx[q]] = v[q];
+// A's entries of the listed fronts, one CTA per front: F_t[idx[q]] = v[q] for q in off[t] ..
+// off[t+1]-1 (idx within the front).
+__global__ void k_fr_scatter(double* __restrict__ arena, FrontTab ft, const int* __restrict__ list,
+                             const int64_t* __restrict__ off, const int64_t* __restrict__ idx,
+                             const double* __restrict__ v) {
+    const int t = list[blockIdx.x];
+    double* F = arena + ft.foff[t];
+    for (int64_t q = off[t] + threadIdx.x; q < off[t + 1]; q += blockDim.x) F[idx[q]] = v[q];
 }
 
 // F_p[map[r] + map[s] m] += C[(wc + r) + (wc + s) mc] for s <= r < nu: child c = child[blockIdx.y]
@@ -566,11 +568,16 @@ extern "C" int sptrsv_factor_multifrontal(int device, int n, const int64_t* a_rp
     std::vector<int64_t> a_idx_off(nf + 1, 0), map_start(nf, 0);
     std::vector<int64_t> a_idx;
     std::vector<double> a_v;
+    a_idx.reserve((size_t)(annz / 2 + n));
+    a_v.reserve((size_t)(annz / 2 + n));
     std::vector<int> maps;
     std::vector<int> mark(n, -1), posmap(n, 0);  // posmap: a row's place in the current front
+    std::vector<int> below, merged;
     for (int t = 0; t < nf; ++t) {
         const int f0 = front_start[t], f1 = front_start[t + 1];
-        std::vector<int> below;
+        // rows below the pivots: A's (few, sorted here), merged with each child's update rows
+        // (already sorted), duplicates dropped
+        below.clear();
         for (int p = f0; p < f1; ++p)
             for (int64_t e = a_rp[p]; e < a_rp[p + 1]; ++e) {
                 const int q = a_col[e];
@@ -579,18 +586,24 @@ extern "C" int sptrsv_factor_multifrontal(int device, int n, const int64_t* a_rp
                     below.push_back(q);
                 }
             }
+        std::sort(below.begin(), below.end());
         for (int c : children[t]) {
             const int wc = front_start[c + 1] - front_start[c];
-            for (size_t k = wc; k < S[c].size(); ++k) {
-                const int q = S[c][k];
-                if (q < f0) return SPTRSV_ERR_INVALID_ARG;  // an update row no ancestor pivots
-                if (q >= f1 && mark[q] != t) {
-                    mark[q] = t;
-                    below.push_back(q);
-                }
+            const int* u = S[c].data() + wc;
+            const int* ue = S[c].data() + S[c].size();
+            if (u < ue && *u < f0) return SPTRSV_ERR_INVALID_ARG;  // an update row no ancestor pivots
+            while (u < ue && *u < f1) ++u;                          // the parent's own pivots
+            merged.clear();
+            size_t k = 0;
+            while (k < below.size() || u < ue) {
+                int q;
+                if (u == ue || (k < below.size() && below[k] < *u)) q = below[k++];
+                else if (k < below.size() && below[k] == *u) q = below[k++], ++u;
+                else q = *u++;
+                merged.push_back(q);
             }
+            below.swap(merged);
         }
-        std::sort(below.begin(), below.end());
         std::vector<int>& St = S[t];
         St.reserve((size_t)(f1 - f0) + below.size());
         for (int p = f0; p < f1; ++p) St.push_back(p);
@@ -666,28 +679,13 @@ extern "C" int sptrsv_factor_multifrontal(int device, int n, const int64_t* a_rp
         arena_size = std::max(arena_size, at + size);
         for (int t : level[h]) foff[t] += at;
     }
-    // A's entries by level, each index already offset to its front
-    std::vector<int64_t> sc_idx, lvl_a(H + 1, 0);
-    std::vector<double> sc_v;
-    sc_idx.reserve(a_idx.size());
-    sc_v.reserve(a_v.size());
-    for (int h = 0; h < H; ++h) {
-        for (int t : level[h])
-            for (int64_t q = a_idx_off[t]; q < a_idx_off[t + 1]; ++q) {
-                sc_idx.push_back(foff[t] + a_idx[q]);
-                sc_v.push_back(a_v[q]);
-            }
-        lvl_a[h + 1] = (int64_t)sc_idx.size();
-    }
-    std::vector<int64_t>().swap(a_idx);
-    std::vector<double>().swap(a_v);
     std::vector<int> rows;  // every front's row set, U's column indices
     std::vector<int64_t> soff(nf);
     for (int t = 0; t < nf; ++t) {
         soff[t] = (int64_t)rows.size();
         rows.insert(rows.end(), S[t].begin(), S[t].end());
     }
-    enum { kExtend, kPotrf, kTrsm, kSyrk, kSplit, kSyrkTc, kCopy };
+    enum { kScatter, kExtend, kPotrf, kTrsm, kSyrk, kSplit, kSyrkTc, kCopy };
     struct Launch {
         int kind, k0, nlist, total;  // total: CTAs (kExtend: CTAs per child)
         int64_t list;                // offset of the list in sched; the CTA prefix (nlist + 1) follows it
@@ -716,6 +714,7 @@ extern "C" int sptrsv_factor_multifrontal(int device, int n, const int64_t* a_rp
         launches[h].push_back(L);
     };
     for (int h = 0; h < H; ++h) {
+        add(h, kScatter, 0, level[h], {}, (int)level[h].size());
         // extend-add: the r-th children of the level's fronts in one launch, r = 0, 1, ...
         for (size_t r = 0;; ++r) {
             std::vector<int> kids;
@@ -783,9 +782,10 @@ extern "C" int sptrsv_factor_multifrontal(int device, int n, const int64_t* a_rp
     int rc = 0;
     cudaStream_t st = nullptr;
     int *d_sched = nullptr, *d_fstart = nullptr, *d_fm = nullptr, *d_parent = nullptr, *d_maps = nullptr;
-    int64_t *d_foff = nullptr, *d_mapstart = nullptr, *d_scidx = nullptr, *d_rp = nullptr, *d_soff = nullptr;
+    int64_t *d_foff = nullptr, *d_mapstart = nullptr, *d_aidx = nullptr, *d_aoff = nullptr, *d_rp = nullptr,
+            *d_soff = nullptr;
     int* d_rows = nullptr;
-    double *d_scv = nullptr, *d_arena = nullptr;
+    double *d_av = nullptr, *d_arena = nullptr;
     const int64_t unnz = fct->rp[n];
     int* d_bad = nullptr;
     unsigned char* d_tcbuf = nullptr;
@@ -804,8 +804,6 @@ extern "C" int sptrsv_factor_multifrontal(int device, int n, const int64_t* a_rp
         if (!ck(cudaFuncSetAttribute(k_fr_syrk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)syrk_smem), "attr") ||
             !ck(cudaFuncSetAttribute(k_fr_syrk_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem), "attr"))
             break;
-        int sm_count = 0;
-        if (!ck(cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, device), "attr")) break;
         auto up = [&](auto** d, const auto* h, size_t count) {
             using E = std::remove_pointer_t<std::remove_pointer_t<decltype(d)>>;
             if (!ck(cudaMallocAsync((void**)d, sizeof(E) * std::max<size_t>(1, count), st), "alloc")) return false;
@@ -814,8 +812,9 @@ extern "C" int sptrsv_factor_multifrontal(int device, int n, const int64_t* a_rp
         if (!up(&d_sched, sched.data(), sched.size()) || !up(&d_fstart, front_start, (size_t)nf + 1) ||
             !up(&d_fm, fm.data(), (size_t)nf) || !up(&d_parent, front_parent, (size_t)nf) ||
             !up(&d_maps, maps.data(), maps.size()) || !up(&d_foff, foff.data(), (size_t)nf) ||
-            !up(&d_mapstart, map_start.data(), (size_t)nf) || !up(&d_scidx, sc_idx.data(), sc_idx.size()) ||
-            !up(&d_scv, sc_v.data(), sc_v.size()) || !up(&d_rp, fct->rp.data(), (size_t)n + 1) ||
+            !up(&d_mapstart, map_start.data(), (size_t)nf) || !up(&d_aidx, a_idx.data(), a_idx.size()) ||
+            !up(&d_av, a_v.data(), a_v.size()) || !up(&d_aoff, a_idx_off.data(), (size_t)nf + 1) ||
+            !up(&d_rp, fct->rp.data(), (size_t)n + 1) ||
             !up(&d_rows, rows.data(), rows.size()) || !up(&d_soff, soff.data(), (size_t)nf))
             break;
         // U's arrays outlive the call (plain cudaMalloc: the factor frees them, on any stream)
@@ -841,15 +840,13 @@ extern "C" int sptrsv_factor_multifrontal(int device, int n, const int64_t* a_rp
         const FrontTab ft{d_fstart, d_fm, d_foff};
         for (int h = 0; h < H && !rc; ++h) {
             if (!ck(cudaMemsetAsync(d_arena + lvl_off[h], 0, sizeof(double) * lvl_size[h], st), "memset")) break;
-            const long long na = lvl_a[h + 1] - lvl_a[h];
-            if (na > 0) {
-                const int g = (int)std::min<long long>((long long)sm_count * 8, (na + 255) / 256);
-                k_fr_scatter<<<g, 256, 0, st>>>(d_arena, d_scidx + lvl_a[h], d_scv + lvl_a[h], na);
-            }
             for (const Launch& L : launches[h]) {
                 const int* lst = d_sched + L.list;
                 const int* pre = lst + L.nlist;
                 switch (L.kind) {
+                    case kScatter:
+                        k_fr_scatter<<<L.nlist, 256, 0, st>>>(d_arena, ft, lst, d_aoff, d_aidx, d_av);
+                        break;
                     case kExtend:
                         k_fr_extend_add<<<dim3(L.total, L.nlist), 256, 0, st>>>(d_arena, ft, lst, d_parent, d_maps,
                                                                                  d_mapstart);
@@ -888,7 +885,8 @@ extern "C" int sptrsv_factor_multifrontal(int device, int n, const int64_t* a_rp
     } while (false);
     if (st) {
         for (void* p : {(void*)d_sched, (void*)d_fstart, (void*)d_fm, (void*)d_parent, (void*)d_maps, (void*)d_foff,
-                        (void*)d_mapstart, (void*)d_scidx, (void*)d_scv, (void*)d_rp, (void*)d_rows, (void*)d_soff,
+                        (void*)d_mapstart, (void*)d_aidx, (void*)d_av, (void*)d_aoff, (void*)d_rp, (void*)d_rows,
+                        (void*)d_soff,
                         (void*)d_arena, (void*)d_bad, (void*)d_tcbuf, (void*)d_ctl})
             if (p) cudaFreeAsync(p, st);
         cudaStreamSynchronize(st);
